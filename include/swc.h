@@ -1,0 +1,218 @@
+/*
+ * swc.h -- C ABI of the GB300 (sm_103a) semi-implicit pseudo-spectral step of the
+ * weakly compressible smectic-A / isotropic phase-field model (order parameter psi,
+ * density rho, quasi-static velocity v).
+ *
+ * The reference (smaiso-wcomp.cpp) has no plugin or FFI surface: its time loop is
+ * inline in main(). This header replaces the two internal boundaries of that loop:
+ *
+ *   1. the transform interface -- eight FFTW-MPI r2r plans executed in place on one
+ *      N^3 buffer (smaiso-wcomp.cpp:499-545, fftw_execute at 969-2197), replaced by
+ *      swc_r2r_plan_create / swc_r2r_execute*;
+ *   2. the model state and the loop body -- the std::vector<double> fields in
+ *      (i,j,k) k-fastest layout and one pass of `while (L1 > limL1)`
+ *      (smaiso-wcomp.cpp:1081-2457), replaced by swc_create / swc_set_state /
+ *      swc_step / swc_diagnostics / swc_get_field.
+ *
+ * Conventions
+ *   - Every call returns an int status: SWC_OK (0) or a negative SWC_ERR_* code.
+ *     No C++ exception crosses this boundary.  swc_last_error() gives a message.
+ *   - Host buffers are owned by the caller and copied in/out; the context owns all
+ *     device memory, its CUDA stream and its captured CUDA graphs.
+ *   - A context is single-threaded (one stream); distinct contexts are independent.
+ *   - Layout of every field: row-major (i,j,k) with k fastest,
+ *     index = (i*ny + j)*nz + k (smaiso-wcomp.cpp:943).
+ */
+#ifndef SWC_H
+#define SWC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWC_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------- */
+enum {
+  SWC_OK = 0,
+  SWC_ERR_BAD_PARAM = -1,  /* invalid argument or unsupported grid */
+  SWC_ERR_OOM = -2,        /* device or host allocation failed */
+  SWC_ERR_CUDA = -3,       /* a CUDA runtime call failed */
+  SWC_ERR_NONFINITE = -4,  /* NaN/Inf detected in the state after a step */
+  SWC_ERR_TIMEOUT = -5,    /* host-side watchdog expired waiting for the stream */
+  SWC_ERR_STATE = -6,      /* call out of order (e.g. swc_step before swc_set_state) */
+  SWC_ERR_IO = -7,         /* checkpoint file could not be read or written */
+  SWC_ERR_NO_DEVICE = -8   /* no usable CUDA device */
+};
+
+/* ---- precision of the step ---------------------------------------------- */
+enum {
+  SWC_PREC_FP64 = 0,  /* every transform and pointwise term in FP64 */
+  SWC_PREC_MIXED = 1  /* FP32 transforms/pointwise; FP64 state, CN/AB2 update, reductions */
+};
+
+/* ---- r2r kinds: same definitions as FFTW's REDFT10/REDFT01/RODFT10/RODFT01 --- */
+enum {
+  SWC_REDFT10 = 0,  /* DCT-II : Y_k = 2 sum_n X_n cos(pi (n+1/2) k / N) */
+  SWC_REDFT01 = 1,  /* DCT-III: Y_k = X_0 + 2 sum_{n>=1} X_n cos(pi n (k+1/2) / N) */
+  SWC_RODFT10 = 2,  /* DST-II : Y_k = 2 sum_n X_n sin(pi (n+1/2)(k+1) / N) */
+  SWC_RODFT01 = 3   /* DST-III: Y_k = (-1)^k X_{N-1} + 2 sum_{n<N-1} X_n sin(pi (n+1)(k+1/2) / N) */
+};
+
+/* ---- fields readable with swc_get_field ---------------------------------- */
+enum {
+  SWC_F_PSI = 0,       /* psi_local (real space) */
+  SWC_F_RHO = 1,       /* rho_local */
+  SWC_F_AMP = 2,       /* amp_local: filtered amplitude A */
+  SWC_F_DIVV = 3,      /* divv_local (real space) */
+  SWC_F_VX = 4,        /* vsolx + virrx (real space), "vx.dat" */
+  SWC_F_VY = 5,
+  SWC_F_VZ = 6,
+  SWC_F_VSOLX = 7,     /* solenoidal part, "vsolx.dat" (last step of a swc_step call) */
+  SWC_F_VSOLY = 8,
+  SWC_F_VSOLZ = 9,
+  SWC_F_ENERGY = 10,   /* energy density of the diagnostic, "energyMid.dat" source */
+  SWC_F_PSIQ = 11,     /* psiq_local: scaled DCT-II of psi */
+  SWC_F_PSIQ_OLD = 12, /* psiq_old_local */
+  SWC_F_NLQ = 13,      /* Nl_local after its DCT-II (becomes Nl_old next step) */
+  SWC_F_FRHO = 14,     /* f_rho_local: previous density source (AB2) */
+  SWC_F_LPSI = 15,     /* dfDlapPsi_local = alpha (q0^2 + lap) psi */
+  SWC_F_MU = 16,       /* mu_local */
+  SWC_F_GPSIX = 17,    /* psiGrad{x,y,z}_local (real space) */
+  SWC_F_GPSIY = 18,
+  SWC_F_GPSIZ = 19,
+  SWC_F_GRHOX = 20,    /* rhoD{x,y,z}_local (real space) */
+  SWC_F_GRHOY = 21,
+  SWC_F_GRHOZ = 22,
+  SWC_F_PSI_OLD = 23,  /* psi_old_local at the last step of a swc_step call */
+  SWC_F_COUNT = 24
+};
+
+/* ---- model and run parameters (smaiso-wcomp.cpp:206-278) ------------------ */
+typedef struct swc_params {
+  int nx, ny, nz;     /* grid (reference: 512^3, :218); powers of two, 8..1024 */
+  int nw;             /* points per wavelength: dx = 2 pi / (q0 nw)  (:261, :267) */
+  double dt;          /* time step (:262) */
+  double alpha;       /* (:241) */
+  double beta;        /* cubic coefficient (:240) */
+  double gamma;       /* quintic coefficient (:239) */
+  double ep;          /* epsilon, already signed: reference ep = -0.001*argv[2] (:243) */
+  double q0;          /* smectic wavenumber (:244) */
+  double nu;          /* shear viscosity, reference argv[1] (:249) */
+  double lambda;      /* second viscosity (:256) */
+  double zeta;        /* density penalty (:257) */
+  double rho_0;       /* isotropic density (:251); kp = (1-rho_0)/Amp (:253) */
+  int divv_switch;    /* relax-phase length in steps (:214, reference 50) */
+  int load;           /* reference load flag: 1 skips the relax phase (:176, :1312) */
+  int ref_ranks;      /* MPI rank count of the reference run reproduced (x slabs);
+                         decides where the slab-start v_z filter applies (:1760-1804
+                         vs :1932). Must divide nx. Reference needs an even count. */
+  int precision;      /* SWC_PREC_FP64 or SWC_PREC_MIXED */
+  int device;         /* CUDA device ordinal */
+  double watchdog_s;  /* host watchdog per swc_step call in seconds (<=0: none) */
+} swc_params;
+
+/* Diagnostics of the last step of a swc_step call (smaiso-wcomp.cpp:2202-2262). */
+typedef struct swc_diag {
+  double l1;          /* sum|psi-psi_old| / (dt sum|psi|)        (:2246) */
+  double mass;        /* sum rho * dx^3                          (:2252) */
+  double energy;      /* free energy * dx^3                      (:2258) */
+  double sum_abs_dpsi;
+  double sum_abs_psi;
+  double sum_rho;
+  double sum_energy;
+  int64_t step;       /* nLoop after the call */
+  int64_t nonfinite;  /* count of non-finite psi/rho values */
+} swc_diag;
+
+typedef struct swc_ctx swc_ctx;
+typedef struct swc_r2r_plan swc_r2r_plan;
+
+/* Library / error helpers. */
+int swc_abi_version(void);
+const char* swc_strerror(int status);
+/* Message of the last failing call on this thread (empty string if none). */
+const char* swc_last_error(void);
+
+/* Fill *p with the reference's hard-coded values (smaiso-wcomp.cpp:206-278) for
+ * a grid of nx x ny x nz, with nu = 1 and argv[2] = 1 (ep = -0.001). */
+int swc_default_params(swc_params* p, int nx, int ny, int nz);
+
+/* Derived constants exactly as the reference computes them (:239-272). */
+typedef struct swc_derived {
+  double amp;    /* Amp = sqrt((3 beta + sqrt(9 beta^2 + 40 ep gamma))/5) */
+  double kp;     /* (1 - rho_0)/Amp */
+  double rho_s;  /* kp Amp + rho_0 */
+  double rho_m;  /* rho_s / 2 */
+  double dx, dy, dz, lx, ly, lz;
+  double scale;  /* 0.125/(nx ny nz) */
+} swc_derived;
+int swc_derive(const swc_params* p, swc_derived* out);
+
+/* ---- the time loop (replaces smaiso-wcomp.cpp:968-2262) -------------------- */
+
+/* Validate *p, allocate the device state and capture nothing yet. */
+int swc_create(const swc_params* p, swc_ctx** out);
+int swc_destroy(swc_ctx* ctx);
+
+/* Copy the initial psi (and rho; NULL means the reference's zero fill, :1053)
+ * from host memory and run the pre-loop (:968-1010): psiq = scale*DCT(psi),
+ * psi = iDCT(psiq), psiq_old = psiq, step counter = 0. */
+int swc_set_state(swc_ctx* ctx, const double* psi, const double* rho);
+
+/* Advance nsteps time steps (each one loop body :1084-2198). The last step of
+ * the call also computes the diagnostics of :2202-2262 and the solenoidal
+ * velocity. Steps run as captured CUDA graphs on the context's stream; the call
+ * returns after the stream is idle. Returns SWC_ERR_NONFINITE if the state holds
+ * NaN/Inf afterwards. */
+int swc_step(swc_ctx* ctx, int nsteps);
+
+/* Read the diagnostics of the last swc_step call. */
+int swc_diagnostics(swc_ctx* ctx, swc_diag* out);
+
+/* Copy one field (SWC_F_*) to host memory as nx*ny*nz doubles. */
+int swc_get_field(swc_ctx* ctx, int field, double* dst);
+
+/* Device pointer of a field in the context's own precision (8-byte elements for
+ * FP64 fields, 4-byte for FP32 work fields of the mixed path); *elem_bytes tells
+ * which. Valid until swc_destroy. */
+int swc_field_device_ptr(swc_ctx* ctx, int field, void** dev_ptr, int* elem_bytes);
+
+/* Step counter (nLoop of the reference). */
+int swc_get_step(swc_ctx* ctx, int64_t* nloop);
+
+/* Elapsed device time (ms) of the kernels of the last swc_step call, measured
+ * with CUDA events on the context's stream. */
+int swc_last_step_ms(swc_ctx* ctx, double* ms);
+
+/* ---- full-state checkpoint (lossless; the reference's psi<rank>.dat text dump
+ *      at :2334-2345 keeps only psi at 6 digits) ------------------------------ */
+int swc_save(swc_ctx* ctx, const char* path);
+int swc_load(swc_ctx* ctx, const char* path);
+
+/* ---- r2r transforms (replaces fftw_mpi_plan_r2r_3d + fftw_execute,
+ *      smaiso-wcomp.cpp:499-545) --------------------------------------------- */
+
+/* Plan a 3D r2r transform of an nx x ny x nz array with one SWC_REDFT10/01,
+ * SWC_RODFT10/01 kind per axis (kx along x = slowest index). precision selects
+ * double (SWC_PREC_FP64) or float (SWC_PREC_MIXED) data. Unnormalised, like FFTW:
+ * a forward/inverse pair multiplies by 2n per axis. */
+int swc_r2r_plan_create(int nx, int ny, int nz, int kx, int ky, int kz, int precision,
+                        swc_r2r_plan** out);
+int swc_r2r_plan_destroy(swc_r2r_plan* plan);
+
+/* In-place execution on device memory (double* or float* per the plan), enqueued
+ * on `stream` (a cudaStream_t; NULL = legacy default stream). Allocates nothing. */
+int swc_r2r_execute(swc_r2r_plan* plan, void* dev_inout, void* stream);
+
+/* Host convenience: copies in, transforms, copies out (out may equal in). The
+ * data is double on the host for both precisions. */
+int swc_r2r_execute_host(swc_r2r_plan* plan, const double* in, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWC_H */

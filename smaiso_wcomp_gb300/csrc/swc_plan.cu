@@ -1,0 +1,166 @@
+// swc_plan.cu -- r2r transform plans: the drop-in for fftw_mpi_plan_r2r_3d +
+// fftw_execute (smaiso-wcomp.cpp:499-545) on one GPU. A 3D transform is three
+// in-place axis passes (z, y, x); the plan owns only its twiddle tables.
+#include <cuda_runtime.h>
+
+#include <new>
+#include <vector>
+
+#include "swc_engine.h"
+#include "swc_r2r.cuh"
+#include "swc_tables.cuh"
+
+using namespace swc;
+
+struct swc_r2r_plan {
+  Grid g;
+  int kind[3];
+  int precision;
+  int device;
+  std::vector<void*> allocs;
+  R2RTables<double> td[3];
+  R2RTables<float> tf[3];
+};
+
+namespace {
+
+template <typename T>
+int upload_tables(swc_r2r_plan* p, int axis, int n, R2RTables<T>* out) {
+  HostTables<T> ht(n);
+  const std::vector<T>* src[3] = {&ht.fft, &ht.post, &ht.pre};
+  const cx_t<T>** dst[3] = {&out->fft, &out->post, &out->pre};
+  for (int q = 0; q < 3; ++q) {
+    void* ptr = nullptr;
+    const size_t bytes = src[q]->size() * sizeof(T);
+    if (cudaMalloc(&ptr, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc for r2r tables failed");
+      return SWC_ERR_OOM;
+    }
+    p->allocs.push_back(ptr);
+    if (cudaMemcpy(ptr, src[q]->data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+      set_error("uploading r2r tables failed");
+      return SWC_ERR_CUDA;
+    }
+    *dst[q] = (const cx_t<T>*)ptr;
+  }
+  (void)axis;
+  return SWC_OK;
+}
+
+template <typename T> cudaError_t run_axis(const swc_r2r_plan* p, int axis, T* data, cudaStream_t s) {
+  const R2RTables<T>& tb = std::is_same<T, double>::value ? *(const R2RTables<T>*)&p->td[axis]
+                                                          : *(const R2RTables<T>*)&p->tf[axis];
+  // FFTW kind -> kernel kind: REDFT10 = DCT-II, REDFT01 = DCT-III, RODFT10 = DST-II, RODFT01 = DST-III
+  const LdPlain<T, T> ld{data};
+  const StPlain<T, T> st{data};
+  switch (p->kind[axis]) {
+    case SWC_REDFT10: return launch_pass<T, K_C2>(p->g, axis, tb, s, ld, st, NoMul<T>());
+    case SWC_REDFT01: return launch_pass<T, K_C3>(p->g, axis, tb, s, ld, st, NoMul<T>());
+    case SWC_RODFT10: return launch_pass<T, K_S2>(p->g, axis, tb, s, ld, st, NoMul<T>());
+    default: return launch_pass<T, K_S3>(p->g, axis, tb, s, ld, st, NoMul<T>());
+  }
+}
+
+template <typename T> int execute(const swc_r2r_plan* p, void* dev, cudaStream_t s) {
+  for (int axis = 2; axis >= 0; --axis) {
+    cudaError_t e = run_axis<T>(p, axis, (T*)dev, s);
+    if (e != cudaSuccess) {
+      set_error("r2r pass failed: %s", cudaGetErrorString(e));
+      return SWC_ERR_CUDA;
+    }
+  }
+  return SWC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swc_r2r_plan_create(int nx, int ny, int nz, int kx, int ky, int kz, int precision, swc_r2r_plan** out) {
+  if (!out) { set_error("out is NULL"); return SWC_ERR_BAD_PARAM; }
+  *out = nullptr;
+  const int dims[3] = {nx, ny, nz}, kinds[3] = {kx, ky, kz};
+  for (int a = 0; a < 3; ++a) {
+    if (!is_pow2(dims[a]) || dims[a] < 4 || dims[a] > 1024) {
+      set_error("r2r extent %d: must be a power of two in [4, 1024]", dims[a]);
+      return SWC_ERR_BAD_PARAM;
+    }
+    if (kinds[a] < SWC_REDFT10 || kinds[a] > SWC_RODFT01) {
+      set_error("unknown r2r kind %d", kinds[a]);
+      return SWC_ERR_BAD_PARAM;
+    }
+  }
+  if (precision != SWC_PREC_FP64 && precision != SWC_PREC_MIXED) {
+    set_error("precision must be SWC_PREC_FP64 or SWC_PREC_MIXED");
+    return SWC_ERR_BAD_PARAM;
+  }
+  int dev = 0, ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("no CUDA device");
+    return SWC_ERR_NO_DEVICE;
+  }
+  swc_r2r_plan* p = new (std::nothrow) swc_r2r_plan();
+  if (!p) { set_error("host allocation failed"); return SWC_ERR_OOM; }
+  p->g.nx = nx; p->g.ny = ny; p->g.nz = nz;
+  p->g.lx = ilog2(nx); p->g.ly = ilog2(ny); p->g.lz = ilog2(nz);
+  p->g.ng = (long long)nx * ny * nz;
+  p->precision = precision;
+  p->device = dev;
+  for (int a = 0; a < 3; ++a) {
+    p->kind[a] = kinds[a];
+    const int rc = precision == SWC_PREC_FP64 ? upload_tables<double>(p, a, dims[a], &p->td[a])
+                                              : upload_tables<float>(p, a, dims[a], &p->tf[a]);
+    if (rc) { swc_r2r_plan_destroy(p); return rc; }
+  }
+  *out = p;
+  return SWC_OK;
+}
+
+int swc_r2r_plan_destroy(swc_r2r_plan* p) {
+  if (!p) return SWC_OK;
+  for (void* a : p->allocs) cudaFree(a);
+  delete p;
+  return SWC_OK;
+}
+
+int swc_r2r_execute(swc_r2r_plan* p, void* dev_inout, void* stream) {
+  if (!p || !dev_inout) { set_error("NULL plan or buffer"); return SWC_ERR_BAD_PARAM; }
+  cudaStream_t s = (cudaStream_t)stream;
+  return p->precision == SWC_PREC_FP64 ? execute<double>(p, dev_inout, s) : execute<float>(p, dev_inout, s);
+}
+
+int swc_r2r_execute_host(swc_r2r_plan* p, const double* in, double* out) {
+  if (!p || !in || !out) { set_error("NULL argument"); return SWC_ERR_BAD_PARAM; }
+  const size_t n = (size_t)p->g.ng;
+  const size_t elem = p->precision == SWC_PREC_FP64 ? sizeof(double) : sizeof(float);
+  void* dev = nullptr;
+  if (cudaMalloc(&dev, n * elem) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc for r2r data failed");
+    return SWC_ERR_OOM;
+  }
+  int rc = SWC_OK;
+  std::vector<float> tmp;
+  if (elem == sizeof(double)) {
+    if (cudaMemcpy(dev, in, n * elem, cudaMemcpyHostToDevice) != cudaSuccess) rc = SWC_ERR_CUDA;
+  } else {
+    tmp.assign(in, in + n);
+    if (cudaMemcpy(dev, tmp.data(), n * elem, cudaMemcpyHostToDevice) != cudaSuccess) rc = SWC_ERR_CUDA;
+  }
+  if (!rc) rc = swc_r2r_execute(p, dev, nullptr);
+  if (!rc) {
+    if (elem == sizeof(double)) {
+      if (cudaMemcpy(out, dev, n * elem, cudaMemcpyDeviceToHost) != cudaSuccess) rc = SWC_ERR_CUDA;
+    } else {
+      if (cudaMemcpy(tmp.data(), dev, n * elem, cudaMemcpyDeviceToHost) != cudaSuccess) rc = SWC_ERR_CUDA;
+      else for (size_t i = 0; i < n; ++i) out[i] = tmp[i];
+    }
+  }
+  if (rc == SWC_ERR_CUDA) set_error("r2r host execution: CUDA copy failed");
+  cudaFree(dev);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,1003 @@
+// swc_step_impl.cuh -- the time step of smaiso-wcomp.cpp (loop body REF:1084-2198,
+// diagnostics REF:2202-2262) as a sequence of sm_103a kernels, templated on the work
+// precision T. The state that carries the scheme's stability and conservation --
+// psiq, psiq_old (the CN/AB2 psi update), rho and its AB2 source f_rho -- is FP64 in
+// both engines; the FP64 engine (T = double) computes everything else in FP64 too,
+// the mixed engine (T = float) runs transforms and pointwise terms in FP32.
+//
+// Reorganisation relative to the reference (same mathematics, FP64 rounding only):
+//  * v = vsol + virr is transformed once per component (REF:2093-2117 transforms
+//    vsol and virr separately and only their sums enter REF:2128-2160); vsol alone
+//    is transformed on the last step of a swc_step call, for output.
+//  * grad.f (ampDgradpsi, REF:2078, 2090) enters Nl only, which is transformed back
+//    by DCT-II (REF:2167); DCT-II^3 o DCT-III^3 = (1/scale) I, so the spectral
+//    divergence is subtracted from the transformed Nl instead of transforming twice.
+//  * the Gaussian factor exp(-1.57^2 2 |q|^2) (REF:1281, 1486, 1603...) is the product
+//    of three per-axis tables; CM1/CM2 are recomputed from the wavenumbers instead
+//    of being read from nine N^3 tables (REF:936-963).
+//  * a forward transform, a spectral multiplier and an inverse transform along the
+//    last axis are one "filter" pass (S3 amplitude filter, S5 Laplacian).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "swc_engine.h"
+#include "swc_r2r.cuh"
+#include "swc_tables.cuh"
+
+namespace swc {
+
+#define SWC_CK(call)                                                                      \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return SWC_ERR_CUDA;                                                                \
+    }                                                                                     \
+  } while (0)
+
+// ---------------------------------------------------------------------------------
+// Load / store / multiplier functors fused into the transform passes
+// ---------------------------------------------------------------------------------
+
+// Shifted spectral derivative onto the sine grid of `axis` (REF:1166-1221):
+// out = -fac * Vs[c] * spec[c + 1], 0 on the last mode of the axis.
+template <typename T, typename U> struct LdGrad {
+  const U* spec;
+  const T* vs;
+  T fac;
+  int axis;
+  int nlast;
+  long long shift;
+  __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
+    const int c = axis == 0 ? i : (axis == 1 ? j : k);
+    if (c >= nlast) return (T)0;
+    return -fac * vs[c] * (T)spec[idx + shift];
+  }
+};
+
+// |psi| amplitude before filtering (REF:1262-1266).
+template <typename T> struct LdAmp {
+  const T *psi, *gx, *gy, *gz;
+  T q02;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
+    const T p = psi[idx], a = gx[idx], b = gy[idx], c = gz[idx];
+    return sqrt(q02 * (p * p) + (a * a) + (b * b) + (c * c));
+  }
+};
+
+// scale * exp(-1.57^2 * 2 * |q|^2) as a product of per-axis tables (REF:1280-1281).
+template <typename T> struct MulGauss {
+  const T *gx, *gy, *gz;
+  T scale;
+  __device__ __forceinline__ T operator()(int i, int j, int k) const { return scale * gx[i] * gy[j] * gz[k]; }
+};
+
+// -scale * |q|^2 (REF:1333-1334).
+template <typename T> struct MulLap {
+  const T *qx, *qy, *qz;
+  T scale;
+  __device__ __forceinline__ T operator()(int i, int j, int k) const {
+    const T a = qx[i], b = qy[j], c = qz[k];
+    return -scale * ((a * a) + (b * b) + (c * c));
+  }
+};
+
+// alpha (q0^2 - |q|^2) psiq (REF:1302).
+template <typename T> struct LdLpsi {
+  const double* psiq;
+  const T *qx, *qy, *qz;
+  T alpha, q02;
+  __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
+    const T a = qx[i], b = qy[j], c = qz[k];
+    const T mq2 = (a * a) + (b * b) + (c * c);
+    return alpha * (q02 - mq2) * (T)psiq[idx];
+  }
+};
+
+// relax phase: -|q|^2 alpha (q0^2 - |q|^2) psiq (REF:1356-1357).
+template <typename T> struct LdRelaxLap {
+  const double* psiq;
+  const T *qx, *qy, *qz;
+  T alpha, q02;
+  __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
+    const T a = qx[i], b = qy[j], c = qz[k];
+    const T mq2 = (a * a) + (b * b) + (c * c);
+    return -mq2 * alpha * (q02 - mq2) * (T)psiq[idx];
+  }
+};
+
+// rho * dfDlapPsi (REF:1321).
+template <typename T> struct LdRhoL {
+  const double* rho;
+  const T* lpsi;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)rho[idx] * lpsi[idx]; }
+};
+
+template <typename T> struct LdSum2 {
+  const T *a, *b;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return a[idx] + b[idx]; }
+};
+
+// First pass of the Nl transform: density AB2 update (REF:2121-2139) and the real
+// space Nl of REF:2153-2160 without the grad.f term (subtracted in spectral space).
+template <typename T> struct LdNl {
+  const T *vx, *vy, *vz, *grx, *gry, *grz, *divv, *mu, *amp, *psi, *gpx, *gpy, *gpz;
+  double *rho, *frho;
+  double dt, kp, zeta, rho0;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
+    const T ux = vx[idx], uy = vy[idx], uz = vz[idx];
+    const double r = rho[idx];
+    const T srho = -ux * grx[idx] - uy * gry[idx] - uz * grz[idx] - (T)r * divv[idx];
+    const double rn = r + dt * (1.5 * (double)srho - 0.5 * frho[idx]);
+    rho[idx] = rn;
+    frho[idx] = (double)srho;
+    const T a = amp[idx];
+    const T c = ((T)kp * (T)zeta / (a + (T)0.001)) * ((T)rn - (T)rho0 - (T)kp * a) * psi[idx];
+    return -mu[idx] + c - ux * gpx[idx] - uy * gpy[idx] - uz * gpz[idx];
+  }
+};
+
+// Last pass of the Nl transform: Nlq = DCT(Nl) - q.f, then the CN/AB2 update of psiq
+// (REF:2170-2190). FP64 engine: the reference's expression; mixed engine: the same
+// update in increment form psiq + (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
+// which follows from C1 - C2 = 1/2 and avoids cancelling C1 psiq against psiq_old.
+template <typename T> struct StNlUpdate {
+  const T* dq;
+  double *psiq, *psiq_old;
+  T* nlq;
+  const double *qx, *qy, *qz;
+  double ep, alpha, q02, dt, rho_m, dtd2, scale;
+  int first;
+  int increment;
+  __device__ __forceinline__ void operator()(int i, int j, int k, long long idx, T v) const {
+    const T nl = v - dq[idx];
+    const T nlo = first ? nl : nlq[idx];
+    const double a = qx[i], b = qy[j], c = qz[k];
+    const double mq2 = a * a + b * b + c * c;
+    const double s = q02 - mq2;
+    const double aLin = ep - alpha * (s * s);
+    const double C1 = (2.0 - dt * rho_m * aLin);
+    const double C2 = (1.5 - dt * rho_m * aLin);
+    const double pq = psiq[idx], pqo = psiq_old[idx];
+    const double src = dtd2 * scale * (3.0 * (double)nl - (double)nlo);
+    double pn;
+    if (increment) pn = pq + (0.5 * (pq - pqo) + src) / C2;
+    else pn = (C1 * pq - 0.5 * pqo + src) / C2;
+    psiq_old[idx] = pq;
+    psiq[idx] = pn;
+    nlq[idx] = nl;
+  }
+};
+
+// ---------------------------------------------------------------------------------
+// Pointwise kernels
+// ---------------------------------------------------------------------------------
+
+__device__ __forceinline__ void decompose(const Grid& g, long long idx, int& i, int& j, int& k) {
+  k = (int)(idx & (g.nz - 1));
+  j = (int)((idx >> g.lz) & (g.ny - 1));
+  i = (int)(idx >> (g.ly + g.lz));
+}
+
+// S5 relax tail + S6 (REF:1363-1425): stresses, chemical potential, forces.
+template <typename T> struct S6Args {
+  const T *lapR, *lpsi, *psi, *amp, *gpx, *gpy, *gpz, *grx, *gry, *grz;
+  double* rho;
+  T *fgrad, *ener, *Sx, *Sy, *Sz, *fx, *fy, *fz, *mu;
+  double ep, beta, gamma, zeta, kp, rho0, amp_eq;
+  int relax;
+};
+
+template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S6Args<T> a) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.ng) return;
+  double r = a.rho[idx];
+  const T A = a.amp[idx];
+  T lapR = a.lapR[idx];
+  if (a.relax) {
+    // REF:1371-1374: rho reset to rho_0 + kp A during the relax phase
+    const double rho1 = a.rho0;
+    r = rho1 + ((1 - rho1) / a.amp_eq) * (double)A;
+    a.rho[idx] = r;
+    lapR = (T)r * lapR;
+  }
+  const T rr = (T)r;
+  const T L = a.lpsi[idx];
+  const T p = a.psi[idx];
+  const T E = (T)0.5 * (L * L);
+  const T t = (T)a.rho0 + (T)a.kp * A;
+  a.fgrad[idx] = (T)0.5 * (T)a.zeta * (rr * rr - t * t);
+  const T mu1 = lapR + rr * L;
+  const T gpx = a.gpx[idx], gpy = a.gpy[idx], gpz = a.gpz[idx];
+  a.Sx[idx] = mu1 * gpx + E * a.grx[idx];
+  a.Sy[idx] = mu1 * gpy + E * a.gry[idx];
+  a.Sz[idx] = mu1 * gpz + E * a.grz[idx];
+  const T p2 = p * p;
+  a.mu[idx] = lapR + rr * (L - (T)a.ep * p - (T)a.beta * (p2 * p) + (T)a.gamma * (p2 * p2 * p));
+  a.ener[idx] = rr * E;
+  const T c = (T)a.kp * (T)a.zeta * (rr - (T)a.rho0 - (T)a.kp * A) / (A + (T)0.001);
+  a.fx[idx] = c * gpx;
+  a.fy[idx] = c * gpy;
+  a.fz[idx] = c * gpz;
+}
+
+// S8 + S9 (REF:1479-1974): Stokes solve on the three staggered grids, spectral.
+template <typename T> struct StokesArgs {
+  const T *Sx, *Sy, *Sz, *fgrad, *ener;
+  T *vsolx, *vsoly, *vsolz, *virrx, *virry, *virrz;
+  const T *vqx, *vqy, *vqz, *vsx, *vsy, *vsz;  // wavenumbers
+  const T *gqx, *gqy, *gqz, *gsx, *gsy, *gsz;  // exp(-1.57^2 2 q^2) per axis
+  T scale, nu, lam2nu;
+  int block;  // x-slab size of the reference decomposition (REF:299)
+};
+
+template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid g, StokesArgs<T> a) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.ng) return;
+  int i, j, k;
+  decompose(g, idx, i, j, k);
+  const long long sx = 1LL << (g.ly + g.lz), sy = g.nz;
+  const T Sxc = a.Sx[idx], Syc = a.Sy[idx], Szc = a.Sz[idx];
+  const T qxi = a.vqx[i], qyj = a.vqy[j], qzk = a.vqz[k];
+  // v_x on the x-sine grid, i < nx-1 (REF:1581-1699)
+  T vs = 0, vi = 0;
+  if (i < g.nx - 1) {
+    const T sxi = a.vsx[i];
+    const T Sy = (j != 0) ? a.Sy[idx + sx - sy] : (T)0;
+    const T Sz = (k != 0) ? a.Sz[idx + sx - 1] : (T)0;
+    const T dot = sxi * Sxc + qyj * Sy + qzk * Sz;
+    const T mq2 = sxi * sxi + qyj * qyj + qzk * qzk;
+    const T CM1 = a.scale / mq2, CM2 = sxi / mq2;
+    const long long n1 = idx + sx;
+    const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i + 1] * a.gqy[j] * a.gqz[k]);
+    vs = (CM1 / a.nu) * (Sxc - CM2 * dot);
+    vi = (CM1 / a.lam2nu) * (sxi * fg + CM2 * dot * (a.gsx[i] * a.gqy[j] * a.gqz[k]));
+  }
+  a.vsolx[idx] = vs;
+  a.virrx[idx] = vi;
+  // v_y, v_z for j < ny-1, k < nz-1 (REF:1758-1974); other modes stay 0
+  T ys = 0, yi = 0, zs = 0, zi = 0;
+  if (j < g.ny - 1 && k < g.nz - 1) {
+    const T syj = a.vsy[j], szk = a.vsz[k];
+    {
+      const T Sx = (i > 0) ? a.Sx[idx - sx + sy] : (T)0;
+      const T Sz = (k != 0) ? a.Sz[idx + sy - 1] : (T)0;
+      const T dot = qxi * Sx + syj * Syc + qzk * Sz;
+      const T mq2 = qxi * qxi + syj * syj + qzk * qzk;
+      const T CM1 = a.scale / mq2, CM2 = syj / mq2;
+      const long long n1 = idx + sy;
+      const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i] * a.gqy[j + 1] * a.gqz[k]);
+      ys = (CM1 / a.nu) * (Syc - CM2 * dot);
+      yi = (CM1 / a.lam2nu) * (syj * fg + CM2 * dot * (a.gqx[i] * a.gsy[j] * a.gqz[k]));
+    }
+    {
+      const T Sx = (i > 0) ? a.Sx[idx - sx + 1] : (T)0;
+      const T Sy = (j != 0) ? a.Sy[idx - sy + 1] : (T)0;
+      const T dot = qxi * Sx + qyj * Sy + szk * Szc;
+      const T mq2 = qxi * qxi + qyj * qyj + szk * szk;
+      const T CM1 = a.scale / mq2, CM2 = szk / mq2;
+      const long long n1 = idx + 1;
+      const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i] * a.gqy[j] * a.gqz[k + 1]);
+      // REF:1932: off the first slab of a rank, the k = 0, j > 0 modes use CM1y's filter
+      const bool q1 = (k == 0) && (j > 0) && (i % a.block != 0);
+      const T G = q1 ? (a.gqx[i] * a.gsy[j] * a.gqz[k]) : (a.gqx[i] * a.gqy[j] * a.gsz[k]);
+      zs = (CM1 / a.nu) * (Szc - CM2 * dot);
+      zi = (CM1 / a.lam2nu) * (szk * fg + CM2 * dot * G);
+    }
+  }
+  a.vsoly[idx] = ys;
+  a.virry[idx] = yi;
+  a.vsolz[idx] = zs;
+  a.virrz[idx] = zi;
+}
+
+// S10 (REF:2042-2079): div v and q.f on the cosine grid (q.f without `scale`).
+template <typename T> struct DivArgs {
+  const T *virrx, *virry, *virrz, *fx, *fy, *fz;
+  T *divv, *dq;
+  const T *vqx, *vqy, *vqz;
+};
+template <typename T> __global__ void __launch_bounds__(256) div_kernel(Grid g, DivArgs<T> a) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.ng) return;
+  int i, j, k;
+  decompose(g, idx, i, j, k);
+  const long long sx = 1LL << (g.ly + g.lz), sy = g.nz;
+  const T vx = (i > 0) ? a.virrx[idx - sx] : (T)0, fx = (i > 0) ? a.fx[idx - sx] : (T)0;
+  const T vy = (j > 0) ? a.virry[idx - sy] : (T)0, fy = (j > 0) ? a.fy[idx - sy] : (T)0;
+  const T vz = (k > 0) ? a.virrz[idx - 1] : (T)0, fz = (k > 0) ? a.fz[idx - 1] : (T)0;
+  const T qx = a.vqx[i], qy = a.vqy[j], qz = a.vqz[k];
+  a.divv[idx] = qx * vx + qy * vy + qz * vz;
+  a.dq[idx] = qx * fx + qy * fy + qz * fz;
+}
+
+// S15 (REF:2214-2231): per-block partial sums of |psi - psi_old|, |psi|, rho, the
+// free energy density and the non-finite count; also rotates psi_old <- psi <- psi_new
+// and writes the energy density field.
+template <typename T> struct DiagArgs {
+  const T *psi_new, *lpsi, *amp;
+  T *psi, *psi_old, *energy;
+  const double* rho;
+  double* partial;  // 5 doubles per block
+  double ep, beta, gamma, zeta, rho0, kp;
+};
+constexpr int kDiagThreads = 256;
+
+template <typename T> __global__ void __launch_bounds__(kDiagThreads) diag_kernel(Grid g, DiagArgs<T> a) {
+  __shared__ double sh[5][kDiagThreads / 32];
+  double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.ng;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double pn = (double)a.psi_new[idx];
+    const double po = (double)a.psi[idx];
+    const double r = a.rho[idx];
+    const double L = (double)a.lpsi[idx];
+    const double A = (double)a.amp[idx];
+    s0 += fabs(pn - po);
+    s1 += fabs(pn);
+    s2 += r;
+    const double p2 = pn * pn;
+    const double e = -0.5 * a.ep * p2 + 0.5 * (L * L) - 0.25 * a.beta * (p2 * p2) + (a.gamma / 6) * (p2 * p2 * p2);
+    const double d = r - a.rho0 - a.kp * A;
+    s3 += r * e + 0.5 * a.zeta * (d * d);
+    s4 += (double)(!isfinite(pn)) + (double)(!isfinite(r));
+    a.energy[idx] = (T)e;
+    a.psi_old[idx] = a.psi[idx];
+    a.psi[idx] = a.psi_new[idx];
+  }
+  double v[5] = {s0, s1, s2, s3, s4};
+#pragma unroll
+  for (int q = 0; q < 5; ++q)
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0)
+    for (int q = 0; q < 5; ++q) sh[q][w] = v[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 5; ++q) {
+      double t = 0;
+      for (int ww = 0; ww < kDiagThreads / 32; ++ww) t += sh[q][ww];
+      a.partial[5 * blockIdx.x + q] = t;
+    }
+  }
+}
+
+// Deterministic final sum of the per-block partials (one block, fixed order).
+static __global__ void __launch_bounds__(32) diag_final_kernel(const double* partial, int nblocks, double* out) {
+  const int q = threadIdx.x;
+  if (q < 5) {
+    double t = 0;
+    for (int b = 0; b < nblocks; ++b) t += partial[5 * b + q];
+    out[q] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Engine
+// ---------------------------------------------------------------------------------
+
+template <typename T> struct DevTables {
+  R2RTables<T> t[3];  // per axis
+};
+
+template <typename T> class StepEngine : public EngineBase {
+ public:
+  explicit StepEngine(const swc_params& p) : p_(p) {}
+  ~StepEngine() override { release(); }
+
+  int init();
+  int set_state(const double* psi, const double* rho) override;
+  int step(int nsteps) override;
+  int diagnostics(swc_diag* out) override {
+    *out = diag_;
+    return SWC_OK;
+  }
+  int get_field(int field, double* dst) override;
+  int field_ptr(int field, void** ptr, int* elem_bytes) override;
+  int get_step(int64_t* n) override {
+    *n = nloop_;
+    return SWC_OK;
+  }
+  int last_ms(double* ms) override {
+    *ms = last_ms_;
+    return SWC_OK;
+  }
+  int save(const char* path) override;
+  int load(const char* path) override;
+
+ private:
+  // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
+  template <typename U, int KIND, class LD, class ST, class MUL = NoMul<U>>
+  int passU(int axis, LD ld, ST st, MUL mul = MUL());
+  template <int KIND, class LD, class ST, class MUL = NoMul<T>>
+  int pass(int axis, LD ld, ST st, MUL mul = MUL()) {
+    return passU<T, KIND, LD, ST, MUL>(axis, ld, st, mul);
+  }
+  template <typename U> R2RTables<U> tabs(int a) const {
+    if constexpr (std::is_same<U, T>::value) return tab_.t[a];
+    else return tabd_.t[a];
+  }
+  int enqueue_step(bool relax, bool first, bool diag);
+  int run_graph(bool relax, bool first, bool diag);
+  void release();
+  int field_src(int field, const void** src, bool* is_double);
+
+  swc_params p_;
+  Grid g_{};
+  double amp_ = 0, kp_ = 0, rho_s_ = 0, rho_m_ = 0, dx_ = 0, scale_ = 0;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  std::vector<void*> allocs_;
+  // tables
+  DevTables<T> tab_{};
+  DevTables<double> tabd_{};  // FP64 tables (same as tab_ when T = double)
+  const T *vq_[3] = {}, *vs_[3] = {}, *gq_[3] = {}, *gs_[3] = {};
+  const double* vqd_[3] = {};
+  // state (FP64)
+  double *psiq_ = nullptr, *psiq_old_ = nullptr, *rho_ = nullptr, *frho_ = nullptr;
+  // work (T)
+  T *nlq_ = nullptr, *psi_ = nullptr, *psi_new_ = nullptr, *psi_old_ = nullptr, *rhoq_ = nullptr;
+  T *gp_[3] = {}, *gr_[3] = {}, *amp_f_ = nullptr, *lpsi_ = nullptr, *lapR_ = nullptr, *mu_ = nullptr;
+  T *fgrad_ = nullptr, *ener_ = nullptr, *S_[3] = {}, *f_[3] = {}, *vsol_[3] = {}, *virr_[3] = {};
+  T *divv_ = nullptr, *dq_ = nullptr, *v_[3] = {}, *vsolr_[3] = {}, *energy_ = nullptr, *nlw_ = nullptr;
+  double *partial_ = nullptr, *dsum_ = nullptr;
+  int diag_blocks_ = 0;
+  std::map<int, cudaGraphExec_t> graphs_;
+  bool have_state_ = false;
+  bool have_vsol_ = false;
+  int64_t nloop_ = 0;
+  swc_diag diag_{};
+  double last_ms_ = 0;
+};
+
+template <typename T> void StepEngine<T>::release() {
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  for (void* a : allocs_) cudaFree(a);
+  allocs_.clear();
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (stream_) cudaStreamDestroy(stream_);
+  ev0_ = ev1_ = nullptr;
+  stream_ = nullptr;
+}
+
+template <typename T> int StepEngine<T>::init() {
+  SWC_CK(cudaSetDevice(p_.device));
+  g_.nx = p_.nx; g_.ny = p_.ny; g_.nz = p_.nz;
+  g_.lx = ilog2(p_.nx); g_.ly = ilog2(p_.ny); g_.lz = ilog2(p_.nz);
+  g_.ng = (long long)p_.nx * p_.ny * p_.nz;
+  // REF:250-272
+  amp_ = std::sqrt((3 * p_.beta + std::sqrt(9 * p_.beta * p_.beta + 40 * p_.ep * p_.gamma)) / 5);
+  kp_ = (1 - p_.rho_0) / amp_;
+  rho_s_ = kp_ * amp_ + p_.rho_0;
+  rho_m_ = rho_s_ / 2;
+  const double pi = 3.14159265358979323846;
+  const int dims[3] = {p_.nx, p_.ny, p_.nz};
+  double d[3];
+  for (int a = 0; a < 3; ++a) d[a] = (dims[a] * 2.0 * pi / (p_.q0 * p_.nw)) / dims[a];
+  dx_ = d[0];
+  scale_ = 0.125 / ((double)p_.nx * p_.ny * p_.nz);
+  SWC_CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  SWC_CK(cudaEventCreate(&ev0_));
+  SWC_CK(cudaEventCreate(&ev1_));
+
+  auto dalloc = [&](size_t bytes, void** out) -> int {
+    void* ptr = nullptr;
+    cudaError_t e = cudaMalloc(&ptr, bytes);
+    if (e != cudaSuccess) {
+      set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+      cudaGetLastError();
+      return SWC_ERR_OOM;
+    }
+    allocs_.push_back(ptr);
+    *out = ptr;
+    return SWC_OK;
+  };
+  auto upload = [&](const void* host, size_t bytes, const void** out) -> int {
+    void* ptr;
+    int rc = dalloc(bytes, &ptr);
+    if (rc) return rc;
+    SWC_CK(cudaMemcpy(ptr, host, bytes, cudaMemcpyHostToDevice));
+    *out = ptr;
+    return SWC_OK;
+  };
+  // wavenumbers REF:445-481 and Gaussian factors, per axis
+  for (int a = 0; a < 3; ++a) {
+    const int n = dims[a];
+    std::vector<double> vq(n), vs(n), gq(n), gs(n);
+    for (int i = 0; i < n; ++i) {
+      vq[i] = pi * (i) / (d[a] * n);
+      vs[i] = pi * (i + 1) / (d[a] * n);
+      gq[i] = std::exp(-1.57 * 1.57 * 2 * (vq[i] * vq[i]));
+      gs[i] = std::exp(-1.57 * 1.57 * 2 * (vs[i] * vs[i]));
+    }
+    std::vector<T> tq(vq.begin(), vq.end()), ts(vs.begin(), vs.end()), tgq(gq.begin(), gq.end()),
+        tgs(gs.begin(), gs.end());
+    int rc;
+    if ((rc = upload(tq.data(), n * sizeof(T), (const void**)&vq_[a]))) return rc;
+    if ((rc = upload(ts.data(), n * sizeof(T), (const void**)&vs_[a]))) return rc;
+    if ((rc = upload(tgq.data(), n * sizeof(T), (const void**)&gq_[a]))) return rc;
+    if ((rc = upload(tgs.data(), n * sizeof(T), (const void**)&gs_[a]))) return rc;
+    if ((rc = upload(vq.data(), n * sizeof(double), (const void**)&vqd_[a]))) return rc;
+    HostTables<T> ht(n);
+    if ((rc = upload(ht.fft.data(), ht.fft.size() * sizeof(T), (const void**)&tab_.t[a].fft))) return rc;
+    if ((rc = upload(ht.post.data(), ht.post.size() * sizeof(T), (const void**)&tab_.t[a].post))) return rc;
+    if ((rc = upload(ht.pre.data(), ht.pre.size() * sizeof(T), (const void**)&tab_.t[a].pre))) return rc;
+    if constexpr (std::is_same<T, double>::value) {
+      tabd_.t[a] = tab_.t[a];
+    } else {
+      HostTables<double> hd(n);
+      if ((rc = upload(hd.fft.data(), hd.fft.size() * sizeof(double), (const void**)&tabd_.t[a].fft))) return rc;
+      if ((rc = upload(hd.post.data(), hd.post.size() * sizeof(double), (const void**)&tabd_.t[a].post))) return rc;
+      if ((rc = upload(hd.pre.data(), hd.pre.size() * sizeof(double), (const void**)&tabd_.t[a].pre))) return rc;
+    }
+  }
+  const size_t nd = (size_t)g_.ng * sizeof(double), nt = (size_t)g_.ng * sizeof(T);
+  int rc;
+  double** dbufs[] = {&psiq_, &psiq_old_, &rho_, &frho_};
+  for (double** b : dbufs)
+    if ((rc = dalloc(nd, (void**)b))) return rc;
+  T** tbufs[] = {&nlq_, &psi_, &psi_new_, &psi_old_, &rhoq_, &gp_[0], &gp_[1], &gp_[2], &gr_[0], &gr_[1],
+                 &gr_[2], &amp_f_, &lpsi_, &lapR_, &mu_, &fgrad_, &ener_, &S_[0], &S_[1], &S_[2], &f_[0],
+                 &f_[1], &f_[2], &vsol_[0], &vsol_[1], &vsol_[2], &virr_[0], &virr_[1], &virr_[2], &divv_,
+                 &dq_, &v_[0], &v_[1], &v_[2], &vsolr_[0], &vsolr_[1], &vsolr_[2], &energy_, &nlw_};
+  for (T** b : tbufs) {
+    if ((rc = dalloc(nt, (void**)b))) return rc;
+    SWC_CK(cudaMemset(*b, 0, nt));
+  }
+  for (double** b : dbufs) SWC_CK(cudaMemset(*b, 0, nd));
+  int sms = 0;
+  SWC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p_.device));
+  diag_blocks_ = sms * 4;
+  long long need = (g_.ng + kDiagThreads - 1) / kDiagThreads;
+  if (need < diag_blocks_) diag_blocks_ = (int)need;
+  if ((rc = dalloc(sizeof(double) * 5 * diag_blocks_, (void**)&partial_))) return rc;
+  if ((rc = dalloc(sizeof(double) * 8, (void**)&dsum_))) return rc;
+  return SWC_OK;
+}
+
+template <typename T>
+template <typename U, int KIND, class LD, class ST, class MUL>
+int StepEngine<T>::passU(int axis, LD ld, ST st, MUL mul) {
+  SWC_CK((launch_pass<U, KIND, LD, ST, MUL>(g_, axis, tabs<U>(axis), stream_, ld, st, mul)));
+  return SWC_OK;
+}
+
+#define SWC_TRY(x)         \
+  do {                     \
+    int rc_ = (x);         \
+    if (rc_) return rc_;   \
+  } while (0)
+
+template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bool diag) {
+  using LP = LdPlain<T, T>;
+  using SP = StPlain<T, T>;
+  const long long sx = 1LL << (g_.ly + g_.lz), sy = g_.nz;
+  const int nlast[3] = {g_.nx - 1, g_.ny - 1, g_.nz - 1};
+  const long long shifts[3] = {sx, sy, 1};
+  const unsigned pw_blocks = (unsigned)((g_.ng + 255) / 256);
+
+  // S1 (REF:1104-1106): rhoq = DCT(rho)
+  SWC_TRY((pass<K_C2>(2, LdPlain<T, double>{rho_}, SP{rhoq_})));
+  SWC_TRY((pass<K_C2>(1, LP{rhoq_}, SP{rhoq_})));
+  SWC_TRY((pass<K_C2>(0, LP{rhoq_}, SP{rhoq_})));
+  // S1 + S2 (REF:1166-1250): spectral gradients -> inverse mixed transforms
+  for (int ax = 0; ax < 3; ++ax) {
+    LdGrad<T, double> lpsi{psiq_, vs_[ax], (T)1, ax, nlast[ax], shifts[ax]};
+    LdGrad<T, T> lrho{rhoq_, vs_[ax], (T)scale_, ax, nlast[ax], shifts[ax]};
+    for (int which = 0; which < 2; ++which) {
+      T* out = which == 0 ? gp_[ax] : gr_[ax];
+      // z pass: sine along z only for the z component
+      if (ax == 2) {
+        if (which == 0) SWC_TRY((pass<K_S3>(2, lpsi, SP{out})));
+        else SWC_TRY((pass<K_S3>(2, lrho, SP{out})));
+      } else {
+        if (which == 0) SWC_TRY((pass<K_C3>(2, lpsi, SP{out})));
+        else SWC_TRY((pass<K_C3>(2, lrho, SP{out})));
+      }
+      if (ax == 1) SWC_TRY((pass<K_S3>(1, LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3>(1, LP{out}, SP{out})));
+      if (ax == 0) SWC_TRY((pass<K_S3>(0, LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3>(0, LP{out}, SP{out})));
+    }
+  }
+  // S3 (REF:1254-1289): amplitude, Gaussian filter
+  SWC_TRY((pass<K_C2>(2, LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
+  SWC_TRY((pass<K_C2>(1, LP{amp_f_}, SP{amp_f_})));
+  SWC_TRY((pass<K_FILT>(0, LP{amp_f_}, SP{amp_f_}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
+  SWC_TRY((pass<K_C3>(1, LP{amp_f_}, SP{amp_f_})));
+  SWC_TRY((pass<K_C3>(2, LP{amp_f_}, SP{amp_f_})));
+  // S4 (REF:1293-1308): dfDlapPsi
+  const T alpha = (T)p_.alpha, q02 = (T)(p_.q0 * p_.q0);
+  SWC_TRY((pass<K_C3>(2, LdLpsi<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
+  SWC_TRY((pass<K_C3>(1, LP{lpsi_}, SP{lpsi_})));
+  SWC_TRY((pass<K_C3>(0, LP{lpsi_}, SP{lpsi_})));
+  // S5 (REF:1312-1380)
+  if (!relax) {
+    SWC_TRY((pass<K_C2>(2, LdRhoL<T>{rho_, lpsi_}, SP{lapR_})));
+    SWC_TRY((pass<K_C2>(1, LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_FILT>(0, LP{lapR_}, SP{lapR_}, MulLap<T>{vq_[0], vq_[1], vq_[2], (T)scale_})));
+    SWC_TRY((pass<K_C3>(1, LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_C3>(2, LP{lapR_}, SP{lapR_})));
+  } else {
+    SWC_TRY((pass<K_C3>(2, LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
+    SWC_TRY((pass<K_C3>(1, LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_C3>(0, LP{lapR_}, SP{lapR_})));
+  }
+  // S5 relax tail + S6 (REF:1363-1425)
+  {
+    S6Args<T> a{lapR_, lpsi_, psi_, amp_f_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2], rho_,
+                fgrad_, ener_, S_[0], S_[1], S_[2], f_[0], f_[1], f_[2], mu_,
+                p_.ep, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, amp_, relax ? 1 : 0};
+    s6_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+  }
+  // S7 (REF:1427-1457): forward transforms
+  T* cts[2] = {fgrad_, ener_};
+  for (T* b : cts) {
+    SWC_TRY((pass<K_C2>(2, LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2>(1, LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2>(0, LP{b}, SP{b})));
+  }
+  for (int ax = 0; ax < 3; ++ax) {
+    T* bs[2] = {S_[ax], f_[ax]};
+    for (T* b : bs) {
+      if (ax == 2) SWC_TRY((pass<K_S2>(2, LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2>(2, LP{b}, SP{b})));
+      if (ax == 1) SWC_TRY((pass<K_S2>(1, LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2>(1, LP{b}, SP{b})));
+      if (ax == 0) SWC_TRY((pass<K_S2>(0, LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2>(0, LP{b}, SP{b})));
+    }
+  }
+  // S8 + S9 (REF:1468-1974)
+  {
+    StokesArgs<T> a{S_[0], S_[1], S_[2], fgrad_, ener_, vsol_[0], vsol_[1], vsol_[2], virr_[0], virr_[1],
+                    virr_[2], vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2], gq_[0], gq_[1], gq_[2], gs_[0],
+                    gs_[1], gs_[2], (T)scale_, (T)p_.nu, (T)(p_.lambda + 2 * p_.nu), p_.nx / p_.ref_ranks};
+    stokes_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+  }
+  // S10 (REF:1977-2091)
+  {
+    DivArgs<T> a{virr_[0], virr_[1], virr_[2], f_[0], f_[1], f_[2], divv_, dq_, vq_[0], vq_[1], vq_[2]};
+    div_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+  }
+  SWC_TRY((pass<K_C3>(2, LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3>(1, LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3>(0, LP{divv_}, SP{divv_})));
+  // S11 (REF:2093-2117): v = vsol + virr to real space; vsol alone on diagnostic steps
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int which = 0; which < (diag ? 2 : 1); ++which) {
+      T* out = which == 0 ? v_[ax] : vsolr_[ax];
+      if (which == 0) {
+        LdSum2<T> ld{vsol_[ax], virr_[ax]};
+        if (ax == 2) SWC_TRY((pass<K_S3>(2, ld, SP{out})));
+        else SWC_TRY((pass<K_C3>(2, ld, SP{out})));
+      } else {
+        LP ld{vsol_[ax]};
+        if (ax == 2) SWC_TRY((pass<K_S3>(2, ld, SP{out})));
+        else SWC_TRY((pass<K_C3>(2, ld, SP{out})));
+      }
+      if (ax == 1) SWC_TRY((pass<K_S3>(1, LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3>(1, LP{out}, SP{out})));
+      if (ax == 0) SWC_TRY((pass<K_S3>(0, LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3>(0, LP{out}, SP{out})));
+    }
+  }
+  // S12 + S13 + S14 (REF:2121-2190): rho update, Nl, its DCT, the psiq update
+  {
+    LdNl<T> ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
+               rho_, frho_, p_.dt, kp_, p_.zeta, p_.rho_0};
+    SWC_TRY((pass<K_C2>(2, ld, SP{nlw_})));
+    SWC_TRY((pass<K_C2>(1, LP{nlw_}, SP{nlw_})));
+    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0,
+                     p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, std::is_same<T, float>::value ? 1 : 0};
+    SWC_TRY((pass<K_C2>(0, LP{nlw_}, st)));
+  }
+  // S14 (REF:2194-2197): psi = iDCT(psiq_new)
+  T* pout = diag ? psi_new_ : psi_;
+  SWC_TRY((pass<K_C3>(2, LdPlain<T, double>{psiq_}, SP{pout})));
+  SWC_TRY((pass<K_C3>(1, LP{pout}, SP{pout})));
+  SWC_TRY((pass<K_C3>(0, LP{pout}, SP{pout})));
+  if (diag) {
+    DiagArgs<T> a{psi_new_, lpsi_, amp_f_, psi_, psi_old_, energy_, rho_, partial_,
+                  p_.ep, p_.beta, p_.gamma, p_.zeta, p_.rho_0, kp_};
+    diag_kernel<T><<<diag_blocks_, kDiagThreads, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+    diag_final_kernel<<<1, 32, 0, stream_>>>(partial_, diag_blocks_, dsum_);
+    SWC_CK(cudaGetLastError());
+  }
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag) {
+  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0);
+  auto it = graphs_.find(key);
+  if (it == graphs_.end()) {
+    cudaGraph_t graph = nullptr;
+    SWC_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
+    int rc = enqueue_step(relax, first, diag);
+    cudaError_t e = cudaStreamEndCapture(stream_, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) {
+      set_error("cudaStreamEndCapture: %s", cudaGetErrorString(e));
+      return SWC_ERR_CUDA;
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+      return SWC_ERR_CUDA;
+    }
+    it = graphs_.emplace(key, exec).first;
+  }
+  SWC_CK(cudaGraphLaunch(it->second, stream_));
+  return SWC_OK;
+}
+
+// psiq = scale * v (last pass of the pre-loop DCT, REF:982)
+struct StScaleD {
+  double* p;
+  double s;
+  __device__ __forceinline__ void operator()(int, int, int, long long idx, double v) const { p[idx] = s * v; }
+};
+
+template <typename T> int StepEngine<T>::set_state(const double* psi, const double* rho) {
+  SWC_CK(cudaSetDevice(p_.device));
+  const size_t nd = (size_t)g_.ng * sizeof(double), nt = (size_t)g_.ng * sizeof(T);
+  // REF:968-982: psiq = scale * DCT(psi), in FP64 for both engines (psi staged in frho_)
+  SWC_CK(cudaMemcpyAsync(frho_, psi, nd, cudaMemcpyHostToDevice, stream_));
+  SWC_TRY((passU<double, K_C2>(2, LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
+  SWC_TRY((passU<double, K_C2>(1, LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
+  SWC_TRY((passU<double, K_C2>(0, LdPlain<double, double>{frho_}, StScaleD{psiq_, scale_})));
+  // REF:1052-1071 (+ caller's rho); f_rho, Nl_old and the work arrays start at zero
+  if (rho) SWC_CK(cudaMemcpyAsync(rho_, rho, nd, cudaMemcpyHostToDevice, stream_));
+  else SWC_CK(cudaMemsetAsync(rho_, 0, nd, stream_));
+  SWC_CK(cudaMemsetAsync(frho_, 0, nd, stream_));
+  SWC_CK(cudaMemcpyAsync(psiq_old_, psiq_, nd, cudaMemcpyDeviceToDevice, stream_));  // REF:1005
+  T* zero[] = {nlq_, psi_old_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2], amp_f_, divv_, v_[0], v_[1], v_[2],
+               vsolr_[0], vsolr_[1], vsolr_[2], energy_, lpsi_, mu_};
+  for (T* z : zero) SWC_CK(cudaMemsetAsync(z, 0, nt, stream_));
+  // REF:984-988: psi = iDCT(psiq)
+  SWC_TRY((pass<K_C3>(2, LdPlain<T, double>{psiq_}, StPlain<T, T>{psi_})));
+  SWC_TRY((pass<K_C3>(1, LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
+  SWC_TRY((pass<K_C3>(0, LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
+  SWC_CK(cudaMemcpyAsync(psi_old_, psi_, nt, cudaMemcpyDeviceToDevice, stream_));  // REF:1010
+  SWC_CK(cudaStreamSynchronize(stream_));
+  nloop_ = 0;
+  have_state_ = true;
+  have_vsol_ = false;
+  std::memset(&diag_, 0, sizeof(diag_));
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::step(int nsteps) {
+  if (nsteps < 0) {
+    set_error("nsteps must be >= 0");
+    return SWC_ERR_BAD_PARAM;
+  }
+  if (!have_state_) {
+    set_error("swc_step before swc_set_state");
+    return SWC_ERR_STATE;
+  }
+  if (nsteps == 0) return SWC_OK;
+  SWC_CK(cudaSetDevice(p_.device));
+  SWC_CK(cudaEventRecord(ev0_, stream_));
+  for (int s = 0; s < nsteps; ++s) {
+    const int64_t n = nloop_ + 1;  // nLoop after the increment at REF:1085
+    const bool relax = !(n > p_.divv_switch || p_.load == 1);
+    SWC_TRY(run_graph(relax, n == 1, s == nsteps - 1));
+    nloop_ = n;
+  }
+  SWC_CK(cudaEventRecord(ev1_, stream_));
+  // host watchdog: poll the stream's last event, never spin on the device
+  if (p_.watchdog_s > 0) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+      cudaError_t e = cudaEventQuery(ev1_);
+      if (e == cudaSuccess) break;
+      if (e != cudaErrorNotReady) {
+        set_error("step failed: %s", cudaGetErrorString(e));
+        return SWC_ERR_CUDA;
+      }
+      const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (el > p_.watchdog_s) {
+        set_error("watchdog: swc_step exceeded %.3f s", p_.watchdog_s);
+        return SWC_ERR_TIMEOUT;
+      }
+      std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+  } else {
+    SWC_CK(cudaEventSynchronize(ev1_));
+  }
+  float ms = 0;
+  SWC_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
+  last_ms_ = ms;
+  double sums[5];
+  SWC_CK(cudaMemcpy(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost));
+  // REF:2244-2258
+  diag_.sum_abs_dpsi = sums[0];
+  diag_.sum_abs_psi = sums[1];
+  diag_.sum_rho = sums[2];
+  diag_.sum_energy = sums[3];
+  diag_.l1 = sums[0] / (p_.dt * sums[1]);
+  diag_.mass = sums[2] * dx_ * dx_ * dx_;
+  diag_.energy = sums[3] * dx_ * dx_ * dx_;
+  diag_.step = nloop_;
+  diag_.nonfinite = (int64_t)sums[4];
+  have_vsol_ = true;
+  if (diag_.nonfinite) {
+    set_error("non-finite psi/rho after step %lld (%lld values)", (long long)nloop_, (long long)diag_.nonfinite);
+    return SWC_ERR_NONFINITE;
+  }
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::field_src(int field, const void** src, bool* is_double) {
+  *is_double = false;
+  switch (field) {
+    case SWC_F_PSI: *src = psi_; break;
+    case SWC_F_RHO: *src = rho_; *is_double = true; break;
+    case SWC_F_AMP: *src = amp_f_; break;
+    case SWC_F_DIVV: *src = divv_; break;
+    case SWC_F_VX: *src = v_[0]; break;
+    case SWC_F_VY: *src = v_[1]; break;
+    case SWC_F_VZ: *src = v_[2]; break;
+    case SWC_F_VSOLX: *src = vsolr_[0]; break;
+    case SWC_F_VSOLY: *src = vsolr_[1]; break;
+    case SWC_F_VSOLZ: *src = vsolr_[2]; break;
+    case SWC_F_ENERGY: *src = energy_; break;
+    case SWC_F_PSIQ: *src = psiq_; *is_double = true; break;
+    case SWC_F_PSIQ_OLD: *src = psiq_old_; *is_double = true; break;
+    case SWC_F_NLQ: *src = nlq_; break;
+    case SWC_F_FRHO: *src = frho_; *is_double = true; break;
+    case SWC_F_LPSI: *src = lpsi_; break;
+    case SWC_F_MU: *src = mu_; break;
+    case SWC_F_GPSIX: *src = gp_[0]; break;
+    case SWC_F_GPSIY: *src = gp_[1]; break;
+    case SWC_F_GPSIZ: *src = gp_[2]; break;
+    case SWC_F_GRHOX: *src = gr_[0]; break;
+    case SWC_F_GRHOY: *src = gr_[1]; break;
+    case SWC_F_GRHOZ: *src = gr_[2]; break;
+    case SWC_F_PSI_OLD: *src = psi_old_; break;
+    default:
+      set_error("unknown field id %d", field);
+      return SWC_ERR_BAD_PARAM;
+  }
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::get_field(int field, double* dst) {
+  const void* src;
+  bool is_d;
+  SWC_TRY(field_src(field, &src, &is_d));
+  SWC_CK(cudaSetDevice(p_.device));
+  SWC_CK(cudaStreamSynchronize(stream_));
+  const size_t n = (size_t)g_.ng;
+  if (is_d || std::is_same<T, double>::value) {
+    SWC_CK(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<T> tmp(n);
+    SWC_CK(cudaMemcpy(tmp.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i];
+  }
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::field_ptr(int field, void** ptr, int* elem_bytes) {
+  const void* src;
+  bool is_d;
+  SWC_TRY(field_src(field, &src, &is_d));
+  *ptr = const_cast<void*>(src);
+  *elem_bytes = is_d ? 8 : (int)sizeof(T);
+  return SWC_OK;
+}
+
+// Checkpoint: header + psiq, psiq_old, rho, f_rho (FP64) + Nl_old, psi (T).
+struct CkptHeader {
+  char magic[8];
+  int32_t version, nx, ny, nz, precision, elem;
+  int64_t nloop;
+};
+
+template <typename T> int StepEngine<T>::save(const char* path) {
+  if (!have_state_) {
+    set_error("swc_save before swc_set_state");
+    return SWC_ERR_STATE;
+  }
+  SWC_CK(cudaSetDevice(p_.device));
+  SWC_CK(cudaStreamSynchronize(stream_));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    set_error("cannot open %s for writing", path);
+    return SWC_ERR_IO;
+  }
+  CkptHeader h{};
+  std::memcpy(h.magic, "SWCCKPT1", 8);
+  h.version = 1; h.nx = p_.nx; h.ny = p_.ny; h.nz = p_.nz; h.precision = p_.precision;
+  h.elem = (int)sizeof(T); h.nloop = nloop_;
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+  const size_t n = (size_t)g_.ng;
+  std::vector<char> buf(n * sizeof(double));
+  const void* dsrc[] = {psiq_, psiq_old_, rho_, frho_};
+  for (const void* s : dsrc) {
+    if (!ok) break;
+    if (cudaMemcpy(buf.data(), s, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+    else ok = std::fwrite(buf.data(), 1, n * sizeof(double), f) == n * sizeof(double);
+  }
+  const void* tsrc[] = {nlq_, psi_};
+  for (const void* s : tsrc) {
+    if (!ok) break;
+    if (cudaMemcpy(buf.data(), s, n * sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+    else ok = std::fwrite(buf.data(), 1, n * sizeof(T), f) == n * sizeof(T);
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) {
+    set_error("writing checkpoint %s failed", path);
+    return SWC_ERR_IO;
+  }
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::load(const char* path) {
+  SWC_CK(cudaSetDevice(p_.device));
+  FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    set_error("cannot open %s", path);
+    return SWC_ERR_IO;
+  }
+  CkptHeader h{};
+  bool ok = std::fread(&h, sizeof(h), 1, f) == 1;
+  if (!ok || std::memcmp(h.magic, "SWCCKPT1", 8) != 0 || h.version != 1 || h.nx != p_.nx || h.ny != p_.ny ||
+      h.nz != p_.nz || h.elem != (int)sizeof(T) || h.nloop < 0) {
+    std::fclose(f);
+    set_error("checkpoint %s does not match this context (grid/precision/format)", path);
+    return SWC_ERR_IO;
+  }
+  const size_t n = (size_t)g_.ng;
+  std::vector<char> buf(n * sizeof(double));
+  double* ddst[] = {psiq_, psiq_old_, rho_, frho_};
+  for (double* d : ddst) {
+    if (!ok) break;
+    ok = std::fread(buf.data(), 1, n * sizeof(double), f) == n * sizeof(double);
+    if (ok) ok = cudaMemcpy(d, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess;
+  }
+  T* tdst[] = {nlq_, psi_};
+  for (T* d : tdst) {
+    if (!ok) break;
+    ok = std::fread(buf.data(), 1, n * sizeof(T), f) == n * sizeof(T);
+    if (ok) ok = cudaMemcpy(d, buf.data(), n * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+  }
+  std::fclose(f);
+  if (!ok) {
+    set_error("checkpoint %s is truncated or unreadable", path);
+    return SWC_ERR_IO;
+  }
+  SWC_CK(cudaMemcpy(psi_old_, psi_, n * sizeof(T), cudaMemcpyDeviceToDevice));
+  nloop_ = h.nloop;
+  have_state_ = true;
+  have_vsol_ = false;
+  std::memset(&diag_, 0, sizeof(diag_));
+  diag_.step = nloop_;
+  return SWC_OK;
+}
+
+}  // namespace swc

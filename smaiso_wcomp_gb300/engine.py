@@ -1,0 +1,132 @@
+"""Python host mirror of the C ABI (include/swc.h): the time loop and r2r plans.
+
+Every call goes through libswc.so (the sm_103a CUDA library); a failing status
+raises SwcError carrying swc_last_error(). There is no CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+
+class SwcError(RuntimeError):
+    def __init__(self, status, where, msg=""):
+        self.status = status
+        super().__init__(f"{where}: status {status} ({msg})")
+
+
+def _check(lib, rc, where):
+    if rc != abi.SWC_OK:
+        raise SwcError(rc, where, lib.swc_last_error().decode(errors="replace"))
+
+
+class Engine:
+    """One simulation context: swc_create / swc_set_state / swc_step / ... / swc_destroy."""
+
+    def __init__(self, params, lib=None):
+        self.lib = lib or abi.load_library()
+        self.p = params
+        self.shape = (params.nx, params.ny, params.nz)
+        self._h = ctypes.c_void_p()
+        _check(self.lib, self.lib.swc_create(ctypes.byref(params), ctypes.byref(self._h)), "swc_create")
+
+    def close(self):
+        if self._h:
+            self.lib.swc_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, psi, rho=None):
+        psi = np.ascontiguousarray(psi, dtype=np.float64).reshape(self.shape)
+        rp = None
+        if rho is not None:
+            rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(self.shape)
+            rp = abi.as_dptr(rho)
+        _check(self.lib, self.lib.swc_set_state(self._h, abi.as_dptr(psi), rp), "swc_set_state")
+
+    def step(self, n=1, check=True):
+        rc = self.lib.swc_step(self._h, int(n))
+        if check:
+            _check(self.lib, rc, "swc_step")
+        return rc
+
+    def diagnostics(self):
+        d = abi.SwcDiag()
+        _check(self.lib, self.lib.swc_diagnostics(self._h, ctypes.byref(d)), "swc_diagnostics")
+        return d.as_dict()
+
+    def field(self, name, out=None):
+        if out is None:
+            out = np.empty(self.shape, dtype=np.float64)
+        _check(self.lib, self.lib.swc_get_field(self._h, abi.FIELD_ID[name], abi.as_dptr(out)),
+               f"swc_get_field({name})")
+        return out
+
+    def device_ptr(self, name):
+        ptr = ctypes.c_void_p()
+        eb = ctypes.c_int()
+        _check(self.lib, self.lib.swc_field_device_ptr(self._h, abi.FIELD_ID[name], ctypes.byref(ptr),
+                                                       ctypes.byref(eb)), "swc_field_device_ptr")
+        return ptr.value, eb.value
+
+    @property
+    def nloop(self):
+        n = ctypes.c_int64()
+        _check(self.lib, self.lib.swc_get_step(self._h, ctypes.byref(n)), "swc_get_step")
+        return n.value
+
+    def last_step_ms(self):
+        ms = ctypes.c_double()
+        _check(self.lib, self.lib.swc_last_step_ms(self._h, ctypes.byref(ms)), "swc_last_step_ms")
+        return ms.value
+
+    def save(self, path):
+        _check(self.lib, self.lib.swc_save(self._h, str(path).encode()), "swc_save")
+
+    def load(self, path):
+        _check(self.lib, self.lib.swc_load(self._h, str(path).encode()), "swc_load")
+
+
+class R2RPlan:
+    """3D r2r transform with FFTW semantics (kinds SWC_REDFT10/01, SWC_RODFT10/01 per axis)."""
+
+    def __init__(self, shape, kinds, precision=abi.SWC_PREC_FP64, lib=None):
+        self.lib = lib or abi.load_library()
+        self.shape = tuple(shape)
+        self._h = ctypes.c_void_p()
+        _check(self.lib, self.lib.swc_r2r_plan_create(*self.shape, *kinds, precision, ctypes.byref(self._h)),
+               "swc_r2r_plan_create")
+
+    def __call__(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(self.shape)
+        out = np.empty_like(x)
+        _check(self.lib, self.lib.swc_r2r_execute_host(self._h, abi.as_dptr(x), abi.as_dptr(out)),
+               "swc_r2r_execute_host")
+        return out
+
+    def execute_device(self, dev_ptr, stream=None):
+        _check(self.lib, self.lib.swc_r2r_execute(self._h, ctypes.c_void_p(dev_ptr), ctypes.c_void_p(stream)),
+               "swc_r2r_execute")
+
+    def close(self):
+        if self._h:
+            self.lib.swc_r2r_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,145 @@
+"""GPU time step through the C ABI against the FP64 oracle on the same seeded inputs."""
+import os
+
+import numpy as np
+import pytest
+
+from smaiso_wcomp_gb300 import abi, ic
+from smaiso_wcomp_gb300.engine import Engine, SwcError
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["psi", "rho", "amp", "divv", "vx", "vy", "vz", "vsolx", "vsoly", "vsolz", "energy", "psiq",
+          "psiq_old", "nlq", "frho", "lpsi", "mu", "gpsix", "gpsiy", "gpsiz", "grhox", "grhoy", "grhoz",
+          "psi_old"]
+FP64_TOL = 1e-10   # relative L2 per field (the FP64 parity bar)
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a)
+
+
+def run_pair(O, p, psi, rho, schedule):
+    o = O.Oracle(p)
+    o.set_state(psi, rho)
+    e = Engine(p)
+    e.set_state(psi, rho)
+    for n in schedule:
+        assert o.step(n) == 0
+        e.step(n)
+    return o, e
+
+
+CASES = [
+    ((16, 16, 32), dict(rho_0=0.9, divv_switch=3, ref_ranks=2), "flat", [2, 3, 4]),
+    ((32, 16, 8), dict(rho_0=0.8, divv_switch=2, ref_ranks=4), "undulated", [5, 5]),
+    ((8, 32, 16), dict(rho_0=0.01, divv_switch=50, ref_ranks=2, nu=0.5), "band", [4]),
+    ((16, 16, 16), dict(rho_0=0.5, divv_switch=0, load=1, ref_ranks=8, dt=0.002), "undulated", [3, 1]),
+]
+
+
+@pytest.mark.parametrize("shape,kw,gen,schedule", CASES)
+def test_fp64_step_parity(lib, oracle_mod, shape, kw, gen, schedule):
+    p = abi.default_params(*shape, **kw)
+    psi, rho = {"flat": ic.flat_interface, "undulated": ic.undulated_interface,
+                "band": ic.reference_band}[gen](p)
+    if gen == "band":
+        rho = None  # the reference's own start: rho = 0 (REF:1053)
+    o, e = run_pair(oracle_mod, p, psi, rho, schedule)
+    errs = {f: rel(e.field(f), o.field(f)) for f in FIELDS}
+    bad = {f: v for f, v in errs.items() if not v <= FP64_TOL}
+    assert not bad, bad
+    do, de = o.diagnostics(), e.diagnostics()
+    for k in ("l1", "mass", "energy", "sum_abs_psi"):
+        assert abs(de[k] - do[k]) <= FP64_TOL * abs(do[k]) + 1e-300, (k, de[k], do[k])
+    assert de["step"] == do["step"] == sum(schedule)
+
+
+def test_mixed_step_accuracy(lib, oracle_mod):
+    p = abi.default_params(32, 32, 32, rho_0=0.8, divv_switch=10)
+    psi, rho = ic.undulated_interface(p)
+    o = oracle_mod.Oracle(p)
+    o.set_state(psi, rho)
+    o.step(60)
+    pm = abi.default_params(32, 32, 32, rho_0=0.8, divv_switch=10, precision=abi.SWC_PREC_MIXED)
+    with Engine(pm) as e:
+        e.set_state(psi, rho)
+        e.step(60)
+        for f in ("psi", "rho"):
+            assert rel(e.field(f), o.field(f)) <= 1e-5, f
+        for f in ("vx", "vy", "vz"):
+            assert rel(e.field(f), o.field(f)) <= 1e-3, f
+        assert abs(e.diagnostics()["mass"] - o.diagnostics()["mass"]) <= 1e-9 * abs(o.diagnostics()["mass"])
+
+
+def test_zero_state_fixed_point(lib):
+    p = abi.default_params(16, rho_0=0.3, divv_switch=2)
+    with Engine(p) as e:
+        e.set_state(np.zeros((16, 16, 16)), np.full((16, 16, 16), 0.3))
+        e.step(5)
+        assert np.max(np.abs(e.field("psi"))) == 0.0
+        np.testing.assert_allclose(e.field("rho"), 0.3, rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
+def test_checkpoint_continuation_is_bitwise(lib, tmp_path, prec):
+    p = abi.default_params(16, 16, 16, rho_0=0.8, divv_switch=3, precision=prec)
+    psi, rho = ic.undulated_interface(p)
+    path = os.path.join(tmp_path, "state.swc")
+    with Engine(p) as e:
+        e.set_state(psi, rho)
+        e.step(4)
+        e.save(path)
+        e.step(5)
+        a = {f: e.field(f) for f in ("psi", "rho", "psiq", "nlq")}
+    with Engine(p) as e2:
+        e2.load(path)
+        assert e2.nloop == 4
+        e2.step(5)
+        for f, v in a.items():
+            assert np.array_equal(e2.field(f), v), f
+
+
+def test_nonfinite_detected(lib):
+    p = abi.default_params(8)
+    psi = np.zeros((8, 8, 8))
+    psi[1, 2, 3] = np.nan
+    with Engine(p) as e:
+        e.set_state(psi)
+        with pytest.raises(SwcError) as ex:
+            e.step(2)
+        assert ex.value.status == abi.SWC_ERR_NONFINITE
+
+
+def test_step_before_state_is_rejected(lib):
+    with Engine(abi.default_params(8)) as e:
+        with pytest.raises(SwcError) as ex:
+            e.step(1)
+        assert ex.value.status == abi.SWC_ERR_STATE
+
+
+def test_watchdog_returns_timeout_and_context_recovers(lib):
+    p = abi.default_params(128, rho_0=0.8, watchdog_s=1e-6)
+    psi, rho = ic.flat_interface(p)
+    with Engine(p) as e:
+        e.set_state(psi, rho)
+        rc = e.step(3, check=False)
+        assert rc == abi.SWC_ERR_TIMEOUT
+        e.step(1)  # drains the previous work first, then runs normally
+        assert e.nloop == 4
+
+
+def test_full_size_fp64_vs_mixed_256(lib):
+    """At 256^3: a few steps of both engines stay finite and agree (mixed within 1e-5 on psi)."""
+    p = abi.default_params(256, rho_0=0.8, divv_switch=3)
+    psi, rho = ic.undulated_interface(p)
+    out = {}
+    for prec in (abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED):
+        p.precision = prec
+        with Engine(p) as e:
+            e.set_state(psi, rho)
+            e.step(5)
+            out[prec] = (e.field("psi"), e.diagnostics())
+    assert out[0][1]["nonfinite"] == 0 and out[1][1]["nonfinite"] == 0
+    assert rel(out[1][0], out[0][0]) <= 1e-5
