@@ -1,0 +1,352 @@
+"""Benchmark of the semi-implicit spectral step at 256^3 (mixed vs FP64 GPU).
+
+Workload: the 256x256x256 undulated-interface state (density ratio 0.8, Gaussian
+psi noise sigma = 1e-3, seed 1002), reference coefficients, dt = 0.001 (the
+reference's dt for 8 points per wavelength; dt = 0.01 diverges in the FP64 oracle
+at step 20). A step is one full time step (loop body of smaiso-wcomp.cpp:1084-2198).
+
+  value        mixed-path steps/s with the state resident in HBM (graph launches,
+               CUDA events on the context's stream)
+  e2e          the same metric through the C ABI with host buffers: swc_set_state
+               from pinned host memory once, then per step swc_step(1) + the D2H
+               read of psi (swc_get_field), all inside the timed region
+  roofline     the dominant kernel (the FP32 r2r axis pass, HBM-bound)
+  cpu_baseline the FP64 CPU oracle (restatement of the reference loop; the
+               reference itself needs FFTW3-MPI + MPI C++ bindings) on host cores
+
+Multi-GPU: the path does not shard in this build (one GPU, no collectives); N
+ranks run N independent replicas and value = N * steps / max-over-ranks time.
+`--impl reference` times the CPU oracle port instead (rank 0 only).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s at 256³: mixed vs FP64 GPU @ψ L2 err≤1e-5; gradient/forward time ratio"
+N = 256
+WORKLOAD = "undulated interface 256x256x256, density ratio 0.8, psi noise sigma 1e-3, dt 1e-3"
+L2_BYTES = 129 * 2 ** 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: steps/5, >= 10)")
+    ap.add_argument("--cpu-sample-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
+                    help="profiling mode: run only this engine's warm-up + timed steps and print its timing")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_params(precision, device=0):
+    from smaiso_wcomp_gb300 import abi
+    return abi.default_params(N, rho_0=0.8, divv_switch=50, precision=precision, device=device)
+
+
+def initial_state(p):
+    from smaiso_wcomp_gb300 import ic
+    return ic.undulated_interface(p, seed=1002)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_engine(p, psi, rho, warmup, steps):
+    """Device-timed steps of one engine: CUDA events on the context's stream."""
+    from smaiso_wcomp_gb300.engine import Engine
+    e = Engine(p)
+    e.set_state(psi, rho)
+    e.step(warmup)
+    e.step(steps)
+    ms = e.last_step_ms()
+    launches = e.last_step_launches()
+    return e, ms, launches
+
+
+def time_e2e(p, psi_h, rho_h, steps):
+    """Through the C ABI with host buffers: set_state from pinned host memory, then per
+    step swc_step(1) and the D2H read of psi, all inside the timed region."""
+    from smaiso_wcomp_gb300.engine import Engine
+    e = Engine(p)
+    out = pinned((N, N, N))
+    e.set_state(psi_h, rho_h)   # graph capture / warm-up outside the timed region
+    e.step(2)
+    e.field("psi", out=out)
+    t0 = time.perf_counter()
+    e.set_state(psi_h, rho_h)
+    for _ in range(steps):
+        e.step(1)
+        e.field("psi", out=out)
+    dt = time.perf_counter() - t0
+    e.close()
+    h2d = 2 * psi_h.nbytes / steps
+    return steps / dt, h2d, out.nbytes
+
+
+def pinned(shape):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        pass
+    return np.empty(shape, dtype=np.float64)
+
+
+def pass_roofline(precision, reps=20):
+    """Live CUDA-event timing of the dominant kernel (one r2r axis pass over 256^3)
+    on the stream it is launched on; achieved = algorithmic bytes / launch time."""
+    import torch
+    from smaiso_wcomp_gb300 import abi
+    from smaiso_wcomp_gb300.engine import R2RPlan
+    dt = torch.float32 if precision == abi.SWC_PREC_MIXED else torch.float64
+    x = torch.randn((N, N, N), dtype=dt, device="cuda")
+    plan = R2RPlan((N, N, N), (0, 0, 0), precision)
+    s = torch.cuda.Stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            plan.execute_device(x.data_ptr(), s.cuda_stream)
+        ev0.record(s)
+        for _ in range(reps):
+            plan.execute_device(x.data_ptr(), s.cuda_stream)
+        ev1.record(s)
+    ev1.synchronize()
+    ms_pass = ev0.elapsed_time(ev1) / (3 * reps)   # 3 axis passes per 3D transform
+    elem = 4 if precision == abi.SWC_PREC_MIXED else 8
+    alg_bytes = 2 * N ** 3 * elem                   # one read + one write of the field
+    del x
+    plan.close()
+    return ms_pass, alg_bytes
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(steps):
+    """FP64 CPU oracle on all host cores at the benchmark workload, `steps` steps."""
+    from oracle import oracle as O
+    from smaiso_wcomp_gb300 import abi
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    p = make_params(abi.SWC_PREC_FP64)
+    psi, rho = initial_state(p)
+    o = O.Oracle(p)
+    o.set_state(psi, rho)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": steps / dt, "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} FP64 oracle steps of the 256^3 workload (relax phase), OpenMP {cores} threads"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    base = cpu_baseline(max(1, args.warmup + args.steps) if args.steps <= 3 else 3)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": [N, N, N]},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    import torch
+    torch.cuda.set_device(local)
+    from smaiso_wcomp_gb300 import abi
+    from smaiso_wcomp_gb300.engine import device_fma_peak
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
+    psi, rho = initial_state(p_mix)
+    if args.only:
+        prec = abi.SWC_PREC_MIXED if args.only == "mixed" else abi.SWC_PREC_FP64
+        e, ms, launches = time_engine(make_params(prec, device=local), psi, rho, args.warmup, args.steps)
+        print(json.dumps({"only": args.only, "steps": args.steps, "ms_per_step": ms / args.steps,
+                          "steps_per_s": args.steps / (ms * 1e-3), "gpu_launches": launches}), flush=True)
+        e.close()
+        return
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+
+    # mixed engine: the headline value
+    barrier()
+    with ClockSampler(local) as clk:
+        e_mix, ms_mix, launches = time_engine(p_mix, psi, rho, max(args.warmup, 3), args.steps)
+    barrier()
+    clocks = clk.summary()
+    # FP64 engine on the same state
+    k64 = args.fp64_steps or max(10, args.steps // 5)
+    p64 = make_params(abi.SWC_PREC_FP64, device=local)
+    e_64, ms_64, _ = time_engine(p64, psi, rho, max(args.warmup, 3), k64)
+    # accuracy of mixed vs FP64 after the same number of steps
+    nsteps_mix, nsteps_64 = e_mix.nloop, e_64.nloop
+    if nsteps_64 < nsteps_mix:
+        e_64.step(nsteps_mix - nsteps_64)
+    elif nsteps_64 > nsteps_mix:
+        e_mix.step(nsteps_64 - nsteps_mix)
+    a, b = e_mix.field("psi"), e_64.field("psi")
+    psi_err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    rho_err = float(np.linalg.norm(e_mix.field("rho") - e_64.field("rho")) / np.linalg.norm(e_64.field("rho")))
+    e_mix.close()
+    e_64.close()
+
+    # max over ranks of the device time
+    t = torch.tensor([ms_mix, ms_64], dtype=torch.float64, device="cuda")
+    if pg:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    ms_mix, ms_64 = float(t[0]), float(t[1])
+    sps_mix = args.steps / (ms_mix * 1e-3)
+    sps_64 = k64 / (ms_64 * 1e-3)
+
+    psi_h = pinned((N, N, N))
+    rho_h = pinned((N, N, N))
+    psi_h[...] = psi
+    rho_h[...] = rho
+    e2e_sps, h2d, d2h = time_e2e(p_mix, psi_h, rho_h, max(10, min(args.steps, 50)))
+
+    peaks, peak_kind = load_peaks()
+    ms_pass, alg = pass_roofline(abi.SWC_PREC_MIXED)
+    achieved = alg / (ms_pass * 1e-3) / 1e9
+    ms_pass64, alg64 = pass_roofline(abi.SWC_PREC_FP64)
+    fp64_peak = device_fma_peak(abi.SWC_PREC_FP64)
+    # FP64 pass flops: FFT part ~ (17/4) M log2 M + pre/post, counted per launch from the
+    # operation count of the kernel (see profiles/): 5 N log2 N real flops per line
+    fp64_flops = 5.0 * N * np.log2(N) * N * N
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": PASS_TRAFFIC.get("fp32"),
+                "kernel": "r2r_pass_kernel<float, K_C2> (one axis pass, 256^3)",
+                "peak_source": f"{peak_kind} hbm_gbs"}
+    line = {
+        "metric": METRIC, "value": sps_mix * world, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mix / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [N, N, N], "parallelism": f"replicas{world}",
+                   "l2": f"inputs larger than L2 (working set {working_set_gb():.1f} GB > 129 MB L2)"},
+        "fp64_steps_per_s": sps_64 * world, "mixed_over_fp64": sps_mix / sps_64,
+        "grid_point_steps_per_s": sps_mix * world * N ** 3,
+        "psi_rel_l2_mixed_vs_fp64": psi_err, "rho_rel_l2_mixed_vs_fp64": rho_err,
+        "accuracy_steps": max(nsteps_mix, nsteps_64),
+        "gradient_forward_ratio": None,
+        "e2e": {"value": e2e_sps * world, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": roofline,
+        "roofline_fp64_pass": {"bound": "fp64_alu", "achieved": fp64_flops / (ms_pass64 * 1e-3) / 1e12,
+                               "peak": fp64_peak, "unit": "TFLOP/s",
+                               "frac": fp64_flops / (ms_pass64 * 1e-3) / 1e12 / fp64_peak,
+                               "hbm_gbs": alg64 / (ms_pass64 * 1e-3) / 1e9,
+                               "peak_source": "measured swc_device_fma_peak(FP64)"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_sample_steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+# DRAM bytes per launch of the dominant kernel from the committed ncu capture
+# (profiles/r2r_pass_256.md); None until captured.
+PASS_TRAFFIC = {"fp32": None}
+
+
+def working_set_gb():
+    return (38 * 4 + 4 * 8) * N ** 3 / 1e9
+
+
+if __name__ == "__main__":
+    main()

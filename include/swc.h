@@ -188,6 +188,15 @@ int swc_get_step(swc_ctx* ctx, int64_t* nloop);
  * with CUDA events on the context's stream. */
 int swc_last_step_ms(swc_ctx* ctx, double* ms);
 
+/* Number of kernels the last swc_step call launched (all steps of the call). */
+int swc_last_step_launches(swc_ctx* ctx, int64_t* launches);
+
+/* Dense FMA throughput of the current device in TFLOP/s (FMA = 2 flops) for
+ * precision SWC_PREC_FP64 (double) or SWC_PREC_MIXED (float): independent FMA
+ * chains on every SM, timed with CUDA events. Used as the roofline denominator of
+ * the ALU-bound FP64 kernels. */
+int swc_device_fma_peak(int precision, double* tflops);
+
 /* ---- full-state checkpoint (lossless; the reference's psi<rank>.dat text dump
  *      at :2334-2345 keeps only psi at 6 digits) ------------------------------ */
 int swc_save(swc_ctx* ctx, const char* path);

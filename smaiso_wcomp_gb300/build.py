@@ -47,6 +47,13 @@ def build(verbose=False, extra=()):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
+    # C++ host driver with the reference's command line, linked against libswc.so
+    exe = os.path.join(OUT, "swc_run")
+    cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", os.path.join(CSRC, "swc_run.cpp"), "-o", exe,
+           f"-L{OUT}", "-lswc", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"swc_run build failed:\n{r.stderr}")
     return lib
 
 

@@ -13,6 +13,66 @@
 
 namespace swc {
 
+// Independent FMA chains per thread (8 per thread, no memory traffic in the loop).
+template <typename T> __global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+  T x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = (T)(threadIdx.x + q) * (T)1e-3;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = x[q] * a + b;
+  }
+  T s = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) s += x[q];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T> static int fma_peak_t(double* tflops) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("no CUDA device");
+    return SWC_ERR_NO_DEVICE;
+  }
+  const int blocks = sms * 8, threads = 256;
+  const int iters = sizeof(T) == 8 ? 4096 : 65536;
+  T* out = nullptr;
+  if (cudaMalloc(&out, sizeof(T) * (size_t)blocks * threads) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("cudaMalloc failed");
+    return SWC_ERR_OOM;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int w = 0; w < 2; ++w) fma_probe_kernel<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(e0);
+    fma_probe_kernel<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = ms < best ? ms : best;
+  }
+  const cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) {
+    set_error("FMA probe failed: %s", cudaGetErrorString(err));
+    return SWC_ERR_CUDA;
+  }
+  *tflops = 2.0 * 8 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+  return SWC_OK;
+}
+
+int fma_peak(int precision, double* tflops) {
+  return precision == SWC_PREC_FP64 ? fma_peak_t<double>(tflops) : fma_peak_t<float>(tflops);
+}
+
 static thread_local std::string g_last_error;
 
 void set_error(const char* fmt, ...) {
@@ -203,6 +263,20 @@ int swc_last_step_ms(swc_ctx* ctx, double* ms) {
   SWC_NEED_CTX(ctx);
   if (!ms) { set_error("NULL output"); return SWC_ERR_BAD_PARAM; }
   SWC_GUARD(ctx->eng->last_ms(ms));
+}
+
+int swc_last_step_launches(swc_ctx* ctx, int64_t* n) {
+  SWC_NEED_CTX(ctx);
+  if (!n) { set_error("NULL output"); return SWC_ERR_BAD_PARAM; }
+  SWC_GUARD(ctx->eng->last_launches(n));
+}
+
+int swc_device_fma_peak(int precision, double* tflops) {
+  if (!tflops || (precision != SWC_PREC_FP64 && precision != SWC_PREC_MIXED)) {
+    set_error("bad argument");
+    return SWC_ERR_BAD_PARAM;
+  }
+  return swc::fma_peak(precision, tflops);
 }
 
 int swc_save(swc_ctx* ctx, const char* path) {

@@ -22,9 +22,13 @@ class EngineBase {
   virtual int field_ptr(int field, void** ptr, int* elem_bytes) = 0;
   virtual int get_step(int64_t* n) = 0;
   virtual int last_ms(double* ms) = 0;
+  virtual int last_launches(int64_t* n) = 0;
   virtual int save(const char* path) = 0;
   virtual int load(const char* path) = 0;
 };
+
+// Dense FMA throughput probe of the current device (TFLOP/s, FMA = 2 flops).
+int fma_peak(int precision, double* tflops);
 
 // Validate parameters shared by every engine. Returns SWC_OK or SWC_ERR_BAD_PARAM.
 int validate_params(const swc_params* p);

@@ -124,6 +124,14 @@ template <typename T> struct LdRhoL {
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)rho[idx] * lpsi[idx]; }
 };
 
+// rho - c: the gradients (REF:1191-1219) never read mode 0, so a constant offset
+// keeps them unchanged while the FP32 transform resolves the small variations.
+template <typename T> struct LdOffset {
+  const double* p;
+  double c;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)(p[idx] - c); }
+};
+
 template <typename T> struct LdSum2 {
   const T *a, *b;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return a[idx] + b[idx]; }
@@ -413,6 +421,10 @@ template <typename T> class StepEngine : public EngineBase {
     *ms = last_ms_;
     return SWC_OK;
   }
+  int last_launches(int64_t* n) override {
+    *n = last_launches_;
+    return SWC_OK;
+  }
   int save(const char* path) override;
   int load(const char* path) override;
 
@@ -454,6 +466,9 @@ template <typename T> class StepEngine : public EngineBase {
   double *partial_ = nullptr, *dsum_ = nullptr;
   int diag_blocks_ = 0;
   std::map<int, cudaGraphExec_t> graphs_;
+  std::map<int, int64_t> graph_kernels_;  // kernel nodes per captured variant
+  int64_t last_launches_ = 0;
+  int64_t launches_ = 0;  // running count while a variant is captured
   bool have_state_ = false;
   bool have_vsol_ = false;
   int64_t nloop_ = 0;
@@ -462,6 +477,9 @@ template <typename T> class StepEngine : public EngineBase {
 };
 
 template <typename T> void StepEngine<T>::release() {
+  // queued graphs may still run (e.g. after a watchdog timeout): drain before freeing
+  if (stream_) cudaStreamSynchronize(stream_);
+  cudaGetLastError();
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
   for (void* a : allocs_) cudaFree(a);
@@ -572,6 +590,7 @@ template <typename T>
 template <typename U, int KIND, class LD, class ST, class MUL>
 int StepEngine<T>::passU(int axis, LD ld, ST st, MUL mul) {
   SWC_CK((launch_pass<U, KIND, LD, ST, MUL>(g_, axis, tabs<U>(axis), stream_, ld, st, mul)));
+  ++launches_;
   return SWC_OK;
 }
 
@@ -589,8 +608,9 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
   const long long shifts[3] = {sx, sy, 1};
   const unsigned pw_blocks = (unsigned)((g_.ng + 255) / 256);
 
-  // S1 (REF:1104-1106): rhoq = DCT(rho)
-  SWC_TRY((pass<K_C2>(2, LdPlain<T, double>{rho_}, SP{rhoq_})));
+  // S1 (REF:1104-1106): rhoq = DCT(rho); the mixed engine transforms rho - (rho_0 + rho_s)/2
+  const double rho_off = std::is_same<T, double>::value ? 0.0 : 0.5 * (p_.rho_0 + rho_s_);
+  SWC_TRY((pass<K_C2>(2, LdOffset<T>{rho_, rho_off}, SP{rhoq_})));
   SWC_TRY((pass<K_C2>(1, LP{rhoq_}, SP{rhoq_})));
   SWC_TRY((pass<K_C2>(0, LP{rhoq_}, SP{rhoq_})));
   // S1 + S2 (REF:1166-1250): spectral gradients -> inverse mixed transforms
@@ -643,6 +663,7 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
                 p_.ep, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, amp_, relax ? 1 : 0};
     s6_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
+    ++launches_;
   }
   // S7 (REF:1427-1457): forward transforms
   T* cts[2] = {fgrad_, ener_};
@@ -669,12 +690,14 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
                     gs_[1], gs_[2], (T)scale_, (T)p_.nu, (T)(p_.lambda + 2 * p_.nu), p_.nx / p_.ref_ranks};
     stokes_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
+    ++launches_;
   }
   // S10 (REF:1977-2091)
   {
     DivArgs<T> a{virr_[0], virr_[1], virr_[2], f_[0], f_[1], f_[2], divv_, dq_, vq_[0], vq_[1], vq_[2]};
     div_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
+    ++launches_;
   }
   SWC_TRY((pass<K_C3>(2, LP{divv_}, SP{divv_})));
   SWC_TRY((pass<K_C3>(1, LP{divv_}, SP{divv_})));
@@ -720,6 +743,7 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
     SWC_CK(cudaGetLastError());
     diag_final_kernel<<<1, 32, 0, stream_>>>(partial_, diag_blocks_, dsum_);
     SWC_CK(cudaGetLastError());
+    launches_ += 2;
   }
   return SWC_OK;
 }
@@ -730,6 +754,7 @@ template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool 
   if (it == graphs_.end()) {
     cudaGraph_t graph = nullptr;
     SWC_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
+    launches_ = 0;
     int rc = enqueue_step(relax, first, diag);
     cudaError_t e = cudaStreamEndCapture(stream_, &graph);
     if (rc) {
@@ -748,8 +773,10 @@ template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool 
       return SWC_ERR_CUDA;
     }
     it = graphs_.emplace(key, exec).first;
+    graph_kernels_[key] = launches_;
   }
   SWC_CK(cudaGraphLaunch(it->second, stream_));
+  last_launches_ += graph_kernels_[key];
   return SWC_OK;
 }
 
@@ -801,6 +828,7 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   if (nsteps == 0) return SWC_OK;
   SWC_CK(cudaSetDevice(p_.device));
   SWC_CK(cudaEventRecord(ev0_, stream_));
+  last_launches_ = 0;
   for (int s = 0; s < nsteps; ++s) {
     const int64_t n = nloop_ + 1;  // nLoop after the increment at REF:1085
     const bool relax = !(n > p_.divv_switch || p_.load == 1);

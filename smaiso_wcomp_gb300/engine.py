@@ -92,11 +92,24 @@ class Engine:
         _check(self.lib, self.lib.swc_last_step_ms(self._h, ctypes.byref(ms)), "swc_last_step_ms")
         return ms.value
 
+    def last_step_launches(self):
+        n = ctypes.c_int64()
+        _check(self.lib, self.lib.swc_last_step_launches(self._h, ctypes.byref(n)), "swc_last_step_launches")
+        return n.value
+
     def save(self, path):
         _check(self.lib, self.lib.swc_save(self._h, str(path).encode()), "swc_save")
 
     def load(self, path):
         _check(self.lib, self.lib.swc_load(self._h, str(path).encode()), "swc_load")
+
+
+def device_fma_peak(precision, lib=None):
+    """Measured dense FMA TFLOP/s of the current device (FMA = 2 flops)."""
+    lib = lib or abi.load_library()
+    t = ctypes.c_double()
+    _check(lib, lib.swc_device_fma_peak(int(precision), ctypes.byref(t)), "swc_device_fma_peak")
+    return t.value
 
 
 class R2RPlan:
