@@ -166,31 +166,40 @@ def pinned(shape):
     return np.empty(shape, dtype=np.float64)
 
 
-def pass_roofline(precision, reps=20):
-    """Live CUDA-event timing of the dominant kernel (one r2r axis pass over 256^3)
-    on the stream it is launched on; achieved = algorithmic bytes / launch time."""
+def pass_roofline(precision, reps=10):
+    """Live CUDA-event timing of the dominant kernel -- one r2r axis pass over the
+    256^3 field -- on the stream it is launched on, with L2 flushed (a 256 MiB write)
+    before every timed launch. Returns the mean pass time over the three axes (ms),
+    the per-axis times and the algorithmic bytes of one pass (one read + one write)."""
     import torch
     from smaiso_wcomp_gb300 import abi
     from smaiso_wcomp_gb300.engine import R2RPlan
     dt = torch.float32 if precision == abi.SWC_PREC_MIXED else torch.float64
-    x = torch.randn((N, N, N), dtype=dt, device="cuda")
-    plan = R2RPlan((N, N, N), (0, 0, 0), precision)
+    x = torch.randn((N, N, N), dtype=dt, device="cuda") * 1e-3
+    flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
+    plans = [R2RPlan((N, N, N), (0, 0, 0), precision), R2RPlan((N, N, N), (1, 1, 1), precision)]
     s = torch.cuda.Stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    per_axis = []
     with torch.cuda.stream(s):
-        for _ in range(3):
-            plan.execute_device(x.data_ptr(), s.cuda_stream)
-        ev0.record(s)
-        for _ in range(reps):
-            plan.execute_device(x.data_ptr(), s.cuda_stream)
-        ev1.record(s)
-    ev1.synchronize()
-    ms_pass = ev0.elapsed_time(ev1) / (3 * reps)   # 3 axis passes per 3D transform
+        for axis in (2, 1, 0):
+            times = []
+            for r in range(reps + 2):
+                flush.zero_()
+                ev0.record(s)
+                plans[r % 2].execute_axis(axis, x.data_ptr(), s.cuda_stream)   # DCT-II, DCT-III alternate
+                ev1.record(s)
+                ev1.synchronize()
+                x.mul_(1.0 / (2 * N))      # keep the field bounded (outside the timed region)
+                if r >= 2:
+                    times.append(ev0.elapsed_time(ev1))
+            per_axis.append(float(np.median(times)))
     elem = 4 if precision == abi.SWC_PREC_MIXED else 8
-    alg_bytes = 2 * N ** 3 * elem                   # one read + one write of the field
-    del x
-    plan.close()
-    return ms_pass, alg_bytes
+    alg_bytes = 2 * N ** 3 * elem
+    del x, flush
+    for pl in plans:
+        pl.close()
+    return float(np.mean(per_axis)), per_axis, alg_bytes
 
 
 def load_peaks():
@@ -299,16 +308,17 @@ def main():
     e2e_sps, h2d, d2h = time_e2e(p_mix, psi_h, rho_h, max(10, min(args.steps, 50)))
 
     peaks, peak_kind = load_peaks()
-    ms_pass, alg = pass_roofline(abi.SWC_PREC_MIXED)
+    ms_pass, axes_ms, alg = pass_roofline(abi.SWC_PREC_MIXED)
     achieved = alg / (ms_pass * 1e-3) / 1e9
-    ms_pass64, alg64 = pass_roofline(abi.SWC_PREC_FP64)
+    ms_pass64, axes64_ms, alg64 = pass_roofline(abi.SWC_PREC_FP64)
     fp64_peak = device_fma_peak(abi.SWC_PREC_FP64)
-    # FP64 pass flops: FFT part ~ (17/4) M log2 M + pre/post, counted per launch from the
-    # operation count of the kernel (see profiles/): 5 N log2 N real flops per line
-    fp64_flops = 5.0 * N * np.log2(N) * N * N
+    # algorithmic flops of one r2r axis pass: (2.5 log2 n + 8) n per line of length n
+    # (real-data FFT plus the DCT pre/post twiddles), n^2 lines
+    fp64_flops = (2.5 * np.log2(N) + 8.0) * N ** 3
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": PASS_TRAFFIC.get("fp32"),
-                "kernel": "r2r_pass_kernel<float, K_C2> (one axis pass, 256^3)",
+                "kernel": "r2r_pass_kernel<float> (one axis pass, 256^3, mean of z/y/x)",
+                "pass_ms_zyx": axes_ms, "alg_bytes_per_launch": alg,
                 "peak_source": f"{peak_kind} hbm_gbs"}
     line = {
         "metric": METRIC, "value": sps_mix * world, "unit": "steps/s", "n_gpus": world, "steps": args.steps,

@@ -217,6 +217,10 @@ int swc_r2r_plan_destroy(swc_r2r_plan* plan);
  * on `stream` (a cudaStream_t; NULL = legacy default stream). Allocates nothing. */
 int swc_r2r_execute(swc_r2r_plan* plan, void* dev_inout, void* stream);
 
+/* One axis pass of the plan (axis 0 = x, 1 = y, 2 = z), in place on device memory;
+ * swc_r2r_execute is the passes z, y, x in turn. */
+int swc_r2r_execute_axis(swc_r2r_plan* plan, int axis, void* dev_inout, void* stream);
+
 /* Host convenience: copies in, transforms, copies out (out may equal in). The
  * data is double on the host for both precisions. */
 int swc_r2r_execute_host(swc_r2r_plan* plan, const double* in, double* out);

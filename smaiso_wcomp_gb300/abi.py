@@ -41,7 +41,7 @@ EXPORTS = [
     "swc_get_field", "swc_field_device_ptr", "swc_get_step", "swc_last_step_ms",
     "swc_last_step_launches", "swc_device_fma_peak",
     "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
-    "swc_r2r_execute", "swc_r2r_execute_host",
+    "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host",
 ]
 
 
@@ -140,6 +140,7 @@ def load_library(path=None):
         "swc_r2r_plan_create": (ctypes.c_int, [ctypes.c_int] * 7 + [P(vp)]),
         "swc_r2r_plan_destroy": (ctypes.c_int, [vp]),
         "swc_r2r_execute": (ctypes.c_int, [vp, vp, vp]),
+        "swc_r2r_execute_axis": (ctypes.c_int, [vp, ctypes.c_int, vp, vp]),
         "swc_r2r_execute_host": (ctypes.c_int, [vp, dp, dp]),
     }
     for name, (res, args) in sig.items():

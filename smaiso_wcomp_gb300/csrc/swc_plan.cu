@@ -131,6 +131,18 @@ int swc_r2r_execute(swc_r2r_plan* p, void* dev_inout, void* stream) {
   return p->precision == SWC_PREC_FP64 ? execute<double>(p, dev_inout, s) : execute<float>(p, dev_inout, s);
 }
 
+int swc_r2r_execute_axis(swc_r2r_plan* p, int axis, void* dev_inout, void* stream) {
+  if (!p || !dev_inout || axis < 0 || axis > 2) { set_error("bad plan, buffer or axis"); return SWC_ERR_BAD_PARAM; }
+  cudaStream_t s = (cudaStream_t)stream;
+  const cudaError_t e = p->precision == SWC_PREC_FP64 ? run_axis<double>(p, axis, (double*)dev_inout, s)
+                                                      : run_axis<float>(p, axis, (float*)dev_inout, s);
+  if (e != cudaSuccess) {
+    set_error("r2r pass failed: %s", cudaGetErrorString(e));
+    return SWC_ERR_CUDA;
+  }
+  return SWC_OK;
+}
+
 int swc_r2r_execute_host(swc_r2r_plan* p, const double* in, double* out) {
   if (!p || !in || !out) { set_error("NULL argument"); return SWC_ERR_BAD_PARAM; }
   const size_t n = (size_t)p->g.ng;

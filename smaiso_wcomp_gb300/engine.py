@@ -133,6 +133,10 @@ class R2RPlan:
         _check(self.lib, self.lib.swc_r2r_execute(self._h, ctypes.c_void_p(dev_ptr), ctypes.c_void_p(stream)),
                "swc_r2r_execute")
 
+    def execute_axis(self, axis, dev_ptr, stream=None):
+        _check(self.lib, self.lib.swc_r2r_execute_axis(self._h, int(axis), ctypes.c_void_p(dev_ptr),
+                                                       ctypes.c_void_p(stream)), "swc_r2r_execute_axis")
+
     def close(self):
         if self._h:
             self.lib.swc_r2r_plan_destroy(self._h)
