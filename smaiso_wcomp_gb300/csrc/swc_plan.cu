@@ -114,6 +114,12 @@ int swc_r2r_plan_create(int nx, int ny, int nz, int kx, int ky, int kz, int prec
                                               : upload_tables<float>(p, a, dims[a], &p->tf[a]);
     if (rc) { swc_r2r_plan_destroy(p); return rc; }
   }
+  // the uploads ran on the legacy stream; execution may use any (non-blocking) stream
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    set_error("r2r plan: table upload failed");
+    swc_r2r_plan_destroy(p);
+    return SWC_ERR_CUDA;
+  }
   *out = p;
   return SWC_OK;
 }

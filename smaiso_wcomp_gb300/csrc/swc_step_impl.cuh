@@ -527,7 +527,9 @@ template <typename T> int StepEngine<T>::init() {
     void* ptr;
     int rc = dalloc(bytes, &ptr);
     if (rc) return rc;
-    SWC_CK(cudaMemcpy(ptr, host, bytes, cudaMemcpyHostToDevice));
+    // stream-ordered: the engine's stream is non-blocking (not ordered after the legacy stream)
+    SWC_CK(cudaMemcpyAsync(ptr, host, bytes, cudaMemcpyHostToDevice, stream_));
+    SWC_CK(cudaStreamSynchronize(stream_));
     *out = ptr;
     return SWC_OK;
   };
@@ -573,9 +575,10 @@ template <typename T> int StepEngine<T>::init() {
                  &dq_, &v_[0], &v_[1], &v_[2], &vsolr_[0], &vsolr_[1], &vsolr_[2], &energy_, &nlw_};
   for (T** b : tbufs) {
     if ((rc = dalloc(nt, (void**)b))) return rc;
-    SWC_CK(cudaMemset(*b, 0, nt));
+    SWC_CK(cudaMemsetAsync(*b, 0, nt, stream_));
   }
-  for (double** b : dbufs) SWC_CK(cudaMemset(*b, 0, nd));
+  for (double** b : dbufs) SWC_CK(cudaMemsetAsync(*b, 0, nd, stream_));
+  SWC_CK(cudaStreamSynchronize(stream_));
   int sms = 0;
   SWC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p_.device));
   diag_blocks_ = sms * 4;
@@ -860,7 +863,8 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   SWC_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
   last_ms_ = ms;
   double sums[5];
-  SWC_CK(cudaMemcpy(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost));
+  SWC_CK(cudaMemcpyAsync(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost, stream_));
+  SWC_CK(cudaStreamSynchronize(stream_));
   // REF:2244-2258
   diag_.sum_abs_dpsi = sums[0];
   diag_.sum_abs_psi = sums[1];
@@ -921,10 +925,12 @@ template <typename T> int StepEngine<T>::get_field(int field, double* dst) {
   SWC_CK(cudaStreamSynchronize(stream_));
   const size_t n = (size_t)g_.ng;
   if (is_d || std::is_same<T, double>::value) {
-    SWC_CK(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost));
+    SWC_CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    SWC_CK(cudaStreamSynchronize(stream_));
   } else {
     std::vector<T> tmp(n);
-    SWC_CK(cudaMemcpy(tmp.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost));
+    SWC_CK(cudaMemcpyAsync(tmp.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+    SWC_CK(cudaStreamSynchronize(stream_));
     for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i];
   }
   return SWC_OK;
@@ -968,13 +974,17 @@ template <typename T> int StepEngine<T>::save(const char* path) {
   const void* dsrc[] = {psiq_, psiq_old_, rho_, frho_};
   for (const void* s : dsrc) {
     if (!ok) break;
-    if (cudaMemcpy(buf.data(), s, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+    if (cudaMemcpyAsync(buf.data(), s, n * sizeof(double), cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
+        cudaStreamSynchronize(stream_) != cudaSuccess)
+      ok = false;
     else ok = std::fwrite(buf.data(), 1, n * sizeof(double), f) == n * sizeof(double);
   }
   const void* tsrc[] = {nlq_, psi_};
   for (const void* s : tsrc) {
     if (!ok) break;
-    if (cudaMemcpy(buf.data(), s, n * sizeof(T), cudaMemcpyDeviceToHost) != cudaSuccess) ok = false;
+    if (cudaMemcpyAsync(buf.data(), s, n * sizeof(T), cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
+        cudaStreamSynchronize(stream_) != cudaSuccess)
+      ok = false;
     else ok = std::fwrite(buf.data(), 1, n * sizeof(T), f) == n * sizeof(T);
   }
   ok = (std::fclose(f) == 0) && ok;
@@ -987,6 +997,7 @@ template <typename T> int StepEngine<T>::save(const char* path) {
 
 template <typename T> int StepEngine<T>::load(const char* path) {
   SWC_CK(cudaSetDevice(p_.device));
+  SWC_CK(cudaStreamSynchronize(stream_));
   FILE* f = std::fopen(path, "rb");
   if (!f) {
     set_error("cannot open %s", path);
@@ -1006,20 +1017,23 @@ template <typename T> int StepEngine<T>::load(const char* path) {
   for (double* d : ddst) {
     if (!ok) break;
     ok = std::fread(buf.data(), 1, n * sizeof(double), f) == n * sizeof(double);
-    if (ok) ok = cudaMemcpy(d, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) ok = cudaMemcpyAsync(d, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice, stream_) == cudaSuccess &&
+                 cudaStreamSynchronize(stream_) == cudaSuccess;
   }
   T* tdst[] = {nlq_, psi_};
   for (T* d : tdst) {
     if (!ok) break;
     ok = std::fread(buf.data(), 1, n * sizeof(T), f) == n * sizeof(T);
-    if (ok) ok = cudaMemcpy(d, buf.data(), n * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) ok = cudaMemcpyAsync(d, buf.data(), n * sizeof(T), cudaMemcpyHostToDevice, stream_) == cudaSuccess &&
+                 cudaStreamSynchronize(stream_) == cudaSuccess;
   }
   std::fclose(f);
   if (!ok) {
     set_error("checkpoint %s is truncated or unreadable", path);
     return SWC_ERR_IO;
   }
-  SWC_CK(cudaMemcpy(psi_old_, psi_, n * sizeof(T), cudaMemcpyDeviceToDevice));
+  SWC_CK(cudaMemcpyAsync(psi_old_, psi_, n * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  SWC_CK(cudaStreamSynchronize(stream_));
   nloop_ = h.nloop;
   have_state_ = true;
   have_vsol_ = false;

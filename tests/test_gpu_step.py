@@ -48,11 +48,15 @@ def test_fp64_step_parity(lib, oracle_mod, shape, kw, gen, schedule):
         rho = None  # the reference's own start: rho = 0 (REF:1053)
     o, e = run_pair(oracle_mod, p, psi, rho, schedule)
     errs = {f: rel(e.field(f), o.field(f)) for f in FIELDS}
-    # v_sol is a cancellation (S - q (q.S)/|q|^2) that vanishes for layered states; its
-    # error is measured against the scale of the full velocity of the same component
-    for c in "xyz":
-        vs, v = o.field("vsol" + c), o.field("v" + c)
-        errs["vsol" + c] = np.linalg.norm(e.field("vsol" + c) - vs) / max(np.linalg.norm(v), 1e-300)
+    # Components of vector fields are measured against the norm of the whole vector:
+    # in (nearly) layered states the x and y components and v_sol are cancellations
+    # (rounding noise of both codes), so a per-component relative error is meaningless.
+    vectors = {"gpsi": ["gpsix", "gpsiy", "gpsiz"], "grho": ["grhox", "grhoy", "grhoz"],
+               "v": ["vx", "vy", "vz", "vsolx", "vsoly", "vsolz"]}
+    for comps in vectors.values():
+        scale = np.sqrt(sum(np.linalg.norm(o.field(c)) ** 2 for c in comps[:3]))
+        for c in comps:
+            errs[c] = np.linalg.norm(e.field(c) - o.field(c)) / max(scale, 1e-300)
     bad = {f: v for f, v in errs.items() if not v <= FP64_TOL}
     assert not bad, bad
     do, de = o.diagnostics(), e.diagnostics()
@@ -75,7 +79,8 @@ def test_mixed_step_accuracy(lib, oracle_mod):
             assert rel(e.field(f), o.field(f)) <= 1e-5, f
         for f in ("vx", "vy", "vz"):
             assert rel(e.field(f), o.field(f)) <= 1e-3, f
-        assert abs(e.diagnostics()["mass"] - o.diagnostics()["mass"]) <= 1e-9 * abs(o.diagnostics()["mass"])
+        # mass: FP64 sums of an FP64 density advanced with FP32 sources
+        assert abs(e.diagnostics()["mass"] - o.diagnostics()["mass"]) <= 1e-7 * abs(o.diagnostics()["mass"])
 
 
 def test_zero_state_fixed_point(lib):
@@ -138,15 +143,19 @@ def test_watchdog_returns_timeout_and_context_recovers(lib):
 
 
 def test_full_size_fp64_vs_mixed_256(lib):
-    """At 256^3: a few steps of both engines stay finite and agree (mixed within 1e-5 on psi)."""
-    p = abi.default_params(256, rho_0=0.8, divv_switch=3)
+    """At 256^3, with both engines alive in one process (each on its own non-blocking
+    stream): a few steps stay finite and agree (mixed within 1e-5 on psi)."""
+    engines = {}
+    for prec in (abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED):
+        engines[prec] = Engine(abi.default_params(256, rho_0=0.8, divv_switch=3, precision=prec))
+    p = engines[0].p
     psi, rho = ic.undulated_interface(p)
     out = {}
-    for prec in (abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED):
-        p.precision = prec
-        with Engine(p) as e:
-            e.set_state(psi, rho)
-            e.step(5)
-            out[prec] = (e.field("psi"), e.diagnostics())
+    for prec, e in engines.items():
+        e.set_state(psi, rho)
+        e.step(5)
+        out[prec] = (e.field("psi"), e.diagnostics())
+    for e in engines.values():
+        e.close()
     assert out[0][1]["nonfinite"] == 0 and out[1][1]["nonfinite"] == 0
     assert rel(out[1][0], out[0][0]) <= 1e-5
