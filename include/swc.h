@@ -197,6 +197,32 @@ int swc_last_step_launches(swc_ctx* ctx, int64_t* launches);
  * the ALU-bound FP64 kernels. */
 int swc_device_fma_peak(int precision, double* tflops);
 
+/* Allocation-free variant of the diagnostic reduction. No counterpart in the
+ * reference (its sums are plain loops, REF:2214-2231); same arithmetic as the
+ * reduction behind swc_diagnostics, applied to caller-owned FP64 device fields of
+ * nx*ny*nz doubles: psi (new), psi_old, rho, lpsi (dfDlapPsi) and amp. Geometry and
+ * coefficients come from *p (only dt, nw, q0, ep, beta, gamma, zeta and rho_0 are read
+ * besides the grid). Result in *out (step = -1); the call returns after `stream` (a
+ * cudaStream_t, NULL = legacy default stream) has finished the reduction.
+ *
+ * For callers that must not allocate device memory at this point: a host code that
+ * gave this library a fixed device budget and lets its own allocator own the rest, a
+ * latency-critical loop that cannot pay cudaFree's wait for all outstanding device
+ * work, or a job that may not grow its device footprint on a shared GPU. It calls no
+ * cudaMalloc/cudaFree and no allocating library routine: its scratch is a fixed
+ * 160 KiB array inside the library, held by every device that loads the library until
+ * the process exits. Limits and rules:
+ *   - at most SWC_NOALLOC_MAX_POINTS grid points (SWC_ERR_BAD_PARAM beyond);
+ *   - the first call on a device looks up the array's device address (set-up, once
+ *     per device, for the current device): make that first call before any stream
+ *     capture;
+ *   - every call shares the one array per device: calls that overlap on the GPU (on
+ *     different streams or threads) race. Each call writes every scratch slot it
+ *     reads, so no clearing is needed between calls. */
+#define SWC_NOALLOC_MAX_POINTS (1LL << 28)
+int swc_diagnostics_noalloc(const swc_params* p, const double* psi, const double* psi_old, const double* rho,
+                            const double* lpsi, const double* amp, void* stream, swc_diag* out);
+
 /* ---- full-state checkpoint (lossless; the reference's psi<rank>.dat text dump
  *      at :2334-2345 keeps only psi at 6 digits) ------------------------------ */
 int swc_save(swc_ctx* ctx, const char* path);

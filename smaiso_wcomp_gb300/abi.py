@@ -39,7 +39,7 @@ EXPORTS = [
     "swc_abi_version", "swc_strerror", "swc_last_error", "swc_default_params", "swc_derive",
     "swc_create", "swc_destroy", "swc_set_state", "swc_step", "swc_diagnostics",
     "swc_get_field", "swc_field_device_ptr", "swc_get_step", "swc_last_step_ms",
-    "swc_last_step_launches", "swc_device_fma_peak",
+    "swc_last_step_launches", "swc_device_fma_peak", "swc_diagnostics_noalloc",
     "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
     "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host",
 ]
@@ -135,6 +135,7 @@ def load_library(path=None):
         "swc_last_step_ms": (ctypes.c_int, [vp, dp]),
         "swc_last_step_launches": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
         "swc_device_fma_peak": (ctypes.c_int, [ctypes.c_int, dp]),
+        "swc_diagnostics_noalloc": (ctypes.c_int, [P(SwcParams), vp, vp, vp, vp, vp, vp, P(SwcDiag)]),
         "swc_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "swc_load": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "swc_r2r_plan_create": (ctypes.c_int, [ctypes.c_int] * 7 + [P(vp)]),
