@@ -90,7 +90,7 @@ template <typename C> struct Dft<1, C> {
 // One radix-R Stockham stage for butterfly jb of one line (complex rows of pitch P).
 template <int R, typename C>
 __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __restrict__ dst, int M, int Ns,
-                                               int P, int l, int jb, const C* __restrict__ tw) {
+                                               int P, int l, int jb, const C* tw) {
   C v[R];
   const int stride = M / R;
 #pragma unroll
@@ -99,7 +99,7 @@ __device__ __forceinline__ void stockham_stage(const C* __restrict__ src, C* __r
   if (Ns > 1) {
     const int tstep = M / (Ns * R);
 #pragma unroll
-    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * jj * tstep]));
+    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * jj * tstep]);
   }
   Dft<R, C>::run(v);
   const int base = (jb - jj) * R + jj;
@@ -176,7 +176,7 @@ __device__ __forceinline__ void run_stages(const PassShape& ps, cx_t<T>*& src, c
 // DCT-III pre-processing: real input (natural order, `in` reals) -> swapped Z in `out`.
 template <typename T>
 __device__ __forceinline__ void dct3_pre(const PassShape& ps, const T* in, cx_t<T>* out, int l, int tj,
-                                         const cx_t<T>* __restrict__ pre) {
+                                         const cx_t<T>* pre) {
   using C = cx_t<T>;
   const int n = ps.n, M = n >> 1, P = ps.P;
   for (int k = tj; k < M; k += ps.tpl) {
@@ -184,7 +184,7 @@ __device__ __forceinline__ void dct3_pre(const PassShape& ps, const T* in, cx_t<
     const T xnk = (k == 0) ? (T)0 : in[ridx(n - k, l, P)];
     const T xmk = in[ridx(M - k, l, P)];
     const T xmpk = in[ridx(M + k, l, P)];
-    const C a = __ldg(&pre[2 * k]), b = __ldg(&pre[2 * k + 1]);
+    const C a = pre[2 * k], b = pre[2 * k + 1];
     const C U = cmake<C>(xk, -xnk);
     const C Um = cmake<C>(xmk, -xmpk);
     const C Z = cadd(cmul(a, U), cmulc(b, Um));
@@ -196,13 +196,13 @@ __device__ __forceinline__ void dct3_pre(const PassShape& ps, const T* in, cx_t<
 // output order reversed for DST-II and an optional spectral multiplier (filter pass).
 template <typename T, int KIND, class MulOp>
 __device__ __forceinline__ void dct2_post(const Grid& g, const PassShape& ps, long long id, const cx_t<T>* in, T* out,
-                                          int l, int tj, const cx_t<T>* __restrict__ post, const MulOp& mul) {
+                                          int l, int tj, const cx_t<T>* post, const MulOp& mul) {
   using C = cx_t<T>;
   const int n = ps.n, M = n >> 1, P = ps.P;
   for (int k = tj; k <= M; k += ps.tpl) {
     const C zk = in[(k & (M - 1)) * P + l];
     const C zm = in[((M - k) & (M - 1)) * P + l];
-    const C c = __ldg(&post[2 * k]), d = __ldg(&post[2 * k + 1]);
+    const C c = post[2 * k], d = post[2 * k + 1];
     const C u = cadd(cmul(c, zk), cmulc(d, zm));
     T y0 = u.x;
     if constexpr (KIND == K_FILT) {
@@ -225,10 +225,67 @@ __device__ __forceinline__ void dct2_post(const Grid& g, const PassShape& ps, lo
   }
 }
 
+// Element `e` of a CTA's tile -> (position p along the line, tile line le). The z
+// tile is L consecutive rows (contiguous memory): consecutive threads take
+// consecutive positions. x/y tiles are n rows of L consecutive k: consecutive
+// threads take consecutive lines (consecutive k). Both keep global accesses coalesced.
+__device__ __forceinline__ void tile_elem(const PassShape& ps, int e, int& p, int& le) {
+  if (ps.axis == 2) { p = e & (ps.n - 1); le = e >> ps.log2n; }
+  else { le = e & (ps.L - 1); p = e >> ps.log2L; }
+}
+
+// Element `it` of thread `tid` (elements tid + it*threads of the tile): position p,
+// tile line le, grid coordinates and linear index, computed affinely from the
+// thread's fixed line (x/y passes) or the contiguous tile (z pass).
+__device__ __forceinline__ void elem_coords(const Grid& g, const PassShape& ps, long long line0, int tid, int it,
+                                            int& p, int& le, int& i, int& j, int& k, long long& idx) {
+  if (ps.axis == 2) {
+    const int e = tid + it * (ps.L * ps.tpl);
+    p = e & (ps.n - 1);
+    le = e >> ps.log2n;
+    const long long line = line0 + le;
+    i = (int)(line >> g.ly);
+    j = (int)line & (g.ny - 1);
+    k = p;
+    idx = (line0 << ps.log2n) + e;
+  } else {
+    le = tid & (ps.L - 1);
+    p = (tid >> ps.log2L) + it * ps.tpl;
+    const int line = (int)(line0 + le);
+    if (ps.axis == 1) {
+      i = line >> g.lz;
+      k = line & (g.nz - 1);
+      j = p;
+      idx = ((long long)i << (g.ly + g.lz)) + ((long long)(p << g.lz) + k);
+    } else {
+      j = line >> g.lz;
+      k = line & (g.nz - 1);
+      i = p;
+      idx = ((long long)p << (g.ly + g.lz)) + line;
+    }
+  }
+}
+
+// Copy the twiddle tables a pass needs from global memory into shared memory.
+template <typename T, int KIND>
+__device__ __forceinline__ void stage_tables(const PassShape& ps, const R2RTables<T>& tb, cx_t<T>* sfft,
+                                             cx_t<T>* spost, cx_t<T>* spre) {
+  const int M = ps.n >> 1;
+  for (int t = threadIdx.x; t < M; t += blockDim.x) sfft[t] = __ldg(&tb.fft[t]);
+  if constexpr (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT)
+    for (int t = threadIdx.x; t < 2 * (M + 1); t += blockDim.x) spost[t] = __ldg(&tb.post[t]);
+  if constexpr (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT)
+    for (int t = threadIdx.x; t < 2 * M; t += blockDim.x) spre[t] = __ldg(&tb.pre[t]);
+}
+
 // One axis pass. LoadOp: T(i, j, k, idx); StoreOp: void(i, j, k, idx, T).
 // Every element of the array is loaded exactly once and stored exactly once, so
 // load functors may also update other arrays at the same index.
-template <typename T, int KIND, class LoadOp, class StoreOp, class MulOp = NoMul<T>>
+// ITERS = elements per thread in the load/store phases (n*L/threads = 2*RMAX) when
+// known at compile time: all of a thread's loads are then issued before any shared
+// memory store, and all shared reads before any global store. ITERS = 0: runtime
+// loop (short lines).
+template <typename T, int KIND, int ITERS, class LoadOp, class StoreOp, class MulOp = NoMul<T>>
 __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2RTables<T> tb, LoadOp ld,
                                                        StoreOp st, MulOp mul = MulOp()) {
   using C = cx_t<T>;
@@ -236,25 +293,22 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
   const int n = ps.n, M = n >> 1, L = ps.L, P = ps.P;
   C* bufA = reinterpret_cast<C*>(smem_raw);
   C* bufB = bufA + M * P;
+  C* sfft = bufB + M * P;        // M
+  C* spost = sfft + M;           // 2(M+1)
+  C* spre = spost + 2 * (M + 1);  // 2M
   const int tid = threadIdx.x, nt = blockDim.x;
   const long long line0 = (long long)blockIdx.x * L;
   const int l = tid & (L - 1);
   const int tj = tid >> ps.log2L;
   const long long my_line = line0 + l;
-  const int iters = (n * L) / nt;
   constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT);
+
+  stage_tables<T, KIND>(ps, tb, sfft, spost, spre);
 
   // ---- load: global -> bufA reals ----
   {
     T* ra = reinterpret_cast<T*>(bufA);
-    for (int it = 0; it < iters; ++it) {
-      const int e = tid + it * nt;
-      int p, le;
-      if (ps.axis == 2) { p = e & (n - 1); le = e >> ps.log2n; }
-      else { le = e & (L - 1); p = e >> ps.log2L; }
-      int i, j, k; long long idx;
-      line_coords(g, ps.axis, line0 + le, p, i, j, k, idx);
-      T x = ld(i, j, k, idx);
+    auto place = [&](int p, int le, T x) {
       if constexpr (fwd_in) {
         if (KIND == K_S2 && (p & 1)) x = -x;
         const int q = (p & 1) ? (n - 1 - (p >> 1)) : (p >> 1);
@@ -262,6 +316,35 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
       } else {
         const int pos = (KIND == K_S3) ? (n - 1 - p) : p;
         ra[ridx(pos, le, P)] = x;
+      }
+    };
+    if constexpr (ITERS > 0) {
+      // chunks of CH loads in flight per thread, then their shared-memory stores
+      constexpr int CH = (sizeof(T) == 8) ? 8 : 16;
+#pragma unroll 1
+      for (int c0 = 0; c0 < ITERS; c0 += CH) {
+        T vals[CH];
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          int p, le, i, j, k;
+          long long idx;
+          elem_coords(g, ps, line0, tid, c0 + c, p, le, i, j, k, idx);
+          vals[c] = ld(i, j, k, idx);
+        }
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+          int p, le;
+          tile_elem(ps, tid + (c0 + c) * nt, p, le);
+          place(p, le, vals[c]);
+        }
+      }    } else {
+      const int iters = (n * L) / nt;
+      for (int it = 0; it < iters; ++it) {
+        int p, le, i, j, k;
+        long long idx;
+        tile_elem(ps, tid + it * nt, p, le);
+        line_coords(g, ps.axis, line0 + le, p, i, j, k, idx);
+        place(p, le, ld(i, j, k, idx));
       }
     }
   }
@@ -272,14 +355,14 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
   T* res_real;   // natural-order real output
   bool swapped;  // output components are (im, re)-swapped (inverse FFT result)
   if constexpr (fwd_in) {
-    run_stages<T>(ps, src, dst, l, tj, tb.fft);  // result in src
-    dct2_post<T, KIND, MulOp>(g, ps, my_line, src, reinterpret_cast<T*>(dst), l, tj, tb.post, mul);
+    run_stages<T>(ps, src, dst, l, tj, sfft);  // result in src
+    dct2_post<T, KIND, MulOp>(g, ps, my_line, src, reinterpret_cast<T*>(dst), l, tj, spost, mul);
     __syncthreads();
     if constexpr (KIND == K_FILT) {
       // inverse DCT-III of the filtered spectrum, in the same CTA
-      dct3_pre<T>(ps, reinterpret_cast<const T*>(dst), src, l, tj, tb.pre);
+      dct3_pre<T>(ps, reinterpret_cast<const T*>(dst), src, l, tj, spre);
       __syncthreads();
-      run_stages<T>(ps, src, dst, l, tj, tb.fft);
+      run_stages<T>(ps, src, dst, l, tj, sfft);
       res_real = reinterpret_cast<T*>(src);
       swapped = true;
     } else {
@@ -287,35 +370,59 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
       swapped = false;
     }
   } else {
-    dct3_pre<T>(ps, reinterpret_cast<const T*>(src), dst, l, tj, tb.pre);
+    dct3_pre<T>(ps, reinterpret_cast<const T*>(src), dst, l, tj, spre);
     __syncthreads();
     { C* t = src; src = dst; dst = t; }
-    run_stages<T>(ps, src, dst, l, tj, tb.fft);
+    run_stages<T>(ps, src, dst, l, tj, sfft);
     res_real = reinterpret_cast<T*>(src);
     swapped = true;
   }
 
   // ---- store: result -> global ----
-  for (int it = 0; it < iters; ++it) {
-    const int e = tid + it * nt;
-    int p, le;
-    if (ps.axis == 2) { p = e & (n - 1); le = e >> ps.log2n; }
-    else { le = e & (L - 1); p = e >> ps.log2L; }
-    T y;
+  auto fetch = [&](int p, int le) -> T {
     if (swapped) {
       const int q = (p & 1) ? (n - 1 - (p >> 1)) : (p >> 1);
-      y = res_real[ridx(q, le, P) ^ 1];
+      T y = res_real[ridx(q, le, P) ^ 1];
       if (KIND == K_S3 && (p & 1)) y = -y;
-    } else {
-      y = res_real[ridx(p, le, P)];
+      return y;
     }
-    int i, j, k; long long idx;
-    line_coords(g, ps.axis, line0 + le, p, i, j, k, idx);
-    st(i, j, k, idx, y);
+    return res_real[ridx(p, le, P)];
+  };
+  if constexpr (ITERS > 0) {
+    constexpr int CH = (sizeof(T) == 8) ? 8 : 16;
+#pragma unroll 1
+    for (int c0 = 0; c0 < ITERS; c0 += CH) {
+      T vals[CH];
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        int p, le;
+        tile_elem(ps, tid + (c0 + c) * nt, p, le);
+        vals[c] = fetch(p, le);
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        int p, le, i, j, k;
+        long long idx;
+        elem_coords(g, ps, line0, tid, c0 + c, p, le, i, j, k, idx);
+        st(i, j, k, idx, vals[c]);
+      }
+    }  } else {
+    const int iters = (n * L) / nt;
+    for (int it = 0; it < iters; ++it) {
+      int p, le, i, j, k;
+      long long idx;
+      tile_elem(ps, tid + it * nt, p, le);
+      line_coords(g, ps.axis, line0 + le, p, i, j, k, idx);
+      st(i, j, k, idx, fetch(p, le));
+    }
   }
 }
 
-// Shared-memory bytes of a pass.
-inline size_t pass_smem_bytes(const PassShape& ps, size_t elem) { return 2 * (size_t)(ps.n / 2) * ps.P * 2 * elem; }
+// Shared-memory bytes of a pass: two complex buffers of M rows of pitch P, plus the
+// FFT (M), DCT-II post (2(M+1)) and DCT-III pre (2M) twiddle tables.
+inline size_t pass_smem_bytes(const PassShape& ps, size_t elem) {
+  const size_t M = ps.n / 2;
+  return (2 * M * ps.P + 5 * M + 2) * 2 * elem;
+}
 
 }  // namespace swc

@@ -47,7 +47,7 @@ inline PassShape make_shape(const Grid& g, int axis, size_t elem) {
   ps.nlines = g.ng / ps.n;
   int L = 64;
   while (L > 1 && (L * ps.tpl > 256 || (L > 16 && L * ps.tpl > 128) ||
-                   2 * (size_t)M * (L + 1) * 2 * elem > 72 * 1024 || L > ps.nlines))
+                   (2 * (size_t)M * (L + 1) + 5 * (size_t)M + 2) * 2 * elem > 80 * 1024 || L > ps.nlines))
     L >>= 1;
   ps.L = L;
   ps.log2L = ilog2(L);
@@ -101,7 +101,11 @@ cudaError_t launch_pass(const Grid& g, int axis, const R2RTables<U>& tb, cudaStr
                         MUL mul) {
   const PassShape ps = make_shape(g, axis, sizeof(U));
   const size_t smem = pass_smem_bytes(ps, sizeof(U));
-  auto kern = r2r_pass_kernel<U, KIND, LD, ST, MUL>;
+  // elements per thread in the load/store phases: n / tpl = 2 * (largest radix)
+  const int iters = ps.n / ps.tpl;
+  auto kern = iters == 32   ? r2r_pass_kernel<U, KIND, 32, LD, ST, MUL>
+              : iters == 16 ? r2r_pass_kernel<U, KIND, 16, LD, ST, MUL>
+                            : r2r_pass_kernel<U, KIND, 0, LD, ST, MUL>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
