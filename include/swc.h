@@ -113,7 +113,22 @@ typedef struct swc_params {
   int precision;      /* SWC_PREC_FP64 or SWC_PREC_MIXED */
   int device;         /* CUDA device ordinal */
   double watchdog_s;  /* host watchdog per swc_step call in seconds (<=0: none) */
+  int adjoint_ckpt;   /* 0: no adjoint. K > 0 (FP64 engine): swc_step keeps a state
+                         checkpoint every K steps so swc_backward can recompute the
+                         trajectory; device memory = (steps/K + 1) states of 6 N^3
+                         doubles + one segment tape of K x 22 N^3 doubles. */
 } swc_params;
+
+/* Gradients returned by swc_backward: dL/d(coefficient) of the coefficients the
+ * calibration loss is differentiated against. */
+typedef struct swc_grad {
+  double alpha;  /* d/d alpha   (REF:241) */
+  double beta;   /* d/d beta    (REF:240) */
+  double gamma;  /* d/d gamma   (REF:239) */
+  double nu;     /* d/d nu      (REF:249) */
+  double rho_0;  /* d/d rho_0   (REF:251; the density ratio rho_i/rho_s, rho_s = 1) */
+  int64_t steps; /* steps differentiated (nLoop at the call) */
+} swc_grad;
 
 /* Diagnostics of the last step of a swc_step call (smaiso-wcomp.cpp:2202-2262). */
 typedef struct swc_diag {
@@ -222,6 +237,20 @@ int swc_device_fma_peak(int precision, double* tflops);
 #define SWC_NOALLOC_MAX_POINTS (1LL << 28)
 int swc_diagnostics_noalloc(const swc_params* p, const double* psi, const double* psi_old, const double* rho,
                             const double* lpsi, const double* amp, void* stream, swc_diag* out);
+
+/* ---- discrete adjoint of the time loop ------------------------------------
+ * No counterpart in the reference. Differentiates L(psi(T), rho(T)) after the
+ * swc_step calls made since swc_set_state (T = nLoop), given the host cotangents
+ * dL_dpsi = dL/dpsi(T) and dL_drho = dL/drho(T) (either may be NULL = zero), by the
+ * hand-written transpose of every stage of the step (transposed r2r transforms,
+ * adjoint pointwise terms, transposed staggered Stokes solve, adjoint CN/AB2
+ * update). Recomputes the trajectory segment by segment from the checkpoints kept
+ * by swc_step (params.adjoint_ckpt). Outputs dL/dpsi0 and dL/drho0 with respect to
+ * the arrays passed to swc_set_state (host, nx*ny*nz doubles, either may be NULL)
+ * and the coefficient gradients in *grad. FP64 engine only; the context's state is
+ * the state at step T again when the call returns. */
+int swc_backward(swc_ctx* ctx, const double* dL_dpsi, const double* dL_drho, double* dL_dpsi0,
+                 double* dL_drho0, swc_grad* grad);
 
 /* ---- full-state checkpoint (lossless; the reference's psi<rank>.dat text dump
  *      at :2334-2345 keeps only psi at 6 digits) ------------------------------ */

@@ -40,7 +40,7 @@ EXPORTS = [
     "swc_create", "swc_destroy", "swc_set_state", "swc_step", "swc_diagnostics",
     "swc_get_field", "swc_field_device_ptr", "swc_get_step", "swc_last_step_ms",
     "swc_last_step_launches", "swc_device_fma_peak", "swc_diagnostics_noalloc",
-    "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
+    "swc_backward", "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
     "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host",
 ]
 
@@ -53,7 +53,7 @@ class SwcParams(ctypes.Structure):
         ("nu", ctypes.c_double), ("lambda_", ctypes.c_double), ("zeta", ctypes.c_double),
         ("rho_0", ctypes.c_double), ("divv_switch", ctypes.c_int), ("load", ctypes.c_int),
         ("ref_ranks", ctypes.c_int), ("precision", ctypes.c_int), ("device", ctypes.c_int),
-        ("watchdog_s", ctypes.c_double),
+        ("watchdog_s", ctypes.c_double), ("adjoint_ckpt", ctypes.c_int),
     ]
 
 
@@ -64,6 +64,14 @@ class SwcDiag(ctypes.Structure):
         ("sum_rho", ctypes.c_double), ("sum_energy", ctypes.c_double),
         ("step", ctypes.c_int64), ("nonfinite", ctypes.c_int64),
     ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class SwcGrad(ctypes.Structure):
+    _fields_ = [("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("nu", ctypes.c_double), ("rho_0", ctypes.c_double), ("steps", ctypes.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -85,7 +93,7 @@ def default_params(nx, ny=None, nz=None, **overrides):
     p = SwcParams(nx=nx, ny=ny, nz=nz, nw=8, dt=0.001, alpha=1.0, beta=2.0, gamma=1.0,
                   ep=-0.001, q0=1.0, nu=1.0, lambda_=1.0, zeta=1.0, rho_0=0.01,
                   divv_switch=50, load=0, ref_ranks=2, precision=SWC_PREC_FP64, device=0,
-                  watchdog_s=0.0)
+                  watchdog_s=0.0, adjoint_ckpt=0)
     for k, v in overrides.items():
         setattr(p, "lambda_" if k == "lambda" else k, v)
     return p
@@ -136,6 +144,7 @@ def load_library(path=None):
         "swc_last_step_launches": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
         "swc_device_fma_peak": (ctypes.c_int, [ctypes.c_int, dp]),
         "swc_diagnostics_noalloc": (ctypes.c_int, [P(SwcParams), vp, vp, vp, vp, vp, vp, P(SwcDiag)]),
+        "swc_backward": (ctypes.c_int, [vp, dp, dp, dp, dp, P(SwcGrad)]),
         "swc_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "swc_load": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "swc_r2r_plan_create": (ctypes.c_int, [ctypes.c_int] * 7 + [P(vp)]),

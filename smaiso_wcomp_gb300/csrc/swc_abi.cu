@@ -106,6 +106,10 @@ int validate_params(const swc_params* p) {
     set_error("ref_ranks=%d must be >= 1 and divide nx=%d", p->ref_ranks, p->nx);
     return SWC_ERR_BAD_PARAM;
   }
+  if (p->adjoint_ckpt < 0 || (p->adjoint_ckpt > 0 && p->precision != SWC_PREC_FP64)) {
+    set_error("adjoint_ckpt must be >= 0 and needs precision SWC_PREC_FP64");
+    return SWC_ERR_BAD_PARAM;
+  }
   if (p->divv_switch < 0 || (p->precision != SWC_PREC_FP64 && p->precision != SWC_PREC_MIXED) || p->device < 0) {
     set_error("bad divv_switch / precision / device");
     return SWC_ERR_BAD_PARAM;
@@ -179,6 +183,7 @@ int swc_default_params(swc_params* p, int nx, int ny, int nz) {
   p->precision = SWC_PREC_FP64;
   p->device = 0;
   p->watchdog_s = 0.0;
+  p->adjoint_ckpt = 0;
   return SWC_OK;
 }
 
@@ -277,6 +282,13 @@ int swc_device_fma_peak(int precision, double* tflops) {
     return SWC_ERR_BAD_PARAM;
   }
   return swc::fma_peak(precision, tflops);
+}
+
+int swc_backward(swc_ctx* ctx, const double* dL_dpsi, const double* dL_drho, double* dL_dpsi0, double* dL_drho0,
+                 swc_grad* grad) {
+  SWC_NEED_CTX(ctx);
+  if (!grad) { set_error("grad is NULL"); return SWC_ERR_BAD_PARAM; }
+  SWC_GUARD(ctx->eng->backward(dL_dpsi, dL_drho, dL_dpsi0, dL_drho0, grad));
 }
 
 int swc_save(swc_ctx* ctx, const char* path) {

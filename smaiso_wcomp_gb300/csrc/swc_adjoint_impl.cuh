@@ -1,0 +1,322 @@
+// swc_adjoint_impl.cuh -- the discrete adjoint of the FP64 time step and the
+// segmented recompute behind swc_backward (included by the FP64 engine only).
+//
+// Trajectory: swc_step kept the state every K = adjoint_ckpt steps (swc_set_state
+// kept step 0). swc_backward walks the segments from the last: it restores the
+// segment's first state, reruns its steps keeping a tape of the intermediates each
+// adjoint step reads, then applies the adjoint steps in reverse. Device memory:
+// (T/K + 1) checkpoints of 6 N^3 doubles + K tape slots of kTape N^3 doubles + the
+// adjoint work arrays (kAdj N^3 doubles).
+#pragma once
+
+#include "swc_adjoint_kernels.cuh"
+
+namespace swc {
+
+// tape slot layout (N^3 doubles each)
+enum {
+  TP_PSI = 0, TP_QOLD, TP_QNEW, TP_GPX, TP_GPY, TP_GPZ, TP_GRX, TP_GRY, TP_GRZ, TP_A, TP_L, TP_LAPR,
+  TP_RHOIN, TP_RHONEW, TP_VX, TP_VY, TP_VZ, TP_DIVV, TP_VSX, TP_VSY, TP_VSZ, TP_VIX, TP_VIY, TP_VIZ, kTape
+};
+// adjoint work arrays
+enum {
+  AJ_Q = 0, AJ_QO, AJ_NLO, AJ_R, AJ_F, AJ_NL, AJ_FX, AJ_FY, AJ_FZ, AJ_MU, AJ_A, AJ_PSI, AJ_VX, AJ_VY, AJ_VZ,
+  AJ_GPX, AJ_GPY, AJ_GPZ, AJ_GRX, AJ_GRY, AJ_GRZ, AJ_DIVV, AJ_DOTX, AJ_DOTY, AJ_DOTZ, AJ_SDX, AJ_SDY, AJ_SDZ,
+  AJ_FGPX, AJ_FGPY, AJ_FGPZ, AJ_SX, AJ_SY, AJ_SZ, AJ_FG, AJ_E, AJ_LAPR, AJ_L, AJ_RQ, kAdj
+};
+
+template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_steps) {
+  const size_t ng = (size_t)g_.ng;
+  if (!adj_) {
+    if (cudaMalloc(&adj_, (size_t)kAdj * ng * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&pgrad_, PG_COUNT * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc of the adjoint work arrays failed (%zu MB)", (kAdj * ng * 8) >> 20);
+      return SWC_ERR_OOM;
+    }
+  }
+  if (tape_steps_ < tape_steps) {
+    if (tape_) cudaFree(tape_);
+    tape_ = nullptr;
+    if (cudaMalloc(&tape_, tape_steps * (size_t)kTape * ng * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      tape_steps_ = 0;
+      set_error("cudaMalloc of the adjoint tape failed (%zu MB)", (tape_steps * kTape * ng * 8) >> 20);
+      return SWC_ERR_OOM;
+    }
+    tape_steps_ = tape_steps;
+  }
+  return SWC_OK;
+}
+
+template <typename T>
+int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
+  const size_t ng = (size_t)g_.ng;
+  const double* tp = tape_ + slot * (size_t)kTape * ng;
+  auto TP = [&](int q) { return tp + (size_t)q * ng; };
+  auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
+  const unsigned blocks = (unsigned)((g_.ng + 255) / 256);
+  const AdjScalars sc{p_.ep, p_.alpha, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, p_.q0 * p_.q0, p_.dt,
+                      p_.dt / 2, rho_m_, scale_, p_.nu, p_.lambda + 2 * p_.nu};
+  using LP = LdPlain<double, double>;
+  using SP = StPlain<double, double>;
+  const AxisWeights w2{{0, 0, 0}, 2.0}, wh{{0, 0, 0}, 0.5};
+  auto sine_w = [](int ax, double w) { AxisWeights a{{ax == 0, ax == 1, ax == 2}, w}; return a; };
+
+  // (1) CN/AB2 update (REF:2177-2190)
+  adj_cn_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], sc, first ? 1 : 0, TP(TP_QOLD),
+                                             TP(TP_QNEW), AJ(AJ_Q), AJ(AJ_QO), AJ(AJ_NLO), AJ(AJ_NL), pgrad_);
+  SWC_CK(cudaGetLastError());
+  // (2) grad.f subtracted in spectral space, then Nl-hat = DCT-II^3 Nl -> Nl_bar = DCT-III^3 D0 Nlq_bar
+  adj_dq_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], AJ(AJ_NL), AJ(AJ_FX), AJ(AJ_FY),
+                                             AJ(AJ_FZ));
+  SWC_CK(cudaGetLastError());
+  SWC_TRY((pass<K_C3, 2>(LdW{g_, AJ(AJ_NL), w2}, SP{AJ(AJ_NL)})));
+  SWC_TRY((pass<K_C3, 1>(LP{AJ(AJ_NL)}, SP{AJ(AJ_NL)})));
+  SWC_TRY((pass<K_C3, 0>(LP{AJ(AJ_NL)}, SP{AJ(AJ_NL)})));
+  // (3) density update + Nl in real space (REF:2121-2160)
+  {
+    AdjNlArgs a{AJ(AJ_NL), TP(TP_PSI), TP(TP_A), TP(TP_RHOIN), TP(TP_RHONEW), TP(TP_VX), TP(TP_VY), TP(TP_VZ),
+                TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ), TP(TP_GRX), TP(TP_GRY), TP(TP_GRZ), TP(TP_DIVV),
+                adj_ + AJ_R * ng, adj_ + AJ_F * ng, adj_ + AJ_MU * ng, adj_ + AJ_A * ng, adj_ + AJ_PSI * ng,
+                adj_ + AJ_VX * ng, adj_ + AJ_VY * ng, adj_ + AJ_VZ * ng, adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng,
+                adj_ + AJ_GPZ * ng, adj_ + AJ_GRX * ng, adj_ + AJ_GRY * ng, adj_ + AJ_GRZ * ng,
+                adj_ + AJ_DIVV * ng, pgrad_, sc, relax ? 1 : 0};
+    adj_nl_kernel<<<blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+  }
+  // (4) divv = DCT-III^3 divv-hat -> divv-hat_bar = D0^-1 DCT-II^3 divv_bar;
+  //     v_a = inverse mixed of v-hat_a -> v-hat_bar = W^-1 forward-mixed(v_bar)
+  SWC_TRY((pass<K_C2, 2>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
+  SWC_TRY((pass<K_C2, 1>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
+  SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_DIVV)}, StW{g_, adj_ + AJ_DIVV * ng, wh, 0})));
+  {
+    double* bv[3] = {adj_ + AJ_VX * ng, adj_ + AJ_VY * ng, adj_ + AJ_VZ * ng};
+    SWC_TRY((pass<K_C2, 2>(LP{bv[0]}, SP{bv[0]})));
+    SWC_TRY((pass<K_C2, 1>(LP{bv[0]}, SP{bv[0]})));
+    SWC_TRY((pass<K_S2, 0>(LP{bv[0]}, StW{g_, bv[0], sine_w(0, 0.5), 0})));
+    SWC_TRY((pass<K_C2, 2>(LP{bv[1]}, SP{bv[1]})));
+    SWC_TRY((pass<K_S2, 1>(LP{bv[1]}, SP{bv[1]})));
+    SWC_TRY((pass<K_C2, 0>(LP{bv[1]}, StW{g_, bv[1], sine_w(1, 0.5), 0})));
+    SWC_TRY((pass<K_S2, 2>(LP{bv[2]}, SP{bv[2]})));
+    SWC_TRY((pass<K_C2, 1>(LP{bv[2]}, SP{bv[2]})));
+    SWC_TRY((pass<K_C2, 0>(LP{bv[2]}, StW{g_, bv[2], sine_w(2, 0.5), 0})));
+  }
+  // (5) Stokes solve + divergence (REF:1468-2078)
+  {
+    AdjStokesArgs a{AJ(AJ_VX), AJ(AJ_VY), AJ(AJ_VZ), AJ(AJ_DIVV), TP(TP_VSX), TP(TP_VSY), TP(TP_VSZ), TP(TP_VIX),
+                    TP(TP_VIY), TP(TP_VIZ), adj_ + AJ_DOTX * ng, adj_ + AJ_DOTY * ng, adj_ + AJ_DOTZ * ng,
+                    adj_ + AJ_SDX * ng, adj_ + AJ_SDY * ng, adj_ + AJ_SDZ * ng, adj_ + AJ_FGPX * ng,
+                    adj_ + AJ_FGPY * ng, adj_ + AJ_FGPZ * ng, vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2],
+                    gq_[0], gq_[1], gq_[2], gs_[0], gs_[1], gs_[2], scale_, 1.0 / p_.nu,
+                    1.0 / (p_.lambda + 2 * p_.nu), p_.nu, p_.lambda + 2 * p_.nu, p_.nx / p_.ref_ranks, pgrad_};
+    adj_stokes1_kernel<<<blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+    AdjStokes2Args b{AJ(AJ_DOTX), AJ(AJ_DOTY), AJ(AJ_DOTZ), AJ(AJ_SDX), AJ(AJ_SDY), AJ(AJ_SDZ), AJ(AJ_FGPX),
+                     AJ(AJ_FGPY), AJ(AJ_FGPZ), adj_ + AJ_SX * ng, adj_ + AJ_SY * ng, adj_ + AJ_SZ * ng,
+                     adj_ + AJ_FG * ng, adj_ + AJ_E * ng, vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2],
+                     gq_[0], gq_[1], gq_[2]};
+    adj_stokes2_kernel<<<blocks, 256, 0, stream_>>>(g_, b);
+    SWC_CK(cudaGetLastError());
+  }
+  // (6) forward transforms of S7 (REF:1427-1457) transposed: DCT-II^T = DCT-III D0,
+  //     DST-II^T = DST-III DL, applied in place to the spectral cotangents
+  auto cos_t = [&](double* b) -> int {
+    SWC_TRY((pass<K_C3, 2>(LdW{g_, b, w2}, SP{b})));
+    SWC_TRY((pass<K_C3, 1>(LP{b}, SP{b})));
+    SWC_TRY((pass<K_C3, 0>(LP{b}, SP{b})));
+    return SWC_OK;
+  };
+  SWC_TRY(cos_t(adj_ + AJ_FG * ng));
+  SWC_TRY(cos_t(adj_ + AJ_E * ng));
+  for (int c = 0; c < 2; ++c) {
+    double* bx = adj_ + (c == 0 ? AJ_SX : AJ_FX) * ng;
+    double* by = adj_ + (c == 0 ? AJ_SY : AJ_FY) * ng;
+    double* bz = adj_ + (c == 0 ? AJ_SZ : AJ_FZ) * ng;
+    SWC_TRY((pass<K_C3, 2>(LdW{g_, bx, sine_w(0, 2.0)}, SP{bx})));
+    SWC_TRY((pass<K_C3, 1>(LP{bx}, SP{bx})));
+    SWC_TRY((pass<K_S3, 0>(LP{bx}, SP{bx})));
+    SWC_TRY((pass<K_C3, 2>(LdW{g_, by, sine_w(1, 2.0)}, SP{by})));
+    SWC_TRY((pass<K_S3, 1>(LP{by}, SP{by})));
+    SWC_TRY((pass<K_C3, 0>(LP{by}, SP{by})));
+    SWC_TRY((pass<K_S3, 2>(LdW{g_, bz, sine_w(2, 2.0)}, SP{bz})));
+    SWC_TRY((pass<K_C3, 1>(LP{bz}, SP{bz})));
+    SWC_TRY((pass<K_C3, 0>(LP{bz}, SP{bz})));
+  }
+  // (7) S6 and the relax reset (REF:1363-1425)
+  {
+    AdjS6Args a{AJ(AJ_FG), AJ(AJ_E), AJ(AJ_SX), AJ(AJ_SY), AJ(AJ_SZ), AJ(AJ_FX), AJ(AJ_FY), AJ(AJ_FZ), AJ(AJ_MU),
+                TP(TP_LAPR), TP(TP_RHOIN), TP(TP_L), TP(TP_PSI), TP(TP_A), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ),
+                TP(TP_GRX), TP(TP_GRY), TP(TP_GRZ), adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng, adj_ + AJ_GPZ * ng,
+                adj_ + AJ_GRX * ng, adj_ + AJ_GRY * ng, adj_ + AJ_GRZ * ng, adj_ + AJ_A * ng, adj_ + AJ_PSI * ng,
+                adj_ + AJ_R * ng, adj_ + AJ_LAPR * ng, adj_ + AJ_L * ng, pgrad_, sc, relax ? 1 : 0};
+    adj_s6_kernel<<<blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+  }
+  // (8) S5 (REF:1312-1380)
+  double* blap = adj_ + AJ_LAPR * ng;
+  if (!relax) {
+    // lapR = Delta_s(rho L), Delta_s = DCT-III^3 (-scale q^2) DCT-II^3 is symmetric
+    SWC_TRY((pass<K_C2, 2>(LP{blap}, SP{blap})));
+    SWC_TRY((pass<K_C2, 1>(LP{blap}, SP{blap})));
+    SWC_TRY((pass<K_FILT, 0>(LP{blap}, SP{blap}, MulLap<double>{vq_[0], vq_[1], vq_[2], scale_})));
+    SWC_TRY((pass<K_C3, 1>(LP{blap}, SP{blap})));
+    SWC_TRY((pass<K_C3, 2>(LP{blap}, StAdjLap{TP(TP_L), TP(TP_RHOIN), adj_ + AJ_R * ng, adj_ + AJ_L * ng})));
+  } else {
+    // lapR_raw = DCT-III^3 (-q^2 alpha (q0^2 - q^2) psiq)
+    SWC_TRY((pass<K_C2, 2>(LP{blap}, SP{blap})));
+    SWC_TRY((pass<K_C2, 1>(LP{blap}, SP{blap})));
+    SWC_TRY((pass<K_C2, 0>(LP{blap}, StW{g_, blap, wh, 0})));
+    adj_acc_spec_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], 1, p_.alpha, p_.q0 * p_.q0,
+                                                     blap, TP(TP_QOLD), AJ(AJ_Q), pgrad_);
+    SWC_CK(cudaGetLastError());
+  }
+  // (9) dfDlapPsi = DCT-III^3 (alpha (q0^2 - q^2) psiq)  (REF:1293-1308)
+  {
+    double* bl = adj_ + AJ_L * ng;
+    SWC_TRY((pass<K_C2, 2>(LP{bl}, SP{bl})));
+    SWC_TRY((pass<K_C2, 1>(LP{bl}, SP{bl})));
+    SWC_TRY((pass<K_C2, 0>(LP{bl}, StW{g_, bl, wh, 0})));
+    adj_acc_spec_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], 0, p_.alpha, p_.q0 * p_.q0, bl,
+                                                     TP(TP_QOLD), AJ(AJ_Q), pgrad_);
+    SWC_CK(cudaGetLastError());
+  }
+  // (10) amplitude filter A = F(A_raw) (symmetric) and A_raw = |psi, grad psi| (REF:1254-1289)
+  {
+    double* bA = adj_ + AJ_A * ng;
+    SWC_TRY((pass<K_C2, 2>(LP{bA}, SP{bA})));
+    SWC_TRY((pass<K_C2, 1>(LP{bA}, SP{bA})));
+    SWC_TRY((pass<K_FILT, 0>(LP{bA}, SP{bA}, MulGauss<double>{gq_[0], gq_[1], gq_[2], scale_})));
+    SWC_TRY((pass<K_C3, 1>(LP{bA}, SP{bA})));
+    SWC_TRY((pass<K_C3, 2>(LP{bA}, StAdjAmp{TP(TP_PSI), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ), adj_ + AJ_PSI * ng,
+                                            adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng, adj_ + AJ_GPZ * ng,
+                                            p_.q0 * p_.q0})));
+  }
+  // (11) gradients (REF:1166-1250): grad_a = inverse-mixed(-fac Vs shift X); transpose =
+  //      forward-mixed, output weights, then the shifted scatter into X_bar
+  SWC_CK(cudaMemsetAsync(adj_ + AJ_RQ * ng, 0, ng * sizeof(double), stream_));
+  const long long sx = 1LL << (g_.ly + g_.lz), sy = g_.nz;
+  for (int which = 0; which < 2; ++which) {
+    double* target = which == 0 ? adj_ + AJ_Q * ng : adj_ + AJ_RQ * ng;
+    const double fac = which == 0 ? 1.0 : scale_;
+    double* bgx = adj_ + (which == 0 ? AJ_GPX : AJ_GRX) * ng;
+    double* bgy = adj_ + (which == 0 ? AJ_GPY : AJ_GRY) * ng;
+    double* bgz = adj_ + (which == 0 ? AJ_GPZ : AJ_GRZ) * ng;
+    SWC_TRY((pass<K_C2, 2>(LP{bgx}, SP{bgx})));
+    SWC_TRY((pass<K_C2, 1>(LP{bgx}, SP{bgx})));
+    SWC_TRY((pass<K_S2, 0>(LP{bgx}, StAdjGrad{g_, target, vs_[0], fac, 0, sx, sine_w(0, 0.5)})));
+    SWC_TRY((pass<K_C2, 2>(LP{bgy}, SP{bgy})));
+    SWC_TRY((pass<K_S2, 1>(LP{bgy}, SP{bgy})));
+    SWC_TRY((pass<K_C2, 0>(LP{bgy}, StAdjGrad{g_, target, vs_[1], fac, 1, sy, sine_w(1, 0.5)})));
+    SWC_TRY((pass<K_S2, 2>(LP{bgz}, SP{bgz})));
+    SWC_TRY((pass<K_C2, 1>(LP{bgz}, SP{bgz})));
+    SWC_TRY((pass<K_C2, 0>(LP{bgz}, StAdjGrad{g_, target, vs_[2], fac, 2, 1, sine_w(2, 0.5)})));
+  }
+  // (12) rho-hat = DCT-II^3 rho (REF:1104-1106): rho_bar += DCT-III^3 D0 rhoq_bar
+  {
+    double* rq = adj_ + AJ_RQ * ng;
+    SWC_TRY((pass<K_C3, 2>(LdW{g_, rq, w2}, SP{rq})));
+    SWC_TRY((pass<K_C3, 1>(LP{rq}, SP{rq})));
+    SWC_TRY((pass<K_C3, 0>(LP{rq}, StAcc{adj_ + AJ_R * ng})));
+  }
+  // (13) the step's psi = DCT-III^3 psiq: psiq_bar += D0^-1 DCT-II^3 psi_bar
+  {
+    double* bp = adj_ + AJ_PSI * ng;
+    SWC_TRY((pass<K_C2, 2>(LP{bp}, SP{bp})));
+    SWC_TRY((pass<K_C2, 1>(LP{bp}, SP{bp})));
+    SWC_TRY((pass<K_C2, 0>(LP{bp}, StW{g_, adj_ + AJ_Q * ng, wh, 1})));
+  }
+  return SWC_OK;
+}
+
+template <typename T>
+int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double* dpsi0, double* drho0,
+                                 swc_grad* out) {
+  const int K = p_.adjoint_ckpt;
+  if (K <= 0) {
+    set_error("swc_backward needs params.adjoint_ckpt > 0 at swc_create");
+    return SWC_ERR_BAD_PARAM;
+  }
+  if (!have_state_ || !adj_valid_) {
+    set_error("swc_backward: no trajectory from swc_set_state to differentiate");
+    return SWC_ERR_STATE;
+  }
+  SWC_CK(cudaSetDevice(p_.device));
+  SWC_CK(cudaStreamSynchronize(stream_));
+  const size_t ng = (size_t)g_.ng;
+  const int64_t Tn = nloop_;
+  SWC_TRY(adjoint_alloc((size_t)(Tn < K ? (Tn > 0 ? Tn : 1) : K)));
+  // the final state, restored when the call returns (slot past the trajectory's)
+  const size_t last_slot = (size_t)(Tn / K) + 1;
+  SWC_TRY(save_ckpt(last_slot));
+  auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
+  SWC_CK(cudaMemsetAsync(adj_, 0, (size_t)kAdj * ng * sizeof(double), stream_));
+  SWC_CK(cudaMemsetAsync(pgrad_, 0, PG_COUNT * sizeof(double), stream_));
+  // cotangent of the final state: psi(T) = DCT-III^3 psiq(T), rho(T)
+  if (dpsi) {
+    SWC_CK(cudaMemcpyAsync(AJ(AJ_PSI), dpsi, ng * 8, cudaMemcpyHostToDevice, stream_));
+    using LP = LdPlain<double, double>;
+    using SP = StPlain<double, double>;
+    const AxisWeights wh{{0, 0, 0}, 0.5};
+    SWC_TRY((pass<K_C2, 2>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
+    SWC_TRY((pass<K_C2, 1>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
+    SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_PSI)}, StW{g_, AJ(AJ_Q), wh, 0})));
+  }
+  if (drho) SWC_CK(cudaMemcpyAsync(AJ(AJ_R), drho, ng * 8, cudaMemcpyHostToDevice, stream_));
+  // segments [s0, s1), last first
+  const int64_t nseg = (Tn + K - 1) / K;
+  for (int64_t sg = nseg - 1; sg >= 0; --sg) {
+    const int64_t s0 = sg * K, s1 = std::min<int64_t>(s0 + K, Tn);
+    SWC_TRY(restore_ckpt((size_t)sg));
+    for (int64_t n = s0 + 1; n <= s1; ++n) {
+      double* tp = tape_ + (size_t)(n - s0 - 1) * kTape * ng;
+      SWC_CK(cudaMemcpyAsync(tp + TP_RHOIN * ng, rho_, ng * 8, cudaMemcpyDeviceToDevice, stream_));
+      const bool relax = !(n > p_.divv_switch || p_.load == 1);
+      SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old
+      const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
+                                amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
+                                vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
+      for (int q = 0; q < kTape; ++q)
+        if (src[q]) SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src[q], ng * 8, cudaMemcpyDeviceToDevice, stream_));
+    }
+    for (int64_t n = s1; n > s0; --n) {
+      const bool relax = !(n > p_.divv_switch || p_.load == 1);
+      SWC_TRY(adjoint_step((size_t)(n - s0 - 1), relax, n == 1));
+    }
+  }
+  // swc_set_state: psiq0 = scale DCT-II^3 psi0 = psiq_old0  =>  psi0_bar = scale DCT-III^3 D0 (Q_bar + Qo_bar)
+  const unsigned blocks = (unsigned)((g_.ng + 255) / 256);
+  if (dpsi0) {
+    axpby_kernel<<<blocks, 256, 0, stream_>>>(g_.ng, 1.0, AJ(AJ_Q), 1.0, AJ(AJ_QO), AJ(AJ_PSI));
+    SWC_CK(cudaGetLastError());
+    using LP = LdPlain<double, double>;
+    using SP = StPlain<double, double>;
+    const AxisWeights w2{{0, 0, 0}, 2.0};
+    SWC_TRY((pass<K_C3, 2>(LdW{g_, AJ(AJ_PSI), w2}, SP{AJ(AJ_PSI)})));
+    SWC_TRY((pass<K_C3, 1>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
+    SWC_TRY((pass<K_C3, 0>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
+    axpby_kernel<<<blocks, 256, 0, stream_>>>(g_.ng, scale_, AJ(AJ_PSI), 0.0, nullptr, AJ(AJ_PSI));
+    SWC_CK(cudaGetLastError());
+    SWC_CK(cudaMemcpyAsync(dpsi0, AJ(AJ_PSI), ng * 8, cudaMemcpyDeviceToHost, stream_));
+  }
+  if (drho0) SWC_CK(cudaMemcpyAsync(drho0, AJ(AJ_R), ng * 8, cudaMemcpyDeviceToHost, stream_));
+  double pg[PG_COUNT];
+  SWC_CK(cudaMemcpyAsync(pg, pgrad_, sizeof(pg), cudaMemcpyDeviceToHost, stream_));
+  SWC_TRY(restore_ckpt(last_slot));
+  SWC_CK(cudaStreamSynchronize(stream_));
+  // chain rule through Amp(beta, gamma) and kp = (1 - rho_0)/Amp (REF:250-253); rho_s = 1, rho_m = 1/2
+  const double disc = std::sqrt(9 * p_.beta * p_.beta + 40 * p_.ep * p_.gamma);
+  const double dAmp_dX = 1.0 / (10.0 * amp_);
+  const double dAmp_dbeta = dAmp_dX * (3.0 + 9.0 * p_.beta / disc);
+  const double dAmp_dgamma = dAmp_dX * (20.0 * p_.ep / disc);
+  const double dkp_dAmp = -kp_ / amp_, dkp_drho0 = -1.0 / amp_;
+  out->alpha = pg[PG_ALPHA];
+  out->beta = pg[PG_BETA] + pg[PG_KP] * dkp_dAmp * dAmp_dbeta;
+  out->gamma = pg[PG_GAMMA] + pg[PG_KP] * dkp_dAmp * dAmp_dgamma;
+  out->nu = pg[PG_NU];
+  out->rho_0 = pg[PG_RHO0] + pg[PG_KP] * dkp_drho0;
+  out->steps = Tn;
+  return SWC_OK;
+}
+
+}  // namespace swc

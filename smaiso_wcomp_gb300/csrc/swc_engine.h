@@ -25,6 +25,7 @@ class EngineBase {
   virtual int last_launches(int64_t* n) = 0;
   virtual int save(const char* path) = 0;
   virtual int load(const char* path) = 0;
+  virtual int backward(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out) = 0;
 };
 
 // Dense FMA throughput probe of the current device (TFLOP/s, FMA = 2 flops).

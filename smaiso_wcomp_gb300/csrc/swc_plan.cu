@@ -54,11 +54,17 @@ template <typename T> cudaError_t run_axis(const swc_r2r_plan* p, int axis, T* d
   // FFTW kind -> kernel kind: REDFT10 = DCT-II, REDFT01 = DCT-III, RODFT10 = DST-II, RODFT01 = DST-III
   const LdPlain<T, T> ld{data};
   const StPlain<T, T> st{data};
-  switch (p->kind[axis]) {
-    case SWC_REDFT10: return launch_pass<T, K_C2>(p->g, axis, tb, s, ld, st, NoMul<T>());
-    case SWC_REDFT01: return launch_pass<T, K_C3>(p->g, axis, tb, s, ld, st, NoMul<T>());
-    case SWC_RODFT10: return launch_pass<T, K_S2>(p->g, axis, tb, s, ld, st, NoMul<T>());
-    default: return launch_pass<T, K_S3>(p->g, axis, tb, s, ld, st, NoMul<T>());
+  switch (p->kind[axis] * 3 + axis) {
+#define SWC_CASE(KD, K)                                                                              \
+  case KD * 3 + 0: return launch_pass<T, K, 0>(p->g, tb, s, ld, st, NoMul<T>());                   \
+  case KD * 3 + 1: return launch_pass<T, K, 1>(p->g, tb, s, ld, st, NoMul<T>());                   \
+  case KD * 3 + 2: return launch_pass<T, K, 2>(p->g, tb, s, ld, st, NoMul<T>());
+    SWC_CASE(SWC_REDFT10, K_C2)
+    SWC_CASE(SWC_REDFT01, K_C3)
+    SWC_CASE(SWC_RODFT10, K_S2)
+    SWC_CASE(SWC_RODFT01, K_S3)
+#undef SWC_CASE
+    default: return cudaErrorInvalidValue;
   }
 }
 

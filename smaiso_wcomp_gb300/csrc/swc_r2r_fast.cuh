@@ -198,14 +198,118 @@ __device__ __forceinline__ void fast_pre(cx_t<T>* buf, const cx_t<T>* pre, int l
   __syncthreads();
 }
 
-template <typename T, int N, int KIND, class LoadOp, class StoreOp, class MulOp>
-__global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, int axis, R2RTables<T> tb, LoadOp ld,
-                                                                     StoreOp st, MulOp mul) {
+// Coordinates of position p of line `line` of an x (AX = 0) or y (AX = 1) pass.
+template <int AX>
+__device__ __forceinline__ void xy_coords(const Grid& g, int line, int p, int& i, int& j, int& k, long long& idx) {
+  if constexpr (AX == 1) {
+    i = line >> g.lz;
+    k = line & (g.nz - 1);
+    j = p;
+    idx = ((long long)i << (g.ly + g.lz)) + ((long long)(p << g.lz) + k);
+  } else {
+    j = line >> g.lz;
+    k = line & (g.nz - 1);
+    i = p;
+    idx = ((long long)p << (g.ly + g.lz)) + line;
+  }
+}
+
+// Position along the line of real q of the Makhoul sequence v (v_q = x_p): p = 2q
+// for q < N/2, p = 2(N-1-q)+1 otherwise. The same map places DCT-III outputs.
+template <int N> __device__ __forceinline__ int mk_pos(int q) { return (q < N / 2) ? 2 * q : 2 * (N - 1 - q) + 1; }
+
+// x/y forward kinds: DCT-II post-processing on (k, M-k) pairs with the outputs
+// stored straight to global memory (consecutive lines are consecutive addresses).
+template <typename T, int N, int KIND, int AX, class ST>
+__device__ __forceinline__ void fast_post_store(const Grid& g, int line, const cx_t<T>* buf, const cx_t<T>* post,
+                                                int l, int tj, const ST& st) {
+  using Cf = FastCfg<T, N>;
+  using C = cx_t<T>;
+  constexpr int M = Cf::M, P = Cf::P, TPL = Cf::TPL;
+  constexpr int NP = (M / 2) / TPL;
+  auto put = [&](int pos, T v) {
+    const int o = (KIND == K_S2) ? (N - 1 - pos) : pos;
+    int i, j, k;
+    long long idx;
+    xy_coords<AX>(g, line, o, i, j, k, idx);
+    st(i, j, k, idx, v);
+  };
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const C zk = buf[k * P + l];
+    const C zm = buf[((M - k) & (M - 1)) * P + l];
+    const C u0 = cadd(cmul(post[2 * k], zk), cmulc(post[2 * k + 1], zm));
+    const int km = M - k;
+    const C u1 = cadd(cmul(post[2 * km], zm), cmulc(post[2 * km + 1], zk));
+    put(k, u0.x);
+    put(M - k, u1.x);
+    if (k > 0) {
+      put(N - k, -u0.y);
+      put(M + k, -u1.y);
+    }
+  }
+  if (tj == 0) {
+    const C z = buf[(M / 2) * P + l];
+    const C u = cadd(cmul(post[M], z), cmulc(post[M + 1], z));
+    put(M / 2, u.x);
+    put(M + M / 2, -u.y);
+  }
+}
+
+// x/y inverse kinds: the last radix-R2 stage with its outputs stored straight to
+// global memory: slot m holds the (im, re)-swapped z_m, i.e. v_2m = .y, v_2m+1 = .x,
+// and v_q lands at position mk_pos(q) (negated at odd positions for DST-III).
+template <typename T, int N, int KIND, int AX, class ST>
+__device__ __forceinline__ void fast_last_store(const Grid& g, int line, const cx_t<T>* buf, const cx_t<T>* tw, int l,
+                                                int tj, const ST& st) {
+  using Cf = FastCfg<T, N>;
+  using C = cx_t<T>;
+  constexpr int M = Cf::M, P = Cf::P, TPL = Cf::TPL, R = Cf::R2, NS = Cf::R1;
+  constexpr int NB = M / R, PER = NB / TPL, STRIDE = M / R, TSTEP = M / (NS * R);
+  C v[PER][R];
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int jb = tj + b * TPL;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[b][r] = buf[(jb + r * STRIDE) * P + l];
+    const int jj = jb & (NS - 1);
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[b][r] = cmul(v[b][r], tw[r * jj * TSTEP]);
+    Dft<R, C>::run(v[b]);
+  }
+  auto put = [&](int q, T val) {
+    const int pos = mk_pos<N>(q);
+    if (KIND == K_S3 && (pos & 1)) val = -val;
+    int i, j, k;
+    long long idx;
+    xy_coords<AX>(g, line, pos, i, j, k, idx);
+    st(i, j, k, idx, val);
+  };
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int jb = tj + b * TPL;
+    const int jj = jb & (NS - 1);
+    const int base = (jb - jj) * R + jj;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int m = base + r * NS;
+      put(2 * m, v[b][r].y);
+      put(2 * m + 1, v[b][r].x);
+    }
+  }
+}
+
+template <typename T, int N, int KIND, int AX, class LoadOp, class StoreOp, class MulOp>
+__global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2RTables<T> tb, LoadOp ld, StoreOp st,
+                                                                     MulOp mul) {
   using Cf = FastCfg<T, N>;
   using C = cx_t<T>;
   constexpr int M = Cf::M, L = Cf::L, P = Cf::P, NT = Cf::NT, TPL = Cf::TPL, ITERS = Cf::ITERS, CH = Cf::CH;
+  constexpr int R1 = Cf::R1, R2 = Cf::R2;
   constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT);
   constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT);
+  constexpr bool xy = (AX != 2);  // x/y passes: global memory straight to/from registers
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   C* sfft = buf + M * P;
@@ -215,6 +319,7 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, int
   const int tid = threadIdx.x;
   const long long line0 = (long long)blockIdx.x * L;
   const int l = tid & (L - 1), tj = tid >> Cf::LOG2L;
+  const int my_line = (int)(line0 + l);
 
   for (int t = tid; t < M; t += NT) sfft[t] = __ldg(&tb.fft[t]);
   if constexpr (fwd_in)
@@ -222,46 +327,80 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, int
   if constexpr (inv_out)
     for (int t = tid; t < 2 * M; t += NT) spre[t] = __ldg(&tb.pre[t]);
 
-  // ---- load: CH loads in flight per thread, then their shared-memory stores ----
-#pragma unroll 1
-  for (int c0 = 0; c0 < ITERS; c0 += CH) {
-    T vals[CH];
+  if constexpr (xy && fwd_in) {
+    // ---- x/y forward: load the first radix-R1 butterfly's inputs straight into
+    // registers (z_m = v_2m + i v_2m+1, m = tj + r TPL), DFT, one shared write ----
+    C v[R1];
 #pragma unroll
-    for (int c = 0; c < CH; ++c) {
-      int p, le, i, j, k;
+    for (int r = 0; r < R1; ++r) {
+      const int m = tj + r * TPL;
+      int i, j, k;
       long long idx;
-      fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, axis, line0, tid, c0 + c, p, le, i, j, k, idx);
-      vals[c] = ld(i, j, k, idx);
+      const int p0 = mk_pos<N>(2 * m), p1 = mk_pos<N>(2 * m + 1);
+      xy_coords<AX>(g, my_line, p0, i, j, k, idx);
+      T a = ld(i, j, k, idx);
+      xy_coords<AX>(g, my_line, p1, i, j, k, idx);
+      T b = ld(i, j, k, idx);
+      if constexpr (KIND == K_S2) {
+        if (p0 & 1) a = -a;
+        if (p1 & 1) b = -b;
+      }
+      v[r] = cmake<C>(a, b);
     }
+    Dft<R1, C>::run(v);
 #pragma unroll
-    for (int c = 0; c < CH; ++c) {
-      int p, le, i, j, k;
-      long long idx;
-      fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, axis, line0, tid, c0 + c, p, le, i, j, k, idx);
-      T x = vals[c];
-      if constexpr (fwd_in) {
-        if (KIND == K_S2 && (p & 1)) x = -x;
-        const int q = (p & 1) ? (N - 1 - (p >> 1)) : (p >> 1);
-        rb[fridx<P>(q, le)] = x;
-      } else {
-        rb[fridx<P>((KIND == K_S3) ? (N - 1 - p) : p, le)] = x;
+    for (int r = 0; r < R1; ++r) buf[(tj * R1 + r) * P + l] = v[r];
+    __syncthreads();
+  } else {
+    // ---- load through shared memory: CH loads in flight per thread ----
+#pragma unroll 1
+    for (int c0 = 0; c0 < ITERS; c0 += CH) {
+      T vals[CH];
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        int p, le, i, j, k;
+        long long idx;
+        fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, AX, line0, tid, c0 + c, p, le, i, j, k, idx);
+        vals[c] = ld(i, j, k, idx);
+      }
+#pragma unroll
+      for (int c = 0; c < CH; ++c) {
+        int p, le, i, j, k;
+        long long idx;
+        fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, AX, line0, tid, c0 + c, p, le, i, j, k, idx);
+        T x = vals[c];
+        if constexpr (fwd_in) {
+          if (KIND == K_S2 && (p & 1)) x = -x;
+          const int q = (p & 1) ? (N - 1 - (p >> 1)) : (p >> 1);
+          rb[fridx<P>(q, le)] = x;
+        } else {
+          rb[fridx<P>((KIND == K_S3) ? (N - 1 - p) : p, le)] = x;
+        }
       }
     }
+    __syncthreads();
+    if constexpr (fwd_in) fast_stage<C, M, R1, 1, TPL, P>(buf, sfft, l, tj);
   }
-  __syncthreads();
 
   if constexpr (fwd_in) {
-    fast_stage<C, M, Cf::R1, 1, TPL, P>(buf, sfft, l, tj);
-    fast_stage<C, M, Cf::R2, Cf::R1, TPL, P>(buf, sfft, l, tj);
-    fast_post<T, N, KIND, MulOp>(g, axis, line0 + l, buf, spost, l, tj, mul);
+    fast_stage<C, M, R2, R1, TPL, P>(buf, sfft, l, tj);
+    if constexpr (xy && KIND != K_FILT) {
+      fast_post_store<T, N, KIND, AX>(g, my_line, buf, spost, l, tj, st);
+      return;
+    }
+    fast_post<T, N, KIND, MulOp>(g, AX, line0 + l, buf, spost, l, tj, mul);
   }
   if constexpr (inv_out) {
     fast_pre<T, N>(buf, spre, l, tj);
-    fast_stage<C, M, Cf::R1, 1, TPL, P>(buf, sfft, l, tj);
-    fast_stage<C, M, Cf::R2, Cf::R1, TPL, P>(buf, sfft, l, tj);
+    fast_stage<C, M, R1, 1, TPL, P>(buf, sfft, l, tj);
+    if constexpr (xy) {
+      fast_last_store<T, N, KIND, AX>(g, my_line, buf, sfft, l, tj, st);
+      return;
+    }
+    fast_stage<C, M, R2, R1, TPL, P>(buf, sfft, l, tj);
   }
 
-  // ---- store: batched shared reads, then global stores ----
+  // ---- z store: batched shared reads, then global stores ----
 #pragma unroll 1
   for (int c0 = 0; c0 < ITERS; c0 += CH) {
     T vals[CH];
@@ -269,7 +408,7 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, int
     for (int c = 0; c < CH; ++c) {
       int p, le, i, j, k;
       long long idx;
-      fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, axis, line0, tid, c0 + c, p, le, i, j, k, idx);
+      fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, AX, line0, tid, c0 + c, p, le, i, j, k, idx);
       if constexpr (inv_out) {
         const int q = (p & 1) ? (N - 1 - (p >> 1)) : (p >> 1);
         T y = rb[fridx<P>(q, le) ^ 1];
@@ -283,7 +422,7 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, int
     for (int c = 0; c < CH; ++c) {
       int p, le, i, j, k;
       long long idx;
-      fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, axis, line0, tid, c0 + c, p, le, i, j, k, idx);
+      fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, AX, line0, tid, c0 + c, p, le, i, j, k, idx);
       st(i, j, k, idx, vals[c]);
     }
   }

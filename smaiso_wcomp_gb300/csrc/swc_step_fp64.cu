@@ -1,5 +1,6 @@
 // swc_step_fp64.cu -- the FP64 step engine (every transform and pointwise term in FP64).
 #include "swc_step_impl.cuh"
+#include "swc_adjoint_impl.cuh"
 
 namespace swc {
 int make_engine_fp64(const swc_params& p, EngineBase** out) {

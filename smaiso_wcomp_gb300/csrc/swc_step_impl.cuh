@@ -160,28 +160,34 @@ template <typename T> struct LdNl {
 // (REF:2170-2190). FP64 engine: the reference's expression; mixed engine: the same
 // update in increment form psiq + (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
 // which follows from C1 - C2 = 1/2 and avoids cancelling C1 psiq against psiq_old.
+// The mixed engine reads 1/C2 from an FP64 table (inv_c2, built once in FP64) so
+// the pass does no FP64 division; the FP64 engine evaluates C1, C2 per mode.
 template <typename T> struct StNlUpdate {
   const T* dq;
   double *psiq, *psiq_old;
   T* nlq;
   const double *qx, *qy, *qz;
+  const double* inv_c2;  // mixed engine only
   double ep, alpha, q02, dt, rho_m, dtd2, scale;
   int first;
   int increment;
   __device__ __forceinline__ void operator()(int i, int j, int k, long long idx, T v) const {
     const T nl = v - dq[idx];
     const T nlo = first ? nl : nlq[idx];
-    const double a = qx[i], b = qy[j], c = qz[k];
-    const double mq2 = a * a + b * b + c * c;
-    const double s = q02 - mq2;
-    const double aLin = ep - alpha * (s * s);
-    const double C1 = (2.0 - dt * rho_m * aLin);
-    const double C2 = (1.5 - dt * rho_m * aLin);
     const double pq = psiq[idx], pqo = psiq_old[idx];
     const double src = dtd2 * scale * (3.0 * (double)nl - (double)nlo);
     double pn;
-    if (increment) pn = pq + (0.5 * (pq - pqo) + src) / C2;
-    else pn = (C1 * pq - 0.5 * pqo + src) / C2;
+    if (increment) {
+      pn = pq + (0.5 * (pq - pqo) + src) * inv_c2[idx];
+    } else {
+      const double a = qx[i], b = qy[j], c = qz[k];
+      const double mq2 = a * a + b * b + c * c;
+      const double s = q02 - mq2;
+      const double aLin = ep - alpha * (s * s);
+      const double C1 = (2.0 - dt * rho_m * aLin);
+      const double C2 = (1.5 - dt * rho_m * aLin);
+      pn = (C1 * pq - 0.5 * pqo + src) / C2;
+    }
     psiq_old[idx] = pq;
     psiq[idx] = pn;
     nlq[idx] = nl;
@@ -215,8 +221,8 @@ template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S
   T lapR = a.lapR[idx];
   if (a.relax) {
     // REF:1371-1374: rho reset to rho_0 + kp A during the relax phase
-    const double rho1 = a.rho0;
-    r = rho1 + ((1 - rho1) / a.amp_eq) * (double)A;
+    // rho_1 + ((1 - rho_1)/Amp) A with (1 - rho_1)/Amp = kp evaluated once on the host
+    r = a.rho0 + a.kp * (double)A;
     a.rho[idx] = r;
     lapR = (T)r * lapR;
   }
@@ -240,13 +246,26 @@ template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S
   a.fz[idx] = c * gpz;
 }
 
+// 1/C2 per spectral mode in FP64 (REF:957-958), built once for the mixed engine.
+static __global__ void __launch_bounds__(256) inv_c2_kernel(Grid g, const double* qx, const double* qy, const double* qz,
+                                                     double ep, double alpha, double q02, double dt, double rho_m,
+                                                     double* out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= g.ng) return;
+  const int k = (int)(idx & (g.nz - 1)), j = (int)((idx >> g.lz) & (g.ny - 1)), i = (int)(idx >> (g.ly + g.lz));
+  const double mq2 = qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k];
+  const double s = q02 - mq2;
+  const double aLin = ep - alpha * (s * s);
+  out[idx] = 1.0 / (1.5 - dt * rho_m * aLin);
+}
+
 // S8 + S9 (REF:1479-1974): Stokes solve on the three staggered grids, spectral.
 template <typename T> struct StokesArgs {
   const T *Sx, *Sy, *Sz, *fgrad, *ener;
   T *vsolx, *vsoly, *vsolz, *virrx, *virry, *virrz;
   const T *vqx, *vqy, *vqz, *vsx, *vsy, *vsz;  // wavenumbers
   const T *gqx, *gqy, *gqz, *gsx, *gsy, *gsz;  // exp(-1.57^2 2 q^2) per axis
-  T scale, nu, lam2nu;
+  T scale, inv_nu, inv_lam2nu;  // 1/nu, 1/(lambda + 2 nu)
   int block;  // x-slab size of the reference decomposition (REF:299)
 };
 
@@ -266,11 +285,12 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
     const T Sz = (k != 0) ? a.Sz[idx + sx - 1] : (T)0;
     const T dot = sxi * Sxc + qyj * Sy + qzk * Sz;
     const T mq2 = sxi * sxi + qyj * qyj + qzk * qzk;
-    const T CM1 = a.scale / mq2, CM2 = sxi / mq2;
+    const T inv = (T)1 / mq2;
+    const T CM1 = a.scale * inv, CM2 = sxi * inv;
     const long long n1 = idx + sx;
     const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i + 1] * a.gqy[j] * a.gqz[k]);
-    vs = (CM1 / a.nu) * (Sxc - CM2 * dot);
-    vi = (CM1 / a.lam2nu) * (sxi * fg + CM2 * dot * (a.gsx[i] * a.gqy[j] * a.gqz[k]));
+    vs = (CM1 * a.inv_nu) * (Sxc - CM2 * dot);
+    vi = (CM1 * a.inv_lam2nu) * (sxi * fg + CM2 * dot * (a.gsx[i] * a.gqy[j] * a.gqz[k]));
   }
   a.vsolx[idx] = vs;
   a.virrx[idx] = vi;
@@ -283,25 +303,27 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
       const T Sz = (k != 0) ? a.Sz[idx + sy - 1] : (T)0;
       const T dot = qxi * Sx + syj * Syc + qzk * Sz;
       const T mq2 = qxi * qxi + syj * syj + qzk * qzk;
-      const T CM1 = a.scale / mq2, CM2 = syj / mq2;
+      const T inv = (T)1 / mq2;
+      const T CM1 = a.scale * inv, CM2 = syj * inv;
       const long long n1 = idx + sy;
       const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i] * a.gqy[j + 1] * a.gqz[k]);
-      ys = (CM1 / a.nu) * (Syc - CM2 * dot);
-      yi = (CM1 / a.lam2nu) * (syj * fg + CM2 * dot * (a.gqx[i] * a.gsy[j] * a.gqz[k]));
+      ys = (CM1 * a.inv_nu) * (Syc - CM2 * dot);
+      yi = (CM1 * a.inv_lam2nu) * (syj * fg + CM2 * dot * (a.gqx[i] * a.gsy[j] * a.gqz[k]));
     }
     {
       const T Sx = (i > 0) ? a.Sx[idx - sx + 1] : (T)0;
       const T Sy = (j != 0) ? a.Sy[idx - sy + 1] : (T)0;
       const T dot = qxi * Sx + qyj * Sy + szk * Szc;
       const T mq2 = qxi * qxi + qyj * qyj + szk * szk;
-      const T CM1 = a.scale / mq2, CM2 = szk / mq2;
+      const T inv = (T)1 / mq2;
+      const T CM1 = a.scale * inv, CM2 = szk * inv;
       const long long n1 = idx + 1;
       const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i] * a.gqy[j] * a.gqz[k + 1]);
       // REF:1932: off the first slab of a rank, the k = 0, j > 0 modes use CM1y's filter
       const bool q1 = (k == 0) && (j > 0) && (i % a.block != 0);
       const T G = q1 ? (a.gqx[i] * a.gsy[j] * a.gqz[k]) : (a.gqx[i] * a.gqy[j] * a.gsz[k]);
-      zs = (CM1 / a.nu) * (Szc - CM2 * dot);
-      zi = (CM1 / a.lam2nu) * (szk * fg + CM2 * dot * G);
+      zs = (CM1 * a.inv_nu) * (Szc - CM2 * dot);
+      zi = (CM1 * a.inv_lam2nu) * (szk * fg + CM2 * dot * G);
     }
   }
   a.vsoly[idx] = ys;
@@ -427,14 +449,34 @@ template <typename T> class StepEngine : public EngineBase {
   }
   int save(const char* path) override;
   int load(const char* path) override;
+  int backward(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out) override {
+    if constexpr (std::is_same<T, double>::value) {
+      return backward_fp64(dpsi, drho, dpsi0, drho0, out);
+    } else {
+      set_error("swc_backward needs the FP64 engine (precision SWC_PREC_FP64)");
+      return SWC_ERR_BAD_PARAM;
+    }
+  }
 
  private:
+  // ---- adjoint support (checkpoints here; the adjoint itself in swc_adjoint_impl.cuh)
+  int save_ckpt(size_t slot);
+  int restore_ckpt(size_t slot);
+  int backward_fp64(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
+  int adjoint_step(size_t slot, bool relax, bool first);
+  int adjoint_alloc(size_t tape_steps);
+  std::vector<double*> ckpt_;      // state at steps 0, K, 2K, ... (6 arrays each)
+  double* tape_ = nullptr;         // forward intermediates of one segment
+  size_t tape_steps_ = 0;
+  double* adj_ = nullptr;          // adjoint work arrays
+  double* pgrad_ = nullptr;        // parameter-gradient accumulators
+  bool adj_valid_ = false;         // checkpoints describe the run since swc_set_state
   // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
-  template <typename U, int KIND, class LD, class ST, class MUL = NoMul<U>>
-  int passU(int axis, LD ld, ST st, MUL mul = MUL());
-  template <int KIND, class LD, class ST, class MUL = NoMul<T>>
-  int pass(int axis, LD ld, ST st, MUL mul = MUL()) {
-    return passU<T, KIND, LD, ST, MUL>(axis, ld, st, mul);
+  template <typename U, int KIND, int AX, class LD, class ST, class MUL = NoMul<U>>
+  int passU(LD ld, ST st, MUL mul = MUL());
+  template <int KIND, int AX, class LD, class ST, class MUL = NoMul<T>>
+  int pass(LD ld, ST st, MUL mul = MUL()) {
+    return passU<T, KIND, AX, LD, ST, MUL>(ld, st, mul);
   }
   template <typename U> R2RTables<U> tabs(int a) const {
     if constexpr (std::is_same<U, T>::value) return tab_.t[a];
@@ -464,6 +506,7 @@ template <typename T> class StepEngine : public EngineBase {
   T *fgrad_ = nullptr, *ener_ = nullptr, *S_[3] = {}, *f_[3] = {}, *vsol_[3] = {}, *virr_[3] = {};
   T *divv_ = nullptr, *dq_ = nullptr, *v_[3] = {}, *vsolr_[3] = {}, *energy_ = nullptr, *nlw_ = nullptr;
   double *partial_ = nullptr, *dsum_ = nullptr;
+  double* inv_c2_ = nullptr;  // mixed engine: FP64 1/C2 per spectral mode
   int diag_blocks_ = 0;
   std::map<int, cudaGraphExec_t> graphs_;
   std::map<int, int64_t> graph_kernels_;  // kernel nodes per captured variant
@@ -480,6 +523,12 @@ template <typename T> void StepEngine<T>::release() {
   // queued graphs may still run (e.g. after a watchdog timeout): drain before freeing
   if (stream_) cudaStreamSynchronize(stream_);
   cudaGetLastError();
+  for (double* c : ckpt_) cudaFree(c);
+  ckpt_.clear();
+  if (tape_) cudaFree(tape_);
+  if (adj_) cudaFree(adj_);
+  if (pgrad_) cudaFree(pgrad_);
+  tape_ = adj_ = pgrad_ = nullptr;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
   for (void* a : allocs_) cudaFree(a);
@@ -579,6 +628,13 @@ template <typename T> int StepEngine<T>::init() {
   }
   for (double** b : dbufs) SWC_CK(cudaMemsetAsync(*b, 0, nd, stream_));
   SWC_CK(cudaStreamSynchronize(stream_));
+  if constexpr (!std::is_same<T, double>::value) {
+    if ((rc = dalloc(nd, (void**)&inv_c2_))) return rc;
+    inv_c2_kernel<<<(unsigned)((g_.ng + 255) / 256), 256, 0, stream_>>>(
+        g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt, rho_m_, inv_c2_);
+    SWC_CK(cudaGetLastError());
+    SWC_CK(cudaStreamSynchronize(stream_));
+  }
   int sms = 0;
   SWC_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p_.device));
   diag_blocks_ = sms * 4;
@@ -590,9 +646,9 @@ template <typename T> int StepEngine<T>::init() {
 }
 
 template <typename T>
-template <typename U, int KIND, class LD, class ST, class MUL>
-int StepEngine<T>::passU(int axis, LD ld, ST st, MUL mul) {
-  SWC_CK((launch_pass<U, KIND, LD, ST, MUL>(g_, axis, tabs<U>(axis), stream_, ld, st, mul)));
+template <typename U, int KIND, int AX, class LD, class ST, class MUL>
+int StepEngine<T>::passU(LD ld, ST st, MUL mul) {
+  SWC_CK((launch_pass<U, KIND, AX, LD, ST, MUL>(g_, tabs<U>(AX), stream_, ld, st, mul)));
   ++launches_;
   return SWC_OK;
 }
@@ -613,9 +669,9 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
 
   // S1 (REF:1104-1106): rhoq = DCT(rho); the mixed engine transforms rho - (rho_0 + rho_s)/2
   const double rho_off = std::is_same<T, double>::value ? 0.0 : 0.5 * (p_.rho_0 + rho_s_);
-  SWC_TRY((pass<K_C2>(2, LdOffset<T>{rho_, rho_off}, SP{rhoq_})));
-  SWC_TRY((pass<K_C2>(1, LP{rhoq_}, SP{rhoq_})));
-  SWC_TRY((pass<K_C2>(0, LP{rhoq_}, SP{rhoq_})));
+  SWC_TRY((pass<K_C2, 2>(LdOffset<T>{rho_, rho_off}, SP{rhoq_})));
+  SWC_TRY((pass<K_C2, 1>(LP{rhoq_}, SP{rhoq_})));
+  SWC_TRY((pass<K_C2, 0>(LP{rhoq_}, SP{rhoq_})));
   // S1 + S2 (REF:1166-1250): spectral gradients -> inverse mixed transforms
   for (int ax = 0; ax < 3; ++ax) {
     LdGrad<T, double> lpsi{psiq_, vs_[ax], (T)1, ax, nlast[ax], shifts[ax]};
@@ -624,40 +680,40 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
       T* out = which == 0 ? gp_[ax] : gr_[ax];
       // z pass: sine along z only for the z component
       if (ax == 2) {
-        if (which == 0) SWC_TRY((pass<K_S3>(2, lpsi, SP{out})));
-        else SWC_TRY((pass<K_S3>(2, lrho, SP{out})));
+        if (which == 0) SWC_TRY((pass<K_S3, 2>(lpsi, SP{out})));
+        else SWC_TRY((pass<K_S3, 2>(lrho, SP{out})));
       } else {
-        if (which == 0) SWC_TRY((pass<K_C3>(2, lpsi, SP{out})));
-        else SWC_TRY((pass<K_C3>(2, lrho, SP{out})));
+        if (which == 0) SWC_TRY((pass<K_C3, 2>(lpsi, SP{out})));
+        else SWC_TRY((pass<K_C3, 2>(lrho, SP{out})));
       }
-      if (ax == 1) SWC_TRY((pass<K_S3>(1, LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3>(1, LP{out}, SP{out})));
-      if (ax == 0) SWC_TRY((pass<K_S3>(0, LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3>(0, LP{out}, SP{out})));
+      if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
+      if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
     }
   }
   // S3 (REF:1254-1289): amplitude, Gaussian filter
-  SWC_TRY((pass<K_C2>(2, LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
-  SWC_TRY((pass<K_C2>(1, LP{amp_f_}, SP{amp_f_})));
-  SWC_TRY((pass<K_FILT>(0, LP{amp_f_}, SP{amp_f_}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
-  SWC_TRY((pass<K_C3>(1, LP{amp_f_}, SP{amp_f_})));
-  SWC_TRY((pass<K_C3>(2, LP{amp_f_}, SP{amp_f_})));
+  SWC_TRY((pass<K_C2, 2>(LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
+  SWC_TRY((pass<K_C2, 1>(LP{amp_f_}, SP{amp_f_})));
+  SWC_TRY((pass<K_FILT, 0>(LP{amp_f_}, SP{amp_f_}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
+  SWC_TRY((pass<K_C3, 1>(LP{amp_f_}, SP{amp_f_})));
+  SWC_TRY((pass<K_C3, 2>(LP{amp_f_}, SP{amp_f_})));
   // S4 (REF:1293-1308): dfDlapPsi
   const T alpha = (T)p_.alpha, q02 = (T)(p_.q0 * p_.q0);
-  SWC_TRY((pass<K_C3>(2, LdLpsi<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
-  SWC_TRY((pass<K_C3>(1, LP{lpsi_}, SP{lpsi_})));
-  SWC_TRY((pass<K_C3>(0, LP{lpsi_}, SP{lpsi_})));
+  SWC_TRY((pass<K_C3, 2>(LdLpsi<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
+  SWC_TRY((pass<K_C3, 1>(LP{lpsi_}, SP{lpsi_})));
+  SWC_TRY((pass<K_C3, 0>(LP{lpsi_}, SP{lpsi_})));
   // S5 (REF:1312-1380)
   if (!relax) {
-    SWC_TRY((pass<K_C2>(2, LdRhoL<T>{rho_, lpsi_}, SP{lapR_})));
-    SWC_TRY((pass<K_C2>(1, LP{lapR_}, SP{lapR_})));
-    SWC_TRY((pass<K_FILT>(0, LP{lapR_}, SP{lapR_}, MulLap<T>{vq_[0], vq_[1], vq_[2], (T)scale_})));
-    SWC_TRY((pass<K_C3>(1, LP{lapR_}, SP{lapR_})));
-    SWC_TRY((pass<K_C3>(2, LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_C2, 2>(LdRhoL<T>{rho_, lpsi_}, SP{lapR_})));
+    SWC_TRY((pass<K_C2, 1>(LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_FILT, 0>(LP{lapR_}, SP{lapR_}, MulLap<T>{vq_[0], vq_[1], vq_[2], (T)scale_})));
+    SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_C3, 2>(LP{lapR_}, SP{lapR_})));
   } else {
-    SWC_TRY((pass<K_C3>(2, LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
-    SWC_TRY((pass<K_C3>(1, LP{lapR_}, SP{lapR_})));
-    SWC_TRY((pass<K_C3>(0, LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
+    SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
+    SWC_TRY((pass<K_C3, 0>(LP{lapR_}, SP{lapR_})));
   }
   // S5 relax tail + S6 (REF:1363-1425)
   {
@@ -671,26 +727,27 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
   // S7 (REF:1427-1457): forward transforms
   T* cts[2] = {fgrad_, ener_};
   for (T* b : cts) {
-    SWC_TRY((pass<K_C2>(2, LP{b}, SP{b})));
-    SWC_TRY((pass<K_C2>(1, LP{b}, SP{b})));
-    SWC_TRY((pass<K_C2>(0, LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2, 2>(LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2, 1>(LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2, 0>(LP{b}, SP{b})));
   }
   for (int ax = 0; ax < 3; ++ax) {
     T* bs[2] = {S_[ax], f_[ax]};
     for (T* b : bs) {
-      if (ax == 2) SWC_TRY((pass<K_S2>(2, LP{b}, SP{b})));
-      else SWC_TRY((pass<K_C2>(2, LP{b}, SP{b})));
-      if (ax == 1) SWC_TRY((pass<K_S2>(1, LP{b}, SP{b})));
-      else SWC_TRY((pass<K_C2>(1, LP{b}, SP{b})));
-      if (ax == 0) SWC_TRY((pass<K_S2>(0, LP{b}, SP{b})));
-      else SWC_TRY((pass<K_C2>(0, LP{b}, SP{b})));
+      if (ax == 2) SWC_TRY((pass<K_S2, 2>(LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2, 2>(LP{b}, SP{b})));
+      if (ax == 1) SWC_TRY((pass<K_S2, 1>(LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2, 1>(LP{b}, SP{b})));
+      if (ax == 0) SWC_TRY((pass<K_S2, 0>(LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2, 0>(LP{b}, SP{b})));
     }
   }
   // S8 + S9 (REF:1468-1974)
   {
     StokesArgs<T> a{S_[0], S_[1], S_[2], fgrad_, ener_, vsol_[0], vsol_[1], vsol_[2], virr_[0], virr_[1],
                     virr_[2], vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2], gq_[0], gq_[1], gq_[2], gs_[0],
-                    gs_[1], gs_[2], (T)scale_, (T)p_.nu, (T)(p_.lambda + 2 * p_.nu), p_.nx / p_.ref_ranks};
+                    gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu), (T)(1.0 / (p_.lambda + 2 * p_.nu)),
+                    p_.nx / p_.ref_ranks};
     stokes_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
     ++launches_;
@@ -702,43 +759,43 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
     SWC_CK(cudaGetLastError());
     ++launches_;
   }
-  SWC_TRY((pass<K_C3>(2, LP{divv_}, SP{divv_})));
-  SWC_TRY((pass<K_C3>(1, LP{divv_}, SP{divv_})));
-  SWC_TRY((pass<K_C3>(0, LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3, 2>(LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3, 1>(LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3, 0>(LP{divv_}, SP{divv_})));
   // S11 (REF:2093-2117): v = vsol + virr to real space; vsol alone on diagnostic steps
   for (int ax = 0; ax < 3; ++ax) {
     for (int which = 0; which < (diag ? 2 : 1); ++which) {
       T* out = which == 0 ? v_[ax] : vsolr_[ax];
       if (which == 0) {
         LdSum2<T> ld{vsol_[ax], virr_[ax]};
-        if (ax == 2) SWC_TRY((pass<K_S3>(2, ld, SP{out})));
-        else SWC_TRY((pass<K_C3>(2, ld, SP{out})));
+        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
+        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
       } else {
         LP ld{vsol_[ax]};
-        if (ax == 2) SWC_TRY((pass<K_S3>(2, ld, SP{out})));
-        else SWC_TRY((pass<K_C3>(2, ld, SP{out})));
+        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
+        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
       }
-      if (ax == 1) SWC_TRY((pass<K_S3>(1, LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3>(1, LP{out}, SP{out})));
-      if (ax == 0) SWC_TRY((pass<K_S3>(0, LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3>(0, LP{out}, SP{out})));
+      if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
+      if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
     }
   }
   // S12 + S13 + S14 (REF:2121-2190): rho update, Nl, its DCT, the psiq update
   {
     LdNl<T> ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
                rho_, frho_, p_.dt, kp_, p_.zeta, p_.rho_0};
-    SWC_TRY((pass<K_C2>(2, ld, SP{nlw_})));
-    SWC_TRY((pass<K_C2>(1, LP{nlw_}, SP{nlw_})));
-    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0,
+    SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
+    SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
+    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], inv_c2_, p_.ep, p_.alpha, p_.q0 * p_.q0,
                      p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, std::is_same<T, float>::value ? 1 : 0};
-    SWC_TRY((pass<K_C2>(0, LP{nlw_}, st)));
+    SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
   }
   // S14 (REF:2194-2197): psi = iDCT(psiq_new)
   T* pout = diag ? psi_new_ : psi_;
-  SWC_TRY((pass<K_C3>(2, LdPlain<T, double>{psiq_}, SP{pout})));
-  SWC_TRY((pass<K_C3>(1, LP{pout}, SP{pout})));
-  SWC_TRY((pass<K_C3>(0, LP{pout}, SP{pout})));
+  SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
+  SWC_TRY((pass<K_C3, 1>(LP{pout}, SP{pout})));
+  SWC_TRY((pass<K_C3, 0>(LP{pout}, SP{pout})));
   if (diag) {
     DiagArgs<T> a{psi_new_, lpsi_, amp_f_, psi_, psi_old_, energy_, rho_, partial_,
                   p_.ep, p_.beta, p_.gamma, p_.zeta, p_.rho_0, kp_};
@@ -795,9 +852,9 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   const size_t nd = (size_t)g_.ng * sizeof(double), nt = (size_t)g_.ng * sizeof(T);
   // REF:968-982: psiq = scale * DCT(psi), in FP64 for both engines (psi staged in frho_)
   SWC_CK(cudaMemcpyAsync(frho_, psi, nd, cudaMemcpyHostToDevice, stream_));
-  SWC_TRY((passU<double, K_C2>(2, LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
-  SWC_TRY((passU<double, K_C2>(1, LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
-  SWC_TRY((passU<double, K_C2>(0, LdPlain<double, double>{frho_}, StScaleD{psiq_, scale_})));
+  SWC_TRY((passU<double, K_C2, 2>(LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
+  SWC_TRY((passU<double, K_C2, 1>(LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
+  SWC_TRY((passU<double, K_C2, 0>(LdPlain<double, double>{frho_}, StScaleD{psiq_, scale_})));
   // REF:1052-1071 (+ caller's rho); f_rho, Nl_old and the work arrays start at zero
   if (rho) SWC_CK(cudaMemcpyAsync(rho_, rho, nd, cudaMemcpyHostToDevice, stream_));
   else SWC_CK(cudaMemsetAsync(rho_, 0, nd, stream_));
@@ -807,15 +864,47 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
                vsolr_[0], vsolr_[1], vsolr_[2], energy_, lpsi_, mu_};
   for (T* z : zero) SWC_CK(cudaMemsetAsync(z, 0, nt, stream_));
   // REF:984-988: psi = iDCT(psiq)
-  SWC_TRY((pass<K_C3>(2, LdPlain<T, double>{psiq_}, StPlain<T, T>{psi_})));
-  SWC_TRY((pass<K_C3>(1, LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
-  SWC_TRY((pass<K_C3>(0, LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
+  SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, StPlain<T, T>{psi_})));
+  SWC_TRY((pass<K_C3, 1>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
+  SWC_TRY((pass<K_C3, 0>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, nt, cudaMemcpyDeviceToDevice, stream_));  // REF:1010
+  if (p_.adjoint_ckpt > 0) SWC_TRY(save_ckpt(0));
+  adj_valid_ = p_.adjoint_ckpt > 0;
   SWC_CK(cudaStreamSynchronize(stream_));
   nloop_ = 0;
   have_state_ = true;
   have_vsol_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
+  return SWC_OK;
+}
+
+// Checkpoint slot: psiq, psiq_old, Nl_old, rho, f_rho, psi (raw copies, ng*8 bytes each).
+template <typename T> int StepEngine<T>::save_ckpt(size_t slot) {
+  const size_t ng = (size_t)g_.ng;
+  while (ckpt_.size() <= slot) {
+    double* c = nullptr;
+    if (cudaMalloc(&c, 6 * ng * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc for an adjoint checkpoint failed (%zu MB)", (6 * ng * 8) >> 20);
+      return SWC_ERR_OOM;
+    }
+    ckpt_.push_back(c);
+  }
+  double* c = ckpt_[slot];
+  const void* src[6] = {psiq_, psiq_old_, nlq_, rho_, frho_, psi_};
+  const size_t sz[6] = {8, 8, sizeof(T), 8, 8, sizeof(T)};
+  for (int q = 0; q < 6; ++q)
+    SWC_CK(cudaMemcpyAsync(c + q * ng, src[q], ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::restore_ckpt(size_t slot) {
+  const size_t ng = (size_t)g_.ng;
+  const double* c = ckpt_[slot];
+  void* dst[6] = {psiq_, psiq_old_, nlq_, rho_, frho_, psi_};
+  const size_t sz[6] = {8, 8, sizeof(T), 8, 8, sizeof(T)};
+  for (int q = 0; q < 6; ++q)
+    SWC_CK(cudaMemcpyAsync(dst[q], c + q * ng, ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
   return SWC_OK;
 }
 
@@ -837,6 +926,7 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
     const bool relax = !(n > p_.divv_switch || p_.load == 1);
     SWC_TRY(run_graph(relax, n == 1, s == nsteps - 1));
     nloop_ = n;
+    if (p_.adjoint_ckpt > 0 && n % p_.adjoint_ckpt == 0) SWC_TRY(save_ckpt((size_t)(n / p_.adjoint_ckpt)));
   }
   SWC_CK(cudaEventRecord(ev1_, stream_));
   // host watchdog: poll the stream's last event, never spin on the device
@@ -1034,6 +1124,7 @@ template <typename T> int StepEngine<T>::load(const char* path) {
   }
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, n * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
   SWC_CK(cudaStreamSynchronize(stream_));
+  adj_valid_ = false;  // the checkpoints no longer describe this trajectory
   nloop_ = h.nloop;
   have_state_ = true;
   have_vsol_ = false;

@@ -96,35 +96,35 @@ template <typename T> struct HostTables {
   }
 };
 
-template <typename U, int N, int KIND, class LD, class ST, class MUL>
-cudaError_t launch_fast(const Grid& g, int axis, const R2RTables<U>& tb, cudaStream_t stream, LD ld, ST st, MUL mul) {
+template <typename U, int N, int KIND, int AX, class LD, class ST, class MUL>
+cudaError_t launch_fast(const Grid& g, const R2RTables<U>& tb, cudaStream_t stream, LD ld, ST st, MUL mul) {
   using Cf = FastCfg<U, N>;
   const size_t smem = Cf::smem_bytes();
-  auto kern = r2r_fast_kernel<U, N, KIND, LD, ST, MUL>;
+  auto kern = r2r_fast_kernel<U, N, KIND, AX, LD, ST, MUL>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   const unsigned blocks = (unsigned)((g.ng / N) / Cf::L);
-  kern<<<blocks, Cf::NT, smem, stream>>>(g, axis, tb, ld, st, mul);
+  kern<<<blocks, Cf::NT, smem, stream>>>(g, tb, ld, st, mul);
   return cudaGetLastError();
 }
 
 // Launch one axis pass on `stream` (in place or out of place per the functors):
 // the compile-time kernel for line lengths 64..512, the runtime one otherwise.
-template <typename U, int KIND, class LD, class ST, class MUL>
-cudaError_t launch_pass(const Grid& g, int axis, const R2RTables<U>& tb, cudaStream_t stream, LD ld, ST st,
-                        MUL mul) {
+template <typename U, int KIND, int AX, class LD, class ST, class MUL>
+cudaError_t launch_pass(const Grid& g, const R2RTables<U>& tb, cudaStream_t stream, LD ld, ST st, MUL mul) {
+  constexpr int axis = AX;
   const int dims[3] = {g.nx, g.ny, g.nz};
   const int n = dims[axis];
   if (n == 256 && fast_pass_supported<U, 256>(g, axis))
-    return launch_fast<U, 256, KIND, LD, ST, MUL>(g, axis, tb, stream, ld, st, mul);
+    return launch_fast<U, 256, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
   if (n == 128 && fast_pass_supported<U, 128>(g, axis))
-    return launch_fast<U, 128, KIND, LD, ST, MUL>(g, axis, tb, stream, ld, st, mul);
+    return launch_fast<U, 128, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
   if (n == 512 && fast_pass_supported<U, 512>(g, axis))
-    return launch_fast<U, 512, KIND, LD, ST, MUL>(g, axis, tb, stream, ld, st, mul);
+    return launch_fast<U, 512, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
   if (n == 64 && fast_pass_supported<U, 64>(g, axis))
-    return launch_fast<U, 64, KIND, LD, ST, MUL>(g, axis, tb, stream, ld, st, mul);
+    return launch_fast<U, 64, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
   const PassShape ps = make_shape(g, axis, sizeof(U));
   const size_t smem = pass_smem_bytes(ps, sizeof(U));
   auto kern = r2r_pass_kernel<U, KIND, 0, LD, ST, MUL>;
