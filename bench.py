@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: steps/5, >= 10)")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="also run both engines this many steps from the initial state and report psi/rho error")
+    ap.add_argument("--grad-steps", type=int, default=40,
+                    help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="profiling mode: run only this engine's warm-up + timed steps and print its timing")
     return ap.parse_args()
@@ -202,6 +206,50 @@ def pass_roofline(precision, reps=10):
     return float(np.mean(per_axis)), per_axis, alg_bytes
 
 
+def gradient_forward_ratio(steps, ckpt=20, n=128):
+    """Wall time of swc_backward (segment recompute + adjoint steps) over the wall time
+    of the forward steps it differentiates: FP64, n^3, checkpoints every `ckpt` steps."""
+    import torch
+    from smaiso_wcomp_gb300 import abi
+    from smaiso_wcomp_gb300.engine import Engine
+    p = abi.default_params(n, rho_0=0.8, divv_switch=min(50, steps // 2), adjoint_ckpt=ckpt)
+    psi, rho = initial_state(p)
+    e = Engine(p)
+    e.set_state(psi, rho)           # warm-up: graph capture, adjoint buffers
+    e.step(min(steps, ckpt))
+    e.backward(dpsi=np.ones((n, n, n)))
+    e.set_state(psi, rho)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.step(steps)
+    t1 = time.perf_counter()
+    w = np.ones((n, n, n))
+    g = e.backward(dpsi=w)
+    t2 = time.perf_counter()
+    e.close()
+    return {"value": (t2 - t1) / (t1 - t0), "forward_s": t1 - t0, "backward_s": t2 - t1,
+            "config": f"FP64 {n}^3, {steps} steps, checkpoint every {ckpt}, loss sum(psi(T))",
+            "dL_dalpha": g["alpha"]}
+
+
+def accuracy_run(steps, device=0):
+    """Both engines `steps` steps from the same state; relative L2 of psi and rho."""
+    from smaiso_wcomp_gb300 import abi
+    from smaiso_wcomp_gb300.engine import Engine
+    out = {}
+    psi, rho = initial_state(make_params(abi.SWC_PREC_MIXED, device))
+    for prec in (abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED):
+        e = Engine(make_params(prec, device))
+        e.set_state(psi, rho)
+        e.step(steps)
+        out[prec] = (e.field("psi"), e.field("rho"), e.diagnostics())
+        e.close()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    return {"steps": steps, "psi_rel_l2": rel(out[1][0], out[0][0]), "rho_rel_l2": rel(out[1][1], out[0][1]),
+            "mass_rel": abs(out[1][2]["mass"] - out[0][2]["mass"]) / abs(out[0][2]["mass"]),
+            "energy_rel": abs(out[1][2]["energy"] - out[0][2]["energy"]) / abs(out[0][2]["energy"])}
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -330,7 +378,7 @@ def main():
         "grid_point_steps_per_s": sps_mix * world * N ** 3,
         "psi_rel_l2_mixed_vs_fp64": psi_err, "rho_rel_l2_mixed_vs_fp64": rho_err,
         "accuracy_steps": max(nsteps_mix, nsteps_64),
-        "gradient_forward_ratio": None,
+        "gradient_forward_ratio": None,  # filled below
         "e2e": {"value": e2e_sps * world, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roofline,
         "roofline_fp64_pass": {"bound": "fp64_alu", "achieved": fp64_flops / (ms_pass64 * 1e-3) / 1e12,
@@ -341,6 +389,12 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if args.grad_steps > 0:
+        gr = gradient_forward_ratio(args.grad_steps)
+        line["gradient_forward_ratio"] = gr["value"]
+        line["gradient"] = gr
+    if args.accuracy_steps > 0:
+        line["accuracy"] = accuracy_run(args.accuracy_steps, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample_steps)
     if rank == 0:
@@ -349,9 +403,9 @@ def main():
         pg.destroy_process_group()
 
 
-# DRAM bytes per launch of the dominant kernel from the committed ncu capture
-# (profiles/r2r_pass_256.md); None until captured.
-PASS_TRAFFIC = {"fp32": None}
+# DRAM bytes (read + write) per launch of the dominant kernel, mean of its x/z/y passes,
+# from the committed ncu capture profiles/r2r_pass_fp32_n256_256cubed.md.
+PASS_TRAFFIC = {"fp32": 74.3e6}
 
 
 def working_set_gb():

@@ -369,18 +369,18 @@ template <typename T> __global__ void __launch_bounds__(kDiagThreads) diag_kerne
   double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.ng;
        idx += (long long)gridDim.x * blockDim.x) {
-    const double pn = (double)a.psi_new[idx];
-    const double po = (double)a.psi[idx];
+    // per-point terms in the work precision T (FP32 in the mixed engine: its psi, L and
+    // A are FP32), every accumulation in FP64
+    const T pn = a.psi_new[idx], po = a.psi[idx], L = a.lpsi[idx], A = a.amp[idx];
     const double r = a.rho[idx];
-    const double L = (double)a.lpsi[idx];
-    const double A = (double)a.amp[idx];
-    s0 += fabs(pn - po);
-    s1 += fabs(pn);
+    s0 += (double)fabs(pn - po);
+    s1 += (double)fabs(pn);
     s2 += r;
-    const double p2 = pn * pn;
-    const double e = -0.5 * a.ep * p2 + 0.5 * (L * L) - 0.25 * a.beta * (p2 * p2) + (a.gamma / 6) * (p2 * p2 * p2);
-    const double d = r - a.rho0 - a.kp * A;
-    s3 += r * e + 0.5 * a.zeta * (d * d);
+    const T p2 = pn * pn;
+    const T e = (T)(-0.5 * a.ep) * p2 + (T)0.5 * (L * L) - (T)(0.25 * a.beta) * (p2 * p2) +
+                (T)(a.gamma / 6) * (p2 * p2 * p2);
+    const T d = (T)r - (T)a.rho0 - (T)a.kp * A;
+    s3 += (double)((T)r * e + (T)(0.5 * a.zeta) * (d * d));
     s4 += (double)(!isfinite(pn)) + (double)(!isfinite(r));
     a.energy[idx] = (T)e;
     a.psi_old[idx] = a.psi[idx];

@@ -97,6 +97,21 @@ class Engine:
         _check(self.lib, self.lib.swc_last_step_launches(self._h, ctypes.byref(n)), "swc_last_step_launches")
         return n.value
 
+    def backward(self, dpsi=None, drho=None, want_psi0=True, want_rho0=False):
+        """swc_backward: gradients of a loss with dL/dpsi(T) = dpsi, dL/drho(T) = drho."""
+        n = self.shape
+        dp = None if dpsi is None else np.ascontiguousarray(dpsi, dtype=np.float64).reshape(n)
+        dr = None if drho is None else np.ascontiguousarray(drho, dtype=np.float64).reshape(n)
+        o_psi = np.empty(n) if want_psi0 else None
+        o_rho = np.empty(n) if want_rho0 else None
+        g = abi.SwcGrad()
+        ptr = lambda a: None if a is None else abi.as_dptr(a)  # noqa: E731
+        _check(self.lib, self.lib.swc_backward(self._h, ptr(dp), ptr(dr), ptr(o_psi), ptr(o_rho),
+                                               ctypes.byref(g)), "swc_backward")
+        out = g.as_dict()
+        out["psi0"], out["rho0"] = o_psi, o_rho
+        return out
+
     def save(self, path):
         _check(self.lib, self.lib.swc_save(self._h, str(path).encode()), "swc_save")
 

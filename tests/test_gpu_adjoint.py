@@ -1,0 +1,92 @@
+"""Discrete adjoint (swc_backward) against central finite differences of the FP64
+forward through the C ABI, and a torch.autograd.gradcheck over the thin shim."""
+import numpy as np
+import pytest
+
+from smaiso_wcomp_gb300 import abi, ic
+from smaiso_wcomp_gb300.engine import Engine
+
+pytestmark = pytest.mark.gpu
+COEFFS = ("alpha", "beta", "gamma", "nu", "rho_0")
+
+
+def loss(e, wp, wr):
+    return float(np.sum(wp * e.field("psi")) + np.sum(wr * e.field("rho")))
+
+
+def run(p, psi0, rho0, nsteps, wp, wr):
+    with Engine(p) as e:
+        e.set_state(psi0, rho0)
+        for _ in range(nsteps):
+            e.step(1)
+        return loss(e, wp, wr)
+
+
+CASES = [  # shape, divv_switch, steps, checkpoint interval: relax + normal phase, several segments
+    ((16, 16, 32), 3, 6, 2),
+    ((16, 8, 16), 2, 5, 4),
+    ((8, 16, 16), 0, 3, 1),
+]
+
+
+@pytest.mark.parametrize("shape,ds,nsteps,ckpt", CASES)
+def test_adjoint_matches_finite_differences(lib, shape, ds, nsteps, ckpt):
+    rng = np.random.default_rng(7)
+    p = abi.default_params(*shape, rho_0=0.8, divv_switch=ds, adjoint_ckpt=ckpt, ref_ranks=2)
+    psi0, rho0 = ic.undulated_interface(p, sigma=1e-2)
+    wp = rng.standard_normal(shape)
+    wr = rng.standard_normal(shape)
+    with Engine(p) as e:
+        e.set_state(psi0, rho0)
+        e.step(nsteps)
+        L0 = loss(e, wp, wr)
+        g = e.backward(dpsi=wp, drho=wr, want_psi0=True, want_rho0=True)
+        # the state at step T is restored
+        assert abs(loss(e, wp, wr) - L0) <= 1e-14 * abs(L0)
+    assert g["steps"] == nsteps
+    # directional derivative along psi0 and rho0
+    for key, base in (("psi0", psi0), ("rho0", rho0)):
+        d = rng.standard_normal(shape)
+        h = 1e-5
+        args_p = (psi0 + h * d, rho0) if key == "psi0" else (psi0, rho0 + h * d)
+        args_m = (psi0 - h * d, rho0) if key == "psi0" else (psi0, rho0 - h * d)
+        fd = (run(p, *args_p, nsteps, wp, wr) - run(p, *args_m, nsteps, wp, wr)) / (2 * h)
+        ad = float(np.sum(g[key] * d))
+        assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-12 * abs(L0)), (key, ad, fd)
+    # coefficients: 4th-order central difference, h = 1e-3 relative (truncation O(h^4),
+    # rounding ~1e-13 |L| / h): accurate to well below the 1e-6 bar for small gradients
+    errs = {}
+    for name in COEFFS:
+        v = getattr(p, name)
+        h = 1e-3 * max(abs(v), 1e-3)
+
+        def L_at(x):
+            q = abi.SwcParams.from_buffer_copy(p)
+            setattr(q, name, x)
+            return run(q, psi0, rho0, nsteps, wp, wr)
+
+        fd = (8 * (L_at(v + h) - L_at(v - h)) - (L_at(v + 2 * h) - L_at(v - 2 * h))) / (12 * h)
+        errs[name] = (g[name], fd, abs(g[name] - fd) / max(abs(fd), 1e-9))
+    bad = {k: e for k, e in errs.items() if not e[2] <= 1e-6}
+    assert not bad, bad
+
+
+def test_backward_needs_checkpoints_and_fp64(lib):
+    from smaiso_wcomp_gb300.engine import SwcError
+    with Engine(abi.default_params(8)) as e:
+        e.set_state(np.zeros((8, 8, 8)))
+        e.step(1)
+        with pytest.raises(SwcError):
+            e.backward(dpsi=np.zeros((8, 8, 8)))
+
+
+def test_torch_gradcheck_through_the_shim(lib):
+    torch = pytest.importorskip("torch")
+    from smaiso_wcomp_gb300.autograd import StepFunction
+    base = abi.default_params(8, 8, 8, rho_0=0.8, divv_switch=1)
+    psi0, rho0 = ic.undulated_interface(base, sigma=1e-2)
+    x = torch.tensor(psi0, dtype=torch.float64, requires_grad=True)
+    c = torch.tensor([base.alpha, base.beta, base.gamma, base.nu, base.rho_0], dtype=torch.float64,
+                     requires_grad=True)
+    f = lambda x, c: StepFunction.apply(x, c, base, 2, rho0, 1)  # noqa: E731
+    assert torch.autograd.gradcheck(f, (x, c), eps=1e-6, atol=1e-7, rtol=1e-5, fast_mode=True)
