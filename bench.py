@@ -341,13 +341,11 @@ def main():
     e_mix.close()
     e_64.close()
 
-    # max over ranks of the device time
-    t = torch.tensor([ms_mix, ms_64], dtype=torch.float64, device="cuda")
-    if pg:
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    ms_mix, ms_64 = float(t[0]), float(t[1])
-    sps_mix = args.steps / (ms_mix * 1e-3)
-    sps_64 = k64 / (ms_64 * 1e-3)
+    # max over ranks of the device time (replicas: no data-path collective)
+    from smaiso_wcomp_gb300 import replicas
+    ms_mix, ms_64 = replicas.max_over_ranks([ms_mix, ms_64], pg, device="cuda")
+    sps_mix = replicas.job_throughput(args.steps, ms_mix * 1e-3, 1)
+    sps_64 = replicas.job_throughput(k64, ms_64 * 1e-3, 1)
 
     psi_h = pinned((N, N, N))
     rho_h = pinned((N, N, N))
