@@ -8,6 +8,20 @@
 
 #include "swc_r2r.cuh"
 
+// Tuning constants (threads per CTA, loads in flight per thread); defaults measured on GB300.
+#ifndef SWC_FAST_NT_F32
+#define SWC_FAST_NT_F32 256
+#endif
+#ifndef SWC_FAST_NT_F64
+#define SWC_FAST_NT_F64 128
+#endif
+#ifndef SWC_FAST_CH_F32
+#define SWC_FAST_CH_F32 16
+#endif
+#ifndef SWC_FAST_CH_F64
+#define SWC_FAST_CH_F64 8
+#endif
+
 namespace swc {
 
 template <typename T, int N> struct FastCfg {
@@ -16,11 +30,11 @@ template <typename T, int N> struct FastCfg {
   static constexpr int R2 = (M == 32) ? 4 : (M == 64) ? 8 : (M == 128) ? 8 : 16;
   static_assert(R1 * R2 == M, "two-stage plan");
   static constexpr int TPL = M / R1;                              // threads per line
-  static constexpr int NT = (sizeof(T) == 8) ? 128 : 256;         // threads per CTA
+  static constexpr int NT = (sizeof(T) == 8) ? SWC_FAST_NT_F64 : SWC_FAST_NT_F32;  // threads per CTA
   static constexpr int L = NT / TPL;                              // lines per CTA
   static constexpr int P = L + 1;                                 // complex row pitch
   static constexpr int ITERS = N / TPL;                           // load/store elements per thread
-  static constexpr int CH = (sizeof(T) == 8) ? 8 : 16;            // loads in flight per chunk
+  static constexpr int CH = (sizeof(T) == 8) ? SWC_FAST_CH_F64 : SWC_FAST_CH_F32;  // loads in flight per chunk
   static constexpr int LOG2N = (N == 64) ? 6 : (N == 128) ? 7 : (N == 256) ? 8 : 9;
   static constexpr int LOG2L = (L == 8) ? 3 : (L == 16) ? 4 : (L == 32) ? 5 : 6;
   static_assert((1 << LOG2N) == N && (1 << LOG2L) == L, "powers of two");
@@ -44,11 +58,11 @@ __device__ __forceinline__ void fast_elem(const Grid& g, int axis, long long lin
     const int e = tid + it * NT;
     p = e & (N - 1);
     le = e >> LOG2N;
-    const long long line = line0 + le;
-    i = (int)(line >> g.ly);
-    j = (int)line & (g.ny - 1);
+    const int line = (int)line0 + le;
+    i = line >> g.ly;
+    j = line & (g.ny - 1);
     k = p;
-    idx = (line0 << LOG2N) + e;
+    idx = (long long)(((int)line0 << LOG2N) + e);
   } else {
     le = tid & (L - 1);
     p = (tid >> LOG2L) + it * TPL;
@@ -57,12 +71,12 @@ __device__ __forceinline__ void fast_elem(const Grid& g, int axis, long long lin
       i = line >> g.lz;
       k = line & (g.nz - 1);
       j = p;
-      idx = ((long long)i << (g.ly + g.lz)) + ((long long)(p << g.lz) + k);
+      idx = (long long)((i << (g.ly + g.lz)) + (p << g.lz) + k);
     } else {
       j = line >> g.lz;
       k = line & (g.nz - 1);
       i = p;
-      idx = ((long long)p << (g.ly + g.lz)) + line;
+      idx = (long long)((p << (g.ly + g.lz)) + line);
     }
   }
 }
@@ -205,12 +219,12 @@ __device__ __forceinline__ void xy_coords(const Grid& g, int line, int p, int& i
     i = line >> g.lz;
     k = line & (g.nz - 1);
     j = p;
-    idx = ((long long)i << (g.ly + g.lz)) + ((long long)(p << g.lz) + k);
+    idx = (long long)((i << (g.ly + g.lz)) + (p << g.lz) + k);
   } else {
     j = line >> g.lz;
     k = line & (g.nz - 1);
     i = p;
-    idx = ((long long)p << (g.ly + g.lz)) + line;
+    idx = (long long)((p << (g.ly + g.lz)) + line);
   }
 }
 
