@@ -18,6 +18,8 @@ enum {
   TP_PSI = 0, TP_QOLD, TP_QNEW, TP_GPX, TP_GPY, TP_GPZ, TP_GRX, TP_GRY, TP_GRZ, TP_A, TP_L, TP_LAPR,
   TP_RHOIN, TP_RHONEW, TP_VX, TP_VY, TP_VZ, TP_DIVV, TP_VSX, TP_VSY, TP_VSZ, TP_VIX, TP_VIY, TP_VIZ, kTape
 };
+static_assert(PG_COUNT == 8, "pgrad_doubles() assumes 8 parameter slots");
+
 // adjoint work arrays
 enum {
   AJ_Q = 0, AJ_QO, AJ_NLO, AJ_R, AJ_F, AJ_NL, AJ_FX, AJ_FY, AJ_FZ, AJ_MU, AJ_A, AJ_PSI, AJ_VX, AJ_VY, AJ_VZ,
@@ -29,7 +31,7 @@ template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_steps) {
   const size_t ng = (size_t)g_.ng;
   if (!adj_) {
     if (cudaMalloc(&adj_, (size_t)kAdj * ng * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&pgrad_, PG_COUNT * sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&pgrad_, pgrad_doubles() * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
       set_error("cudaMalloc of the adjoint work arrays failed (%zu MB)", (kAdj * ng * 8) >> 20);
       return SWC_ERR_OOM;
@@ -251,7 +253,7 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
   SWC_TRY(save_ckpt(last_slot));
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
   SWC_CK(cudaMemsetAsync(adj_, 0, (size_t)kAdj * ng * sizeof(double), stream_));
-  SWC_CK(cudaMemsetAsync(pgrad_, 0, PG_COUNT * sizeof(double), stream_));
+  SWC_CK(cudaMemsetAsync(pgrad_, 0, pgrad_doubles() * sizeof(double), stream_));
   // cotangent of the final state: psi(T) = DCT-III^3 psiq(T), rho(T)
   if (dpsi) {
     SWC_CK(cudaMemcpyAsync(AJ(AJ_PSI), dpsi, ng * 8, cudaMemcpyHostToDevice, stream_));
@@ -300,6 +302,8 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
     SWC_CK(cudaMemcpyAsync(dpsi0, AJ(AJ_PSI), ng * 8, cudaMemcpyDeviceToHost, stream_));
   }
   if (drho0) SWC_CK(cudaMemcpyAsync(drho0, AJ(AJ_R), ng * 8, cudaMemcpyDeviceToHost, stream_));
+  pg_reduce_kernel<<<PG_COUNT, 256, 0, stream_>>>(pgrad_, blocks);
+  SWC_CK(cudaGetLastError());
   double pg[PG_COUNT];
   SWC_CK(cudaMemcpyAsync(pg, pgrad_, sizeof(pg), cudaMemcpyDeviceToHost, stream_));
   SWC_TRY(restore_ckpt(last_slot));

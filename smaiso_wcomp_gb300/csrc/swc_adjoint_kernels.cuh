@@ -104,8 +104,14 @@ struct StAdjAmp {
   }
 };
 
-// Block sum of v, added atomically to *target (all threads of the block must call).
-__device__ __forceinline__ void block_accum(double v, double* target) {
+// parameter-gradient slots
+enum { PG_ALPHA = 0, PG_BETA = 1, PG_GAMMA = 2, PG_NU = 3, PG_RHO0 = 4, PG_KP = 5, PG_COUNT = 8 };
+
+// Block sum of v added to this block's own cell of parameter slot `slot` (all threads of
+// the block must call). The cells sit after the PG_COUNT totals, gridDim.x per slot, and
+// are summed in a fixed order by pg_reduce_kernel, so the parameter gradients do not
+// depend on the order in which blocks finish (no atomics).
+__device__ __forceinline__ void block_accum(double v, double* pgrad, int slot) {
   __shared__ double sh[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -115,12 +121,27 @@ __device__ __forceinline__ void block_accum(double v, double* target) {
   if (threadIdx.x == 0) {
     double t = 0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += sh[q];
-    atomicAdd(target, t);
+    pgrad[PG_COUNT + (size_t)slot * gridDim.x + blockIdx.x] += t;
   }
 }
 
-// parameter-gradient slots
-enum { PG_ALPHA = 0, PG_BETA = 1, PG_GAMMA = 2, PG_NU = 3, PG_RHO0 = 4, PG_KP = 5, PG_COUNT = 8 };
+
+// pgrad[s] = sum over the nblk cells of slot s, in a fixed order (one block per slot,
+// 256 threads).
+static __global__ void __launch_bounds__(256) pg_reduce_kernel(double* pgrad, unsigned nblk) {
+  __shared__ double sh[256];
+  const int s = blockIdx.x;
+  const double* cells = pgrad + PG_COUNT + (size_t)s * nblk;
+  double t = 0;
+  for (unsigned b = threadIdx.x; b < nblk; b += 256) t += cells[b];
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) pgrad[s] = sh[0];
+}
 
 struct AdjScalars {
   double ep, alpha, beta, gamma, zeta, kp, rho0, q02, dt, dtd2, rho_m, scale, nu, lam2nu;
@@ -153,7 +174,7 @@ __global__ void __launch_bounds__(256) adj_cn_kernel(Grid g, const double* qx, c
     // dC1/dalpha = dC2/dalpha = dt rho_m sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
     da = bq * s.dt * s.rho_m * sq * sq * (Qold[idx] - Qnew[idx]) / C2;
   }
-  block_accum(da, &pgrad[PG_ALPHA]);
+  block_accum(da, pgrad, PG_ALPHA);
 }
 
 // Transpose of dq = q . f-hat shifted (REF:2076-2078, subtracted from Nl-hat): f-hat_a
@@ -214,8 +235,8 @@ __global__ void __launch_bounds__(256) adj_nl_kernel(Grid g, AdjNlArgs a) {
     dkp = b * psi * (a.s.zeta * t2 / den - cp * A);
     drho0 = -b * psi * cp;
   }
-  block_accum(dkp, &a.pgrad[PG_KP]);
-  block_accum(drho0, &a.pgrad[PG_RHO0]);
+  block_accum(dkp, a.pgrad, PG_KP);
+  block_accum(drho0, a.pgrad, PG_RHO0);
 }
 
 // Transpose of the Stokes solve, part 1 (REF:1581-1974 and the divergence REF:2076):
@@ -284,7 +305,7 @@ __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs 
     a.bdoty[idx] = dy; a.bsy[idx] = sdy; a.bgy[idx] = fpy;
     a.bdotz[idx] = dz; a.bsz[idx] = sdz; a.bgz[idx] = fpz;
   }
-  block_accum(dnu, &a.pgrad[PG_NU]);
+  block_accum(dnu, a.pgrad, PG_NU);
 }
 
 // Transpose of the Stokes solve, part 2: gather at each input mode p the terms of
@@ -398,10 +419,10 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args a) {
     }
     a.bA[idx] += bA;
   }
-  block_accum(dbeta, &a.pgrad[PG_BETA]);
-  block_accum(dgamma, &a.pgrad[PG_GAMMA]);
-  block_accum(drho0, &a.pgrad[PG_RHO0]);
-  block_accum(dkp, &a.pgrad[PG_KP]);
+  block_accum(dbeta, a.pgrad, PG_BETA);
+  block_accum(dgamma, a.pgrad, PG_GAMMA);
+  block_accum(drho0, a.pgrad, PG_RHO0);
+  block_accum(dkp, a.pgrad, PG_KP);
 }
 
 // bQ += Lambda(q) Y for the spectral multipliers of the forward (REF:1302 for
@@ -422,7 +443,7 @@ __global__ void __launch_bounds__(256) adj_acc_spec_kernel(Grid g, const double*
     bQ[idx] += alpha * dl * y;
     da = y * dl * Q[idx];
   }
-  block_accum(da, &pgrad[PG_ALPHA]);
+  block_accum(da, pgrad, PG_ALPHA);
 }
 
 // out = a * x (+ b * y): small helper for the final dL/dpsi0 = scale C2^T (bQ + bQo).

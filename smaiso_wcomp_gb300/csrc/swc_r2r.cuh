@@ -19,7 +19,10 @@
 
 namespace swc {
 
-enum Kind { K_C2 = 0, K_C3 = 1, K_S2 = 2, K_S3 = 3, K_FILT = 4 };
+// K_FILT: DCT-II, spectral multiplier, DCT-III along the axis (one CTA).
+// K_DERIV: DCT-II, then w_i = mul(i) u_{i+1} (w_{n-1} = 0), then DST-III: the shifted
+// spectral derivative of REF:1166-1250 along one axis in one pass.
+enum Kind { K_C2 = 0, K_C3 = 1, K_S2 = 2, K_S3 = 3, K_FILT = 4, K_DERIV = 5 };
 
 template <typename T> struct R2RTables {
   const cx_t<T>* fft;   // W_M^t = exp(-2 pi i t/M), t < M
@@ -301,9 +304,9 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
   const int l = tid & (L - 1);
   const int tj = tid >> ps.log2L;
   const long long my_line = line0 + l;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
 
-  stage_tables<T, KIND>(ps, tb, sfft, spost, spre);
+  stage_tables<T, (KIND == K_DERIV ? K_FILT : KIND)>(ps, tb, sfft, spost, spre);
 
   // ---- load: global -> bufA reals ----
   {
@@ -356,9 +359,31 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
   bool swapped;  // output components are (im, re)-swapped (inverse FFT result)
   if constexpr (fwd_in) {
     run_stages<T>(ps, src, dst, l, tj, sfft);  // result in src
-    dct2_post<T, KIND, MulOp>(g, ps, my_line, src, reinterpret_cast<T*>(dst), l, tj, spost, mul);
+    dct2_post<T, (KIND == K_DERIV ? K_C2 : KIND), MulOp>(g, ps, my_line, src, reinterpret_cast<T*>(dst), l, tj,
+                                                          spost, mul);
     __syncthreads();
-    if constexpr (KIND == K_FILT) {
+    if constexpr (KIND == K_DERIV) {
+      // w_i = mul(i) u_{i+1}, stored reversed (DST-III input), then the DST-III
+      const T* u = reinterpret_cast<const T*>(dst);
+      T* w = reinterpret_cast<T*>(src);
+      for (int i = tj; i < n; i += ps.tpl) {
+        T v = (T)0;
+        if (i < n - 1) {
+          int ii, jj, kk;
+          long long idx;
+          line_coords(g, ps.axis, my_line, i, ii, jj, kk, idx);
+          v = mul(ii, jj, kk) * u[ridx(i + 1, l, P)];
+        }
+        w[ridx(n - 1 - i, l, P)] = v;
+      }
+      __syncthreads();
+      dct3_pre<T>(ps, reinterpret_cast<const T*>(src), dst, l, tj, spre);
+      __syncthreads();
+      { C* t = src; src = dst; dst = t; }
+      run_stages<T>(ps, src, dst, l, tj, sfft);
+      res_real = reinterpret_cast<T*>(src);
+      swapped = true;
+    } else if constexpr (KIND == K_FILT) {
       // inverse DCT-III of the filtered spectrum, in the same CTA
       dct3_pre<T>(ps, reinterpret_cast<const T*>(dst), src, l, tj, spre);
       __syncthreads();
@@ -383,7 +408,7 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
     if (swapped) {
       const int q = (p & 1) ? (n - 1 - (p >> 1)) : (p >> 1);
       T y = res_real[ridx(q, le, P) ^ 1];
-      if (KIND == K_S3 && (p & 1)) y = -y;
+      if ((KIND == K_S3 || KIND == K_DERIV) && (p & 1)) y = -y;
       return y;
     }
     return res_real[ridx(p, le, P)];

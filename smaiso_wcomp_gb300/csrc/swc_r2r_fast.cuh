@@ -294,7 +294,7 @@ __device__ __forceinline__ void fast_last_store(const Grid& g, int line, const c
   }
   auto put = [&](int q, T val) {
     const int pos = mk_pos<N>(q);
-    if (KIND == K_S3 && (pos & 1)) val = -val;
+    if ((KIND == K_S3 || KIND == K_DERIV) && (pos & 1)) val = -val;
     int i, j, k;
     long long idx;
     xy_coords<AX>(g, line, pos, i, j, k, idx);
@@ -321,8 +321,8 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
   using C = cx_t<T>;
   constexpr int M = Cf::M, L = Cf::L, P = Cf::P, NT = Cf::NT, TPL = Cf::TPL, ITERS = Cf::ITERS, CH = Cf::CH;
   constexpr int R1 = Cf::R1, R2 = Cf::R2;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT);
-  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
   constexpr bool xy = (AX != 2);  // x/y passes: global memory straight to/from registers
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
@@ -398,11 +398,31 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
 
   if constexpr (fwd_in) {
     fast_stage<C, M, R2, R1, TPL, P>(buf, sfft, l, tj);
-    if constexpr (xy && KIND != K_FILT) {
+    if constexpr (xy && KIND != K_FILT && KIND != K_DERIV) {
       fast_post_store<T, N, KIND, AX>(g, my_line, buf, spost, l, tj, st);
       return;
     }
-    fast_post<T, N, KIND, MulOp>(g, AX, line0 + l, buf, spost, l, tj, mul);
+    fast_post<T, N, (KIND == K_DERIV ? K_C2 : KIND), MulOp>(g, AX, line0 + l, buf, spost, l, tj, mul);
+    if constexpr (KIND == K_DERIV) {
+      // w_i = mul(i) u_{i+1} (w_{N-1} = 0), stored reversed as the DST-III input
+      constexpr int PER = N / TPL;
+      T w[PER];
+#pragma unroll
+      for (int b = 0; b < PER; ++b) {
+        const int i = tj + b * TPL;
+        w[b] = (T)0;
+        if (i < N - 1) {
+          int ii, jj, kk;
+          long long idx;
+          line_coords(g, AX, line0 + l, i, ii, jj, kk, idx);
+          w[b] = mul(ii, jj, kk) * rb[fridx<P>(i + 1, l)];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int b = 0; b < PER; ++b) rb[fridx<P>(N - 1 - (tj + b * TPL), l)] = w[b];
+      __syncthreads();
+    }
   }
   if constexpr (inv_out) {
     fast_pre<T, N>(buf, spre, l, tj);
@@ -426,7 +446,7 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
       if constexpr (inv_out) {
         const int q = (p & 1) ? (N - 1 - (p >> 1)) : (p >> 1);
         T y = rb[fridx<P>(q, le) ^ 1];
-        if (KIND == K_S3 && (p & 1)) y = -y;
+        if ((KIND == K_S3 || KIND == K_DERIV) && (p & 1)) y = -y;
         vals[c] = y;
       } else {
         vals[c] = rb[fridx<P>(p, le)];

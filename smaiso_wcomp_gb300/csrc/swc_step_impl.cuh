@@ -50,19 +50,15 @@ namespace swc {
 // Load / store / multiplier functors fused into the transform passes
 // ---------------------------------------------------------------------------------
 
-// Shifted spectral derivative onto the sine grid of `axis` (REF:1166-1221):
-// out = -fac * Vs[c] * spec[c + 1], 0 on the last mode of the axis.
-template <typename T, typename U> struct LdGrad {
-  const U* spec;
+// Multiplier of the derivative pass (shifted spectral derivative onto the sine grid
+// of `axis`, REF:1166-1221): -c Vs[c_axis], c = 1/(2 n_axis); the pass itself applies
+// the shift and the zero on the last mode.
+template <typename T> struct MulDeriv {
   const T* vs;
-  T fac;
+  T c;
   int axis;
-  int nlast;
-  long long shift;
-  __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
-    const int c = axis == 0 ? i : (axis == 1 ? j : k);
-    if (c >= nlast) return (T)0;
-    return -fac * vs[c] * (T)spec[idx + shift];
+  __device__ __forceinline__ T operator()(int i, int j, int k) const {
+    return -c * vs[axis == 0 ? i : (axis == 1 ? j : k)];
   }
 };
 
@@ -469,7 +465,8 @@ template <typename T> class StepEngine : public EngineBase {
   double* tape_ = nullptr;         // forward intermediates of one segment
   size_t tape_steps_ = 0;
   double* adj_ = nullptr;          // adjoint work arrays
-  double* pgrad_ = nullptr;        // parameter-gradient accumulators
+  double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
+  size_t pgrad_doubles() const { return 8 * (1 + (size_t)((g_.ng + 255) / 256)); }
   bool adj_valid_ = false;         // checkpoints describe the run since swc_set_state
   // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
   template <typename U, int KIND, int AX, class LD, class ST, class MUL = NoMul<U>>
@@ -501,7 +498,7 @@ template <typename T> class StepEngine : public EngineBase {
   // state (FP64)
   double *psiq_ = nullptr, *psiq_old_ = nullptr, *rho_ = nullptr, *frho_ = nullptr;
   // work (T)
-  T *nlq_ = nullptr, *psi_ = nullptr, *psi_new_ = nullptr, *psi_old_ = nullptr, *rhoq_ = nullptr;
+  T *nlq_ = nullptr, *psi_ = nullptr, *psi_new_ = nullptr, *psi_old_ = nullptr;
   T *gp_[3] = {}, *gr_[3] = {}, *amp_f_ = nullptr, *lpsi_ = nullptr, *lapR_ = nullptr, *mu_ = nullptr;
   T *fgrad_ = nullptr, *ener_ = nullptr, *S_[3] = {}, *f_[3] = {}, *vsol_[3] = {}, *virr_[3] = {};
   T *divv_ = nullptr, *dq_ = nullptr, *v_[3] = {}, *vsolr_[3] = {}, *energy_ = nullptr, *nlw_ = nullptr;
@@ -618,7 +615,7 @@ template <typename T> int StepEngine<T>::init() {
   double** dbufs[] = {&psiq_, &psiq_old_, &rho_, &frho_};
   for (double** b : dbufs)
     if ((rc = dalloc(nd, (void**)b))) return rc;
-  T** tbufs[] = {&nlq_, &psi_, &psi_new_, &psi_old_, &rhoq_, &gp_[0], &gp_[1], &gp_[2], &gr_[0], &gr_[1],
+  T** tbufs[] = {&nlq_, &psi_, &psi_new_, &psi_old_, &gp_[0], &gp_[1], &gp_[2], &gr_[0], &gr_[1],
                  &gr_[2], &amp_f_, &lpsi_, &lapR_, &mu_, &fgrad_, &ener_, &S_[0], &S_[1], &S_[2], &f_[0],
                  &f_[1], &f_[2], &vsol_[0], &vsol_[1], &vsol_[2], &virr_[0], &virr_[1], &virr_[2], &divv_,
                  &dq_, &v_[0], &v_[1], &v_[2], &vsolr_[0], &vsolr_[1], &vsolr_[2], &energy_, &nlw_};
@@ -662,35 +659,24 @@ int StepEngine<T>::passU(LD ld, ST st, MUL mul) {
 template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bool diag) {
   using LP = LdPlain<T, T>;
   using SP = StPlain<T, T>;
-  const long long sx = 1LL << (g_.ly + g_.lz), sy = g_.nz;
-  const int nlast[3] = {g_.nx - 1, g_.ny - 1, g_.nz - 1};
-  const long long shifts[3] = {sx, sy, 1};
   const unsigned pw_blocks = (unsigned)((g_.ng + 255) / 256);
 
-  // S1 (REF:1104-1106): rhoq = DCT(rho); the mixed engine transforms rho - (rho_0 + rho_s)/2
+  // S1 + S2 (REF:1104-1250): rhoq = DCT(rho) and the six shifted spectral gradients
+  // taken back to real space. With psiq = scale DCT-II^3 psi and the DCT-III/DCT-II pairs
+  // of the two other axes cancelling (DCT-III DCT-II = 2n per axis), each gradient is
+  // one pass along its own axis: d_a f = DST-III_a(-Vs_a shift_a(DCT-II_a f)) / (2 n_a),
+  // for f = psi (REF:1190-1219) and f = rho (REF:1191-1219, where -scale Vs rhoq gives
+  // the same 1/(2 n_a)). The mixed engine transforms rho - (rho_0 + rho_s)/2: the
+  // gradients never read mode 0, and FP32 then resolves the small variations.
   const double rho_off = std::is_same<T, double>::value ? 0.0 : 0.5 * (p_.rho_0 + rho_s_);
-  SWC_TRY((pass<K_C2, 2>(LdOffset<T>{rho_, rho_off}, SP{rhoq_})));
-  SWC_TRY((pass<K_C2, 1>(LP{rhoq_}, SP{rhoq_})));
-  SWC_TRY((pass<K_C2, 0>(LP{rhoq_}, SP{rhoq_})));
-  // S1 + S2 (REF:1166-1250): spectral gradients -> inverse mixed transforms
-  for (int ax = 0; ax < 3; ++ax) {
-    LdGrad<T, double> lpsi{psiq_, vs_[ax], (T)1, ax, nlast[ax], shifts[ax]};
-    LdGrad<T, T> lrho{rhoq_, vs_[ax], (T)scale_, ax, nlast[ax], shifts[ax]};
-    for (int which = 0; which < 2; ++which) {
-      T* out = which == 0 ? gp_[ax] : gr_[ax];
-      // z pass: sine along z only for the z component
-      if (ax == 2) {
-        if (which == 0) SWC_TRY((pass<K_S3, 2>(lpsi, SP{out})));
-        else SWC_TRY((pass<K_S3, 2>(lrho, SP{out})));
-      } else {
-        if (which == 0) SWC_TRY((pass<K_C3, 2>(lpsi, SP{out})));
-        else SWC_TRY((pass<K_C3, 2>(lrho, SP{out})));
-      }
-      if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
-      if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
-    }
+  {
+    const T cx = (T)(1.0 / (2.0 * g_.nx)), cy = (T)(1.0 / (2.0 * g_.ny)), cz = (T)(1.0 / (2.0 * g_.nz));
+    SWC_TRY((pass<K_DERIV, 2>(LP{psi_}, SP{gp_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
+    SWC_TRY((pass<K_DERIV, 1>(LP{psi_}, SP{gp_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
+    SWC_TRY((pass<K_DERIV, 0>(LP{psi_}, SP{gp_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
+    SWC_TRY((pass<K_DERIV, 2>(LdOffset<T>{rho_, rho_off}, SP{gr_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
+    SWC_TRY((pass<K_DERIV, 1>(LdOffset<T>{rho_, rho_off}, SP{gr_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
+    SWC_TRY((pass<K_DERIV, 0>(LdOffset<T>{rho_, rho_off}, SP{gr_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
   }
   // S3 (REF:1254-1289): amplitude, Gaussian filter
   SWC_TRY((pass<K_C2, 2>(LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
