@@ -50,7 +50,7 @@ def parse():
                     help="also run both engines this many steps from the initial state and report psi/rho error")
     ap.add_argument("--grad-steps", type=int, default=40,
                     help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
-    ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
+    ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
                     help="profiling mode: run only this engine's warm-up + timed steps and print its timing")
     return ap.parse_args()
 
@@ -170,39 +170,43 @@ def pinned(shape):
     return np.empty(shape, dtype=np.float64)
 
 
-def pass_roofline(precision, reps=10):
-    """Live CUDA-event timing of the dominant kernel -- one r2r axis pass over the
-    256^3 field -- on the stream it is launched on, with L2 flushed (a 256 MiB write)
-    before every timed launch. Returns the mean pass time over the three axes (ms),
-    the per-axis times and the algorithmic bytes of one pass (one read + one write)."""
+def pass_roofline(precision, reps=5, fields=8):
+    """Live CUDA-event timing of the dominant kernel -- one r2r axis pass over a 256^3
+    field -- on the stream it is launched on, in the steady state of a step: `fields`
+    distinct fields (8 x 67 MB FP32 = 537 MB, four times the 129 MB L2) each take a
+    DCT-II axis pass, axis-major (all z passes, then all y, then all x), so every pass
+    reads its field from DRAM and pays for the write-back of an earlier pass's output,
+    as the passes of a step do. Returns the mean time of one pass (ms), the per-axis
+    means and the algorithmic bytes of one pass (one read + one write of the field)."""
     import torch
     from smaiso_wcomp_gb300 import abi
     from smaiso_wcomp_gb300.engine import R2RPlan
     dt = torch.float32 if precision == abi.SWC_PREC_MIXED else torch.float64
-    x = torch.randn((N, N, N), dtype=dt, device="cuda") * 1e-3
-    flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device="cuda")
-    plans = [R2RPlan((N, N, N), (0, 0, 0), precision), R2RPlan((N, N, N), (1, 1, 1), precision)]
+    if dt == torch.float64:
+        fields = 4   # 4 x 134 MB, still four times L2
+    xs = [torch.randn((N, N, N), dtype=dt, device="cuda") * 1e-3 for _ in range(fields)]
+    plan = R2RPlan((N, N, N), (0, 0, 0), precision)
     s = torch.cuda.Stream()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    per_axis = []
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    per_axis = [[], [], []]
     with torch.cuda.stream(s):
-        for axis in (2, 1, 0):
-            times = []
-            for r in range(reps + 2):
-                flush.zero_()
-                ev0.record(s)
-                plans[r % 2].execute_axis(axis, x.data_ptr(), s.cuda_stream)   # DCT-II, DCT-III alternate
-                ev1.record(s)
-                ev1.synchronize()
-                x.mul_(1.0 / (2 * N))      # keep the field bounded (outside the timed region)
-                if r >= 2:
-                    times.append(ev0.elapsed_time(ev1))
-            per_axis.append(float(np.median(times)))
+        for r in range(reps + 2):
+            evs[0].record(s)
+            for q, axis in enumerate((2, 1, 0)):
+                for x in xs:
+                    plan.execute_axis(axis, x.data_ptr(), s.cuda_stream)
+                evs[q + 1].record(s)
+            evs[3].synchronize()
+            for x in xs:
+                x.mul_(1.0 / (8 * N ** 3))   # keep the fields bounded (outside the timed region)
+            if r >= 2:
+                for q in range(3):
+                    per_axis[q].append(evs[q].elapsed_time(evs[q + 1]) / fields)
+    per_axis = [float(np.median(t)) for t in per_axis]
     elem = 4 if precision == abi.SWC_PREC_MIXED else 8
     alg_bytes = 2 * N ** 3 * elem
-    del x, flush
-    for pl in plans:
-        pl.close()
+    del xs
+    plan.close()
     return float(np.mean(per_axis)), per_axis, alg_bytes
 
 
@@ -306,6 +310,11 @@ def main():
         pg = dist
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
+    if args.only == "pass":
+        ms, per_axis, alg = pass_roofline(abi.SWC_PREC_MIXED, reps=args.steps)
+        print(json.dumps({"only": "pass", "ms_per_pass": ms, "pass_ms_zyx": per_axis,
+                          "gbs": alg / (ms * 1e-3) / 1e9}), flush=True)
+        return
     if args.only:
         prec = abi.SWC_PREC_MIXED if args.only == "mixed" else abi.SWC_PREC_FP64
         e, ms, launches = time_engine(make_params(prec, device=local), psi, rho, args.warmup, args.steps)
@@ -363,7 +372,7 @@ def main():
     fp64_flops = (2.5 * np.log2(N) + 8.0) * N ** 3
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": PASS_TRAFFIC.get("fp32"),
-                "kernel": "r2r_pass_kernel<float> (one axis pass, 256^3, mean of z/y/x)",
+                "kernel": "r2r_fast_kernel<float, 256> (one DCT-II axis pass, 256^3, steady state of 8 fields, mean of z/y/x)",
                 "pass_ms_zyx": axes_ms, "alg_bytes_per_launch": alg,
                 "peak_source": f"{peak_kind} hbm_gbs"}
     line = {

@@ -268,8 +268,9 @@ int swc_r2r_plan_create(int nx, int ny, int nz, int kx, int ky, int kz, int prec
                         swc_r2r_plan** out);
 int swc_r2r_plan_destroy(swc_r2r_plan* plan);
 
-/* In-place execution on device memory (double* or float* per the plan), enqueued
- * on `stream` (a cudaStream_t; NULL = legacy default stream). Allocates nothing. */
+/* In-place execution on device memory (double* or float* per the plan, 16-byte
+ * aligned, as cudaMalloc returns; SWC_ERR_BAD_PARAM otherwise), enqueued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream). Allocates nothing. */
 int swc_r2r_execute(swc_r2r_plan* plan, void* dev_inout, void* stream);
 
 /* One axis pass of the plan (axis 0 = x, 1 = y, 2 = z), in place on device memory;

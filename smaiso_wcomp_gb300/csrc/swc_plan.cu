@@ -1,6 +1,7 @@
 // swc_plan.cu -- r2r transform plans: the drop-in for fftw_mpi_plan_r2r_3d +
 // fftw_execute (smaiso-wcomp.cpp:499-545) on one GPU. A 3D transform is three
 // in-place axis passes (z, y, x); the plan owns only its twiddle tables.
+#include <cstdint>
 #include <cuda_runtime.h>
 
 #include <new>
@@ -20,6 +21,7 @@ struct swc_r2r_plan {
   std::vector<void*> allocs;
   R2RTables<double> td[3];
   R2RTables<float> tf[3];
+  int* status = nullptr;  // set by a pass whose bounded wait ran out; read by swc_r2r_execute_host
 };
 
 namespace {
@@ -114,7 +116,20 @@ int swc_r2r_plan_create(int nx, int ny, int nz, int kx, int ky, int kz, int prec
   p->g.ng = (long long)nx * ny * nz;
   p->precision = precision;
   p->device = dev;
+  {
+    void* st = nullptr;  // status flag of the passes' bounded waits
+    if (cudaMalloc(&st, sizeof(int)) != cudaSuccess || cudaMemset(st, 0, sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cudaMalloc for the plan status failed");
+      swc_r2r_plan_destroy(p);
+      return SWC_ERR_OOM;
+    }
+    p->allocs.push_back(st);
+    p->status = (int*)st;
+  }
   for (int a = 0; a < 3; ++a) {
+    p->td[a].status = p->status;
+    p->tf[a].status = p->status;
     p->kind[a] = kinds[a];
     const int rc = precision == SWC_PREC_FP64 ? upload_tables<double>(p, a, dims[a], &p->td[a])
                                               : upload_tables<float>(p, a, dims[a], &p->tf[a]);
@@ -139,12 +154,20 @@ int swc_r2r_plan_destroy(swc_r2r_plan* p) {
 
 int swc_r2r_execute(swc_r2r_plan* p, void* dev_inout, void* stream) {
   if (!p || !dev_inout) { set_error("NULL plan or buffer"); return SWC_ERR_BAD_PARAM; }
+  if (reinterpret_cast<uintptr_t>(dev_inout) % 16 != 0) {  // the passes move 16-byte vectors
+    set_error("device buffer must be 16-byte aligned");
+    return SWC_ERR_BAD_PARAM;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   return p->precision == SWC_PREC_FP64 ? execute<double>(p, dev_inout, s) : execute<float>(p, dev_inout, s);
 }
 
 int swc_r2r_execute_axis(swc_r2r_plan* p, int axis, void* dev_inout, void* stream) {
   if (!p || !dev_inout || axis < 0 || axis > 2) { set_error("bad plan, buffer or axis"); return SWC_ERR_BAD_PARAM; }
+  if (reinterpret_cast<uintptr_t>(dev_inout) % 16 != 0) {
+    set_error("device buffer must be 16-byte aligned");
+    return SWC_ERR_BAD_PARAM;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   const cudaError_t e = p->precision == SWC_PREC_FP64 ? run_axis<double>(p, axis, (double*)dev_inout, s)
                                                       : run_axis<float>(p, axis, (float*)dev_inout, s);
@@ -184,6 +207,12 @@ int swc_r2r_execute_host(swc_r2r_plan* p, const double* in, double* out) {
   }
   if (rc == SWC_ERR_CUDA) set_error("r2r host execution: CUDA copy failed");
   cudaFree(dev);
+  int st = 0;
+  if (!rc && cudaMemcpy(&st, p->status, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && st) {
+    cudaMemset(p->status, 0, sizeof(int));
+    set_error("r2r host execution: a tile copy did not complete in time");
+    rc = SWC_ERR_CUDA;
+  }
   return rc;
 }
 

@@ -28,6 +28,7 @@ template <typename T> struct R2RTables {
   const cx_t<T>* fft;   // W_M^t = exp(-2 pi i t/M), t < M
   const cx_t<T>* post;  // DCT-II post-twiddles: post[2k] = c_k, post[2k+1] = d_k, k = 0..M
   const cx_t<T>* pre;   // DCT-III pre-twiddles : pre[2k] = a_k, pre[2k+1] = b_k, k < M
+  int* status;          // device flag set to 1 when a pass's bounded wait runs out (or null)
 };
 
 struct PassShape {
@@ -136,14 +137,77 @@ __device__ __forceinline__ void line_coords(const Grid& g, int axis, long long i
 // real element r of line l in a complex-row buffer: component (r & 1) of slot (r >> 1)
 __device__ __forceinline__ int ridx(int r, int l, int P) { return (((r >> 1) * P + l) << 1) + (r & 1); }
 
-// Plain load / store functors (with precision conversion).
+// Vector loads / stores for the FP32 two-line pass: 2 or 4 consecutive elements from
+// an even / a multiple-of-4 index (float2/float4, or double2 pairs converted to FP32).
+template <typename U> __device__ __forceinline__ float2 ld2v(const U* p, long long idx) {
+  if constexpr (sizeof(U) == 4) {
+    return *reinterpret_cast<const float2*>(p + idx);
+  } else {
+    const double2 d = *reinterpret_cast<const double2*>(p + idx);
+    return make_float2((float)d.x, (float)d.y);
+  }
+}
+template <typename U> __device__ __forceinline__ float4 ld4v(const U* p, long long idx) {
+  if constexpr (sizeof(U) == 4) {
+    return *reinterpret_cast<const float4*>(p + idx);
+  } else {
+    const double2 d0 = *reinterpret_cast<const double2*>(p + idx);
+    const double2 d1 = *reinterpret_cast<const double2*>(p + idx + 2);
+    return make_float4((float)d0.x, (float)d0.y, (float)d1.x, (float)d1.y);
+  }
+}
+// The same loads through the read-only data path (ld.global.nc): for functors that also
+// store, these loads may be scheduled ahead of the stores of earlier elements. Valid
+// when every element is read before it is written and by the thread that writes it.
+template <typename U> __device__ __forceinline__ float2 ld2g(const U* p, long long idx) {
+  if constexpr (sizeof(U) == 4) {
+    return __ldg(reinterpret_cast<const float2*>(p + idx));
+  } else {
+    const double2 d = __ldg(reinterpret_cast<const double2*>(p + idx));
+    return make_float2((float)d.x, (float)d.y);
+  }
+}
+template <typename U> __device__ __forceinline__ float4 ld4g(const U* p, long long idx) {
+  if constexpr (sizeof(U) == 4) {
+    return __ldg(reinterpret_cast<const float4*>(p + idx));
+  } else {
+    const double2 d0 = __ldg(reinterpret_cast<const double2*>(p + idx));
+    const double2 d1 = __ldg(reinterpret_cast<const double2*>(p + idx + 2));
+    return make_float4((float)d0.x, (float)d0.y, (float)d1.x, (float)d1.y);
+  }
+}
+__device__ __forceinline__ double2 ld2dg(const double* p, long long idx) {
+  return __ldg(reinterpret_cast<const double2*>(p + idx));
+}
+template <typename U> __device__ __forceinline__ void st2v(U* p, long long idx, float2 v) {
+  if constexpr (sizeof(U) == 4) {
+    *reinterpret_cast<float2*>(p + idx) = v;
+  } else {
+    *reinterpret_cast<double2*>(p + idx) = make_double2(v.x, v.y);
+  }
+}
+template <typename U> __device__ __forceinline__ void st4v(U* p, long long idx, float4 v) {
+  if constexpr (sizeof(U) == 4) {
+    *reinterpret_cast<float4*>(p + idx) = v;
+  } else {
+    *reinterpret_cast<double2*>(p + idx) = make_double2(v.x, v.y);
+    *reinterpret_cast<double2*>(p + idx + 2) = make_double2(v.z, v.w);
+  }
+}
+
+// Plain load / store functors (with precision conversion); pair / quad are the vector
+// forms used by the FP32 two-line pass.
 template <typename T, typename U> struct LdPlain {
   const U* p;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)p[idx]; }
+  __device__ __forceinline__ float2 pair(int, int, int, long long idx) const { return ld2v(p, idx); }
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const { return ld4v(p, idx); }
 };
 template <typename T, typename U> struct StPlain {
   U* p;
   __device__ __forceinline__ void operator()(int, int, int, long long idx, T v) const { p[idx] = (U)v; }
+  __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const { st2v(p, idx, v); }
+  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 v) const { st4v(p, idx, v); }
 };
 
 // Identity multiplier for non-filter passes.

@@ -1,0 +1,657 @@
+// swc_r2r_pair.cuh -- the FP32 r2r axis pass with two lines per thread.
+//
+// Same transform, kinds, Makhoul mapping and Stockham plan as r2r_fast_kernel
+// (swc_r2r_fast.cuh), but every thread carries the same butterfly of two adjacent
+// lines A and B in "planar pair" registers: PC = {re = (re_A, re_B), im = (im_A, im_B)}.
+// All arithmetic is then sm_100+ packed FP32 (FADD2 / FMUL2 / FFMA2 through
+// __fadd2_rn / __fmul2_rn / __ffma2_rn), one instruction for both lines, with the
+// twiddles broadcast to both halves from float4 tables {c, c, s, s} in shared memory.
+// Global traffic is vectorised too: x/y passes load and store (A, B) as one float2
+// (adjacent lines are adjacent addresses), z passes move four consecutive elements of
+// a line as one float4 and scatter them into Makhoul order in registers.
+#pragma once
+
+#include <type_traits>
+#include <utility>
+
+#include "swc_r2r_fast.cuh"
+
+#ifndef SWC_PAIR_NT
+#define SWC_PAIR_NT 128
+#endif
+
+namespace swc {
+
+// ---- packed FP32 helpers -------------------------------------------------------------
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b as a + (-1) b: exact product, one rounding, same as a subtraction
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+struct PC {
+  float2 re, im;
+};
+__device__ __forceinline__ PC pmake(float2 re, float2 im) { PC r; r.re = re; r.im = im; return r; }
+__device__ __forceinline__ PC padd(PC a, PC b) { return pmake(add2(a.re, b.re), add2(a.im, b.im)); }
+__device__ __forceinline__ PC psub(PC a, PC b) { return pmake(sub2(a.re, b.re), sub2(a.im, b.im)); }
+__device__ __forceinline__ PC pswap(PC a) { return pmake(a.im, a.re); }
+// v * w for a twiddle w = (x, y) held as {x, x, y, y}
+__device__ __forceinline__ PC pmul(PC v, float4 w) {
+  const float2 wx = make_float2(w.x, w.y), wy = make_float2(w.z, w.w);
+  return pmake(fma2(v.re, wx, mul2(v.im, neg2(wy))), fma2(v.re, wy, mul2(v.im, wx)));
+}
+// w * conj(v)
+__device__ __forceinline__ PC pmulc(float4 w, PC v) {
+  const float2 wx = make_float2(w.x, w.y), wy = make_float2(w.z, w.w);
+  return pmake(fma2(v.re, wx, mul2(v.im, wy)), fma2(v.re, wy, mul2(v.im, neg2(wx))));
+}
+// a * x + b * conj(y)   (the Makhoul pre/post combination)
+__device__ __forceinline__ PC pcomb(float4 a, PC x, float4 b, PC y) {
+  const float2 ax = make_float2(a.x, a.y), ay = make_float2(a.z, a.w);
+  const float2 bx = make_float2(b.x, b.y), by = make_float2(b.z, b.w);
+  const float2 re = fma2(x.re, ax, fma2(x.im, neg2(ay), fma2(y.re, bx, mul2(y.im, by))));
+  const float2 im = fma2(x.im, ax, fma2(x.re, ay, fma2(y.re, by, mul2(y.im, neg2(bx)))));
+  return pmake(re, im);
+}
+// the same with the table entries a = (x, y), b = (x, y) broadcast to both lines
+__device__ __forceinline__ PC pcomb(float2 a, PC x, float2 b, PC y) {
+  return pcomb(make_float4(a.x, a.x, a.y, a.y), x, make_float4(b.x, b.x, b.y, b.y), y);
+}
+
+// ---- register DFT on planar pairs (forward, exp(-2 pi i/R)) ---------------------------
+
+template <int R> struct PDft {
+  // butterfly K of the radix-2 combine: v[K] = e + W^K o, v[K + R/2] = e - W^K o
+  template <int K> __device__ __forceinline__ static void combine(PC* v, const PC* e, const PC* o) {
+    if constexpr (K < R / 2) {
+      constexpr int k16 = K * (16 / R);
+      const PC a = e[K], b = o[K];
+      if constexpr (k16 == 0) {
+        v[K] = padd(a, b);
+        v[K + R / 2] = psub(a, b);
+      } else if constexpr (k16 == 4) {  // W = -i: t = (b.im, -b.re)
+        v[K] = pmake(add2(a.re, b.im), sub2(a.im, b.re));
+        v[K + R / 2] = pmake(sub2(a.re, b.im), add2(a.im, b.re));
+      } else if constexpr (k16 == 2) {  // W = (1 - i)/sqrt2: t = r (b.re + b.im, b.im - b.re)
+        const float2 s1 = add2(b.re, b.im), s2 = sub2(b.im, b.re);
+        const float2 r = f2((float)SWC_R2H), nr = f2(-(float)SWC_R2H);
+        v[K] = pmake(fma2(s1, r, a.re), fma2(s2, r, a.im));
+        v[K + R / 2] = pmake(fma2(s1, nr, a.re), fma2(s2, nr, a.im));
+      } else if constexpr (k16 == 6) {  // W = (-1 - i)/sqrt2: t = r (b.im - b.re, -(b.re + b.im))
+        const float2 s1 = add2(b.re, b.im), s2 = sub2(b.im, b.re);
+        const float2 r = f2((float)SWC_R2H), nr = f2(-(float)SWC_R2H);
+        v[K] = pmake(fma2(s2, r, a.re), fma2(s1, nr, a.im));
+        v[K + R / 2] = pmake(fma2(s2, nr, a.re), fma2(s1, r, a.im));
+      } else {  // W = c - i s: t = (b.re c + b.im s, b.im c - b.re s)
+        constexpr double cs[8] = {1.0, SWC_C16_1, SWC_R2H, SWC_S16_1, 0.0, -SWC_S16_1, -SWC_R2H, -SWC_C16_1};
+        constexpr double sn[8] = {0.0, SWC_S16_1, SWC_R2H, SWC_C16_1, 1.0, SWC_C16_1, SWC_R2H, SWC_S16_1};
+        const float2 c = f2((float)cs[k16]), s = f2((float)sn[k16]), ns = f2(-(float)sn[k16]);
+        const float2 tr = fma2(b.re, c, mul2(b.im, s));
+        const float2 ti = fma2(b.im, c, mul2(b.re, ns));
+        v[K] = pmake(add2(a.re, tr), add2(a.im, ti));
+        v[K + R / 2] = pmake(sub2(a.re, tr), sub2(a.im, ti));
+      }
+      combine<K + 1>(v, e, o);
+    }
+  }
+  __device__ __forceinline__ static void run(PC* v) {
+    PC e[R / 2], o[R / 2];
+#pragma unroll
+    for (int i = 0; i < R / 2; ++i) { e[i] = v[2 * i]; o[i] = v[2 * i + 1]; }
+    PDft<R / 2>::run(e);
+    PDft<R / 2>::run(o);
+    combine<0>(v, e, o);
+  }
+};
+template <> struct PDft<1> {
+  __device__ __forceinline__ static void run(PC*) {}
+};
+
+// ---- configuration ---------------------------------------------------------------------
+
+template <int N> struct PairCfg {
+  using F = FastCfg<float, N>;
+  static constexpr int M = N / 2;
+  static constexpr int R1 = F::R1, R2 = F::R2;
+  static constexpr int TPL = M / R1;          // threads per line pair
+  static constexpr int NT = SWC_PAIR_NT;      // threads per CTA
+  static constexpr int LP = NT / TPL;         // line pairs per CTA
+  static constexpr int PP = LP + 1;           // PC row pitch (staggers banks for the z phases)
+  static constexpr int NQ = N / 4;            // float4 per line
+  static constexpr int LOG2LP = (LP == 4) ? 2 : (LP == 8) ? 3 : (LP == 16) ? 4 : (LP == 32) ? 5 : 6;
+  static constexpr int LOG2NQ = (NQ == 16) ? 4 : (NQ == 32) ? 5 : (NQ == 64) ? 6 : 7;
+  static_assert((1 << LOG2LP) == LP && (1 << LOG2NQ) == NQ, "powers of two");
+  static_assert(NT % TPL == 0 && LP >= 4, "line pairs per CTA");
+  // PC buffer + stage twiddles (M, float4 {c, c, s, s}) + post (2(M+1)) and pre (2M)
+  // Makhoul twiddles (float2, broadcast on use)
+  static constexpr size_t table_bytes() { return (size_t)M * 16 + (size_t)(2 * (M + 1) + 2 * M) * 8; }
+  static constexpr size_t smem_bytes() { return (size_t)M * PP * 16 + table_bytes(); }
+};
+
+// Line B of a pair is line A + 1: coordinate k + 1 for x/y passes (needs nz >= 2),
+// j + 1 for z passes (needs ny >= 2). Indices are 32-bit.
+template <int N> inline bool pair_pass_supported(const Grid& g, int axis) {
+  const long long nlines = g.ng / N;
+  if (nlines < 2 * PairCfg<N>::LP || g.ng >= (1LL << 31)) return false;
+  return axis == 2 ? g.ny >= 2 : g.nz >= 2;
+}
+
+// ---- functor adapters: both lines of a pair, or four consecutive z elements --------------
+// A functor may provide pair(i, j, k, idx[, v]) (x/y passes: elements idx, idx + 1 at
+// k, k + 1) and quad(i, j, k, idx[, v]) (z passes: idx .. idx + 3 at k .. k + 3) to move
+// them as vectors; otherwise the scalar operator() is called per element.
+
+template <class F, class = void> struct HasLdPair : std::false_type {};
+template <class F>
+struct HasLdPair<F, std::void_t<decltype(std::declval<const F&>().pair(0, 0, 0, 0LL))>> : std::true_type {};
+template <class F, class = void> struct HasLdQuad : std::false_type {};
+template <class F>
+struct HasLdQuad<F, std::void_t<decltype(std::declval<const F&>().quad(0, 0, 0, 0LL))>> : std::true_type {};
+template <class F, class = void> struct HasStPair : std::false_type {};
+template <class F>
+struct HasStPair<F, std::void_t<decltype(std::declval<const F&>().pair(0, 0, 0, 0LL, float2()))>> : std::true_type {};
+template <class F, class = void> struct HasStQuad : std::false_type {};
+template <class F>
+struct HasStQuad<F, std::void_t<decltype(std::declval<const F&>().quad(0, 0, 0, 0LL, float4()))>> : std::true_type {};
+
+// element (i, j, k, idx) of line A and its partner on line B
+template <int AX, class LD>
+__device__ __forceinline__ float2 ld_ab(const Grid& g, const LD& ld, int i, int j, int k, long long idx) {
+  if constexpr (AX != 2) {
+    if constexpr (HasLdPair<LD>::value) return ld.pair(i, j, k, idx);
+    else return make_float2(ld(i, j, k, idx), ld(i, j, k + 1, idx + 1));
+  } else {
+    return make_float2(ld(i, j, k, idx), ld(i, j + 1, k, idx + g.nz));
+  }
+}
+template <int AX, class ST>
+__device__ __forceinline__ void st_ab(const Grid& g, const ST& st, int i, int j, int k, long long idx, float2 v) {
+  if constexpr (AX != 2) {
+    if constexpr (HasStPair<ST>::value) {
+      st.pair(i, j, k, idx, v);
+    } else {
+      st(i, j, k, idx, v.x);
+      st(i, j, k + 1, idx + 1, v.y);
+    }
+  } else {
+    st(i, j, k, idx, v.x);
+    st(i, j + 1, k, idx + g.nz, v.y);
+  }
+}
+template <int AX, class MUL> __device__ __forceinline__ float2 mul_ab(const MUL& mul, int i, int j, int k) {
+  if constexpr (AX != 2) return make_float2(mul(i, j, k), mul(i, j, k + 1));
+  else return make_float2(mul(i, j, k), mul(i, j + 1, k));
+}
+// elements k .. k+3 of one z line
+template <class LD> __device__ __forceinline__ float4 ld_q(const LD& ld, int i, int j, int k, long long idx) {
+  if constexpr (HasLdQuad<LD>::value) return ld.quad(i, j, k, idx);
+  else return make_float4(ld(i, j, k, idx), ld(i, j, k + 1, idx + 1), ld(i, j, k + 2, idx + 2), ld(i, j, k + 3, idx + 3));
+}
+template <class ST>
+__device__ __forceinline__ void st_q(const ST& st, int i, int j, int k, long long idx, float4 v) {
+  if constexpr (HasStQuad<ST>::value) {
+    st.quad(i, j, k, idx, v);
+  } else {
+    st(i, j, k, idx, v.x);
+    st(i, j, k + 1, idx + 1, v.y);
+    st(i, j, k + 2, idx + 2, v.z);
+    st(i, j, k + 3, idx + 3, v.w);
+  }
+}
+
+// real element r of line pair lp in the PC buffer viewed as float2 (A, B) pairs
+template <int PP> __device__ __forceinline__ int rpi(int r, int lp) { return (((r >> 1) * PP + lp) << 1) + (r & 1); }
+
+// ---- stages ------------------------------------------------------------------------------
+
+// Radix-R Stockham stage from and to the PC buffer (read -> barrier -> write -> barrier).
+template <int M, int R, int NS, int TPL, int PP>
+__device__ __forceinline__ void pair_stage(PC* buf, const float4* tw, int lp, int tj) {
+  constexpr int NB = M / R, PER = NB / TPL, STRIDE = M / R;
+  PC v[PER][R];
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int jb = tj + b * TPL;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[b][r] = buf[(jb + r * STRIDE) * PP + lp];
+    if constexpr (NS > 1) {
+      const int jj = jb & (NS - 1);
+      constexpr int TSTEP = M / (NS * R);
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[b][r] = pmul(v[b][r], tw[r * jj * TSTEP]);
+    }
+    PDft<R>::run(v[b]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int jb = tj + b * TPL;
+    const int jj = jb & (NS - 1);
+    const int base = (jb - jj) * R + jj;
+#pragma unroll
+    for (int r = 0; r < R; ++r) buf[(base + r * NS) * PP + lp] = v[b][r];
+  }
+  __syncthreads();
+}
+
+// DCT-II post-processing on (k, M-k) pairs into the real layout, natural order
+// (reversed for DST-II), times the filter multiplier for K_FILT.
+template <int N, int KIND, int AX, class MUL>
+__device__ __forceinline__ void pair_post(const Grid& g, int lineA, PC* buf, const float2* post, int lp, int tj,
+                                          const MUL& mul) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, NP = (M / 2) / TPL;
+  float2 y[NP][4];
+  float2 ymid[2] = {f2(0.f), f2(0.f)};
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const PC zk = buf[k * PP + lp];
+    const PC zm = buf[((M - k) & (M - 1)) * PP + lp];
+    const PC u0 = pcomb(post[2 * k], zk, post[2 * k + 1], zm);
+    const int km = M - k;
+    const PC u1 = pcomb(post[2 * km], zm, post[2 * km + 1], zk);
+    y[b][0] = u0.re;        // Y_k
+    y[b][1] = neg2(u0.im);  // Y_{N-k}
+    y[b][2] = u1.re;        // Y_{M-k}
+    y[b][3] = neg2(u1.im);  // Y_{M+k}
+  }
+  if (tj == 0) {
+    const PC z = buf[(M / 2) * PP + lp];
+    const PC u = pcomb(post[M], z, post[M + 1], z);
+    ymid[0] = u.re;
+    ymid[1] = neg2(u.im);
+  }
+  __syncthreads();
+  float2* rb2 = reinterpret_cast<float2*>(buf);
+  auto put = [&](int pos, float2 v) {
+    if constexpr (KIND == K_FILT) {
+      int i, j, kk;
+      long long idx;
+      line_coords(g, AX, lineA, pos, i, j, kk, idx);
+      v = mul2(v, mul_ab<AX>(mul, i, j, kk));
+    }
+    const int o = (KIND == K_S2) ? (N - 1 - pos) : pos;
+    rb2[rpi<PP>(o, lp)] = v;
+  };
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    put(k, y[b][0]);
+    put(M - k, y[b][2]);
+    if (k > 0) {
+      put(N - k, y[b][1]);
+      put(M + k, y[b][3]);
+    }
+  }
+  if (tj == 0) {
+    put(M / 2, ymid[0]);
+    put(M + M / 2, ymid[1]);
+  }
+  __syncthreads();
+}
+
+// DCT-III pre-processing of one (k, M-k) pair: reals X_k, X_{N-k}, X_{M-k}, X_{M+k}
+// -> Z_k, Z_{M-k} (U_k = X_k - i X_{N-k}, Z_k = a_k U_k + b_k conj(U_{M-k})).
+__device__ __forceinline__ void pair_pre_one(const float2* pre, int M, int k, float2 xk, float2 xnk, float2 xmk,
+                                             float2 xmpk, PC& z0, PC& z1) {
+  const PC U = pmake(xk, neg2(xnk)), Um = pmake(xmk, neg2(xmpk));
+  z0 = pcomb(pre[2 * k], U, pre[2 * k + 1], Um);
+  const int km = (M - k) & (M - 1);
+  z1 = pcomb(pre[2 * km], Um, pre[2 * km + 1], U);
+}
+
+// DCT-III pre-processing from the real layout (natural order) to (im, re)-swapped Z.
+template <int N> __device__ __forceinline__ void pair_pre(PC* buf, const float2* pre, int lp, int tj) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, NP = (M / 2) / TPL;
+  const float2* rb2 = reinterpret_cast<const float2*>(buf);
+  PC z[NP][2];
+  PC zmid = pmake(f2(0.f), f2(0.f));
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const float2 xnk = (k == 0) ? f2(0.f) : rb2[rpi<PP>(N - k, lp)];
+    pair_pre_one(pre, M, k, rb2[rpi<PP>(k, lp)], xnk, rb2[rpi<PP>(M - k, lp)], rb2[rpi<PP>(M + k, lp)], z[b][0],
+                 z[b][1]);
+  }
+  if (tj == 0) {
+    const int k = M / 2;
+    const PC U = pmake(rb2[rpi<PP>(k, lp)], neg2(rb2[rpi<PP>(N - k, lp)]));
+    zmid = pcomb(pre[2 * k], U, pre[2 * k + 1], U);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    buf[k * PP + lp] = pswap(z[b][0]);
+    if (k > 0) buf[(M - k) * PP + lp] = pswap(z[b][1]);
+  }
+  if (tj == 0) buf[(M / 2) * PP + lp] = pswap(zmid);
+  __syncthreads();
+}
+
+// x/y forward kinds: post-processing with the outputs of both lines stored straight
+// to global memory.
+template <int N, int KIND, int AX, class ST>
+__device__ __forceinline__ void pair_post_store(const Grid& g, int lineA, const PC* buf, const float2* post, int lp,
+                                                int tj, const ST& st) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, NP = (M / 2) / TPL;
+  auto put = [&](int pos, float2 v) {
+    const int o = (KIND == K_S2) ? (N - 1 - pos) : pos;
+    int i, j, k;
+    long long idx;
+    xy_coords<AX>(g, lineA, o, i, j, k, idx);
+    st_ab<AX>(g, st, i, j, k, idx, v);
+  };
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const PC zk = buf[k * PP + lp];
+    const PC zm = buf[((M - k) & (M - 1)) * PP + lp];
+    const PC u0 = pcomb(post[2 * k], zk, post[2 * k + 1], zm);
+    const int km = M - k;
+    const PC u1 = pcomb(post[2 * km], zm, post[2 * km + 1], zk);
+    put(k, u0.re);
+    put(M - k, u1.re);
+    if (k > 0) {
+      put(N - k, neg2(u0.im));
+      put(M + k, neg2(u1.im));
+    }
+  }
+  if (tj == 0) {
+    const PC z = buf[(M / 2) * PP + lp];
+    const PC u = pcomb(post[M], z, post[M + 1], z);
+    put(M / 2, u.re);
+    put(M + M / 2, neg2(u.im));
+  }
+}
+
+// x/y inverse kinds: the last radix-R2 stage with both lines' outputs stored straight
+// to global memory (slot m holds the swapped z_m: v_2m = .im, v_2m+1 = .re, v_q at
+// position mk_pos(q), negated at odd positions for DST-III).
+template <int N, int KIND, int AX, class ST>
+__device__ __forceinline__ void pair_last_store(const Grid& g, int lineA, const PC* buf, const float4* tw, int lp,
+                                                int tj, const ST& st) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, R = Cf::R2, NS = Cf::R1;
+  constexpr int NB = M / R, PER = NB / TPL, STRIDE = M / R, TSTEP = M / (NS * R);
+  PC v[PER][R];
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int jb = tj + b * TPL;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[b][r] = buf[(jb + r * STRIDE) * PP + lp];
+    const int jj = jb & (NS - 1);
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[b][r] = pmul(v[b][r], tw[r * jj * TSTEP]);
+    PDft<R>::run(v[b]);
+  }
+  auto put = [&](int q, float2 val) {
+    const int pos = mk_pos<N>(q);
+    if ((KIND == K_S3 || KIND == K_DERIV) && (pos & 1)) val = neg2(val);
+    int i, j, k;
+    long long idx;
+    xy_coords<AX>(g, lineA, pos, i, j, k, idx);
+    st_ab<AX>(g, st, i, j, k, idx, val);
+  };
+#pragma unroll
+  for (int b = 0; b < PER; ++b) {
+    const int jb = tj + b * TPL;
+    const int jj = jb & (NS - 1);
+    const int base = (jb - jj) * R + jj;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int m = base + r * NS;
+      put(2 * m, v[b][r].im);
+      put(2 * m + 1, v[b][r].re);
+    }
+  }
+}
+
+// Shared-memory twiddle tables: stage twiddles as {c, c, s, s}, Makhoul tables as is.
+template <int N, bool FWD, bool INV>
+__device__ __forceinline__ void pair_tables(const R2RTables<float>& tb, float4* sfft, float2* spost, float2* spre,
+                                            int tid) {
+  constexpr int M = N / 2, NT = PairCfg<N>::NT;
+  for (int t = tid; t < M; t += NT) {
+    const float2 w = __ldg(&tb.fft[t]);
+    sfft[t] = make_float4(w.x, w.x, w.y, w.y);
+  }
+  if constexpr (FWD)
+    for (int t = tid; t < 2 * (M + 1); t += NT) spost[t] = __ldg(&tb.post[t]);
+  if constexpr (INV)
+    for (int t = tid; t < 2 * M; t += NT) spre[t] = __ldg(&tb.pre[t]);
+}
+
+// Everything after the load phase, shared by the direct and the TMA-fed kernels. On
+// entry the PC buffer holds, per kind and axis: x/y forward -> stage-1 output; z forward
+// -> the Makhoul-ordered z; x/y inverse -> the pre-processed, swapped Z; z inverse ->
+// the natural-order reals. Outputs go to global memory through `st`.
+template <int N, int KIND, int AX, class StoreOp, class MulOp>
+__device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int tj, int tid, PC* buf,
+                                          const float4* sfft, const float2* spost, const float2* spre,
+                                          const StoreOp& st, const MulOp& mul) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
+  constexpr int R1 = Cf::R1;
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool xy = (AX != 2);
+  constexpr int ZU = (LP * NQ) / NT;
+  constexpr int ZC = (ZU >= 4) ? 4 : ZU;
+  static_assert(ZU * NT == LP * NQ && ZU % ZC == 0, "z units");
+  float2* rb2 = reinterpret_cast<float2*>(buf);
+  const int lineA = 2 * (pair0 + lp);
+  if constexpr (!xy) {
+    if constexpr (fwd_in) pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
+    else pair_pre<N>(buf, spre, lp, tj);
+  }
+
+  // ---------------- forward FFT + post ----------------
+  if constexpr (fwd_in) {
+    pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
+    if constexpr (xy && KIND != K_FILT && KIND != K_DERIV) {
+      pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
+      return;
+    }
+    pair_post<N, (KIND == K_DERIV ? K_C2 : KIND), AX, MulOp>(g, lineA, buf, spost, lp, tj, mul);
+    if constexpr (KIND == K_DERIV) {
+      // w_i = mul(i) u_{i+1} (w_{N-1} = 0), stored reversed as the DST-III input
+      constexpr int PER = N / TPL;
+      float2 w[PER];
+#pragma unroll
+      for (int b = 0; b < PER; ++b) {
+        const int i = tj + b * TPL;
+        w[b] = f2(0.f);
+        if (i < N - 1) {
+          int ii, jj, kk;
+          long long idx;
+          line_coords(g, AX, lineA, i, ii, jj, kk, idx);
+          w[b] = mul2(mul_ab<AX>(mul, ii, jj, kk), rb2[rpi<PP>(i + 1, lp)]);
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int b = 0; b < PER; ++b) rb2[rpi<PP>(N - 1 - (tj + b * TPL), lp)] = w[b];
+      __syncthreads();
+    }
+    if constexpr (inv_out) pair_pre<N>(buf, spre, lp, tj);
+  }
+
+  // ---------------- inverse FFT ----------------
+  if constexpr (inv_out) {
+    pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
+    if constexpr (xy) {
+      pair_last_store<N, KIND, AX>(g, lineA, buf, sfft, lp, tj, st);
+      return;
+    }
+    pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
+  }
+
+  // ---------------- z store (float4 per line) ----------------
+#pragma unroll 1
+  for (int c0 = 0; c0 < ZU; c0 += ZC) {
+    float4 oa[ZC], ob[ZC];
+#pragma unroll
+    for (int c = 0; c < ZC; ++c) {
+      const int u = tid + (c0 + c) * NT;
+      const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+      if constexpr (inv_out) {
+        // x_4a = slot a .im, x_4a+1 = slot M-1-a .re, x_4a+2 = slot a .re, x_4a+3 = slot M-1-a .im
+        const PC sa = buf[a * PP + q], sb = buf[(M - 1 - a) * PP + q];
+        oa[c] = make_float4(sa.im.x, sb.re.x, sa.re.x, sb.im.x);
+        ob[c] = make_float4(sa.im.y, sb.re.y, sa.re.y, sb.im.y);
+        if constexpr (KIND == K_S3 || KIND == K_DERIV) {
+          oa[c].y = -oa[c].y; oa[c].w = -oa[c].w;
+          ob[c].y = -ob[c].y; ob[c].w = -ob[c].w;
+        }
+      } else {
+        // natural order: slot 2a = (y_4a, y_4a+1), slot 2a+1 = (y_4a+2, y_4a+3)
+        const PC s0 = buf[(2 * a) * PP + q], s1 = buf[(2 * a + 1) * PP + q];
+        oa[c] = make_float4(s0.re.x, s0.im.x, s1.re.x, s1.im.x);
+        ob[c] = make_float4(s0.re.y, s0.im.y, s1.re.y, s1.im.y);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < ZC; ++c) {
+      const int u = tid + (c0 + c) * NT;
+      const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+      const int la = 2 * (pair0 + q);
+      const int i = la >> g.ly, j = la & (g.ny - 1);
+      const long long idx = (long long)(la * N + 4 * a);
+      st_q(st, i, j, 4 * a, idx, oa[c]);
+      st_q(st, i, j + 1, 4 * a, idx + N, ob[c]);
+    }
+  }
+}
+
+template <int N, int KIND, int AX, class LoadOp, class StoreOp, class MulOp>
+__global__ void __launch_bounds__(PairCfg<N>::NT) r2r_pair_kernel(Grid g, R2RTables<float> tb, LoadOp ld,
+                                                                  StoreOp st, MulOp mul) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
+  constexpr int R1 = Cf::R1;
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool xy = (AX != 2);
+  constexpr int ZU = (LP * NQ) / NT;  // z phases: (line pair, float4) units per thread
+  constexpr int ZC = (ZU >= 4) ? 4 : ZU;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PC* buf = reinterpret_cast<PC*>(smem_raw);
+  float4* sfft = reinterpret_cast<float4*>(buf + M * PP);
+  float2* spost = reinterpret_cast<float2*>(sfft + M);
+  float2* spre = spost + 2 * (M + 1);
+  const int tid = threadIdx.x;
+  const int lp = tid & (LP - 1), tj = tid >> Cf::LOG2LP;
+  const int pair0 = blockIdx.x * LP;
+  const int lineA = 2 * (pair0 + lp);
+  pair_tables<N, fwd_in, inv_out>(tb, sfft, spost, spre, tid);
+  __syncthreads();
+
+  // ---------------- load ----------------
+  if constexpr (xy && fwd_in) {
+    // z_m = v_2m + i v_2m+1 of both lines straight into the first radix-R1 butterfly
+    PC v[R1];
+#pragma unroll
+    for (int r = 0; r < R1; ++r) {
+      const int m = tj + r * TPL;
+      const int p0 = mk_pos<N>(2 * m), p1 = mk_pos<N>(2 * m + 1);
+      int i, j, k;
+      long long idx;
+      xy_coords<AX>(g, lineA, p0, i, j, k, idx);
+      float2 a = ld_ab<AX>(g, ld, i, j, k, idx);
+      xy_coords<AX>(g, lineA, p1, i, j, k, idx);
+      float2 b = ld_ab<AX>(g, ld, i, j, k, idx);
+      if constexpr (KIND == K_S2) {
+        if (p0 & 1) a = neg2(a);
+        if (p1 & 1) b = neg2(b);
+      }
+      v[r] = pmake(a, b);
+    }
+    PDft<R1>::run(v);
+#pragma unroll
+    for (int r = 0; r < R1; ++r) buf[(tj * R1 + r) * PP + lp] = v[r];
+    __syncthreads();
+  } else if constexpr (xy) {
+    // inverse-only x/y kinds: the pre-processing reads its four reals per pair straight
+    // from global memory (reversed for DST-III)
+    constexpr int NP = (M / 2) / TPL;
+    auto X = [&](int r) -> float2 {
+      const int p = (KIND == K_S3) ? (N - 1 - r) : r;
+      int i, j, k;
+      long long idx;
+      xy_coords<AX>(g, lineA, p, i, j, k, idx);
+      return ld_ab<AX>(g, ld, i, j, k, idx);
+    };
+    PC z[NP][2];
+    PC zmid = pmake(f2(0.f), f2(0.f));
+#pragma unroll
+    for (int b = 0; b < NP; ++b) {
+      const int k = tj + b * TPL;
+      const float2 xnk = (k == 0) ? f2(0.f) : X(N - k);
+      pair_pre_one(spre, M, k, X(k), xnk, X(M - k), X(M + k), z[b][0], z[b][1]);
+    }
+    if (tj == 0) {
+      const int k = M / 2;
+      const PC U = pmake(X(k), neg2(X(N - k)));
+      zmid = pcomb(spre[2 * k], U, spre[2 * k + 1], U);
+    }
+#pragma unroll
+    for (int b = 0; b < NP; ++b) {
+      const int k = tj + b * TPL;
+      buf[k * PP + lp] = pswap(z[b][0]);
+      if (k > 0) buf[(M - k) * PP + lp] = pswap(z[b][1]);
+    }
+    if (tj == 0) buf[(M / 2) * PP + lp] = pswap(zmid);
+    __syncthreads();
+  } else {
+    // z: four consecutive elements of each line of a pair per unit (float4)
+#pragma unroll 1
+    for (int c0 = 0; c0 < ZU; c0 += ZC) {
+      float4 xa[ZC], xb[ZC];
+#pragma unroll
+      for (int c = 0; c < ZC; ++c) {
+        const int u = tid + (c0 + c) * NT;
+        const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+        const int la = 2 * (pair0 + q);
+        const int i = la >> g.ly, j = la & (g.ny - 1);
+        const long long idx = (long long)(la * N + 4 * a);
+        xa[c] = ld_q(ld, i, j, 4 * a, idx);
+        xb[c] = ld_q(ld, i, j + 1, 4 * a, idx + N);
+      }
+#pragma unroll
+      for (int c = 0; c < ZC; ++c) {
+        const int u = tid + (c0 + c) * NT;
+        const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+        float4 A = xa[c], B = xb[c];
+        if constexpr (fwd_in) {
+          if constexpr (KIND == K_S2) {  // (-1)^p x_p
+            A.y = -A.y; A.w = -A.w;
+            B.y = -B.y; B.w = -B.w;
+          }
+          // z_a = (x_4a, x_4a+2), z_{M-1-a} = (x_4a+3, x_4a+1)
+          buf[a * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.z, B.z));
+          buf[(M - 1 - a) * PP + q] = pmake(make_float2(A.w, B.w), make_float2(A.y, B.y));
+        } else if constexpr (KIND == K_S3) {
+          // X_r = x_{N-1-r}: slot M-2a-2 = (x_4a+3, x_4a+2), slot M-2a-1 = (x_4a+1, x_4a)
+          buf[(M - 2 * a - 2) * PP + q] = pmake(make_float2(A.w, B.w), make_float2(A.z, B.z));
+          buf[(M - 2 * a - 1) * PP + q] = pmake(make_float2(A.y, B.y), make_float2(A.x, B.x));
+        } else {
+          buf[(2 * a) * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.y, B.y));
+          buf[(2 * a + 1) * PP + q] = pmake(make_float2(A.z, B.z), make_float2(A.w, B.w));
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  pair_tail<N, KIND, AX>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
+}
+
+}  // namespace swc

@@ -1,0 +1,277 @@
+// swc_r2r_tma.cuh -- the FP32 two-line r2r pass fed by the Tensor Memory Accelerator.
+//
+// Persistent CTAs walk tiles of 2 LP lines. Each tile arrives in shared memory by one
+// asynchronous copy -- a tiled tensor-map load (cp.async.bulk.tensor.3d) for x/y
+// passes, whose tile is N rows of 2 LP adjacent lines, and a contiguous bulk copy
+// (cp.async.bulk) for z passes, whose 2 LP lines are one block of memory -- issued by
+// one thread as soon as the previous tile has left the staging buffer, so the DRAM
+// read of tile t+1 overlaps the transform and the stores of tile t. Completion is an
+// mbarrier transaction count; every wait is bounded: a wait that runs out sets the
+// tables' status flag and the CTA returns after one more bounded wait for its copy in
+// flight.
+// Used for plain FP32 loads (LdPlain<float, float>), any store/multiplier.
+#pragma once
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <type_traits>
+
+#include "swc_r2r_pair.cuh"
+
+namespace swc {
+
+constexpr int kTmaWaitIters = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < kTmaWaitIters; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// tiled 3D tensor load into shared memory, completing on an mbarrier
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
+}
+// contiguous bulk load (16-byte aligned addresses, size a multiple of 16 bytes)
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+template <int N> struct TmaCfg {
+  using Cf = PairCfg<N>;
+  static constexpr int LINES = 2 * Cf::LP;              // lines per tile
+  static constexpr int TILE_BYTES = LINES * N * 4;      // staging buffer
+  static constexpr int BOXN = (N < 256) ? N : 256;      // tensor box extent along the pass axis
+  static constexpr int NBOX = N / BOXN;
+  static_assert(TILE_BYTES < (1 << 20), "mbarrier transaction count");
+  // staging tile + PC work buffer + tables + mbarrier
+  static constexpr size_t smem_bytes() { return (size_t)TILE_BYTES + Cf::smem_bytes() + 16; }
+};
+
+// x/y: a tile must not straddle rows of the array (nz a multiple of the tile's lines).
+template <int N> inline bool tma_pass_supported(const Grid& g, int axis) {
+  if (!pair_pass_supported<N>(g, axis)) return false;
+  const long long nlines = g.ng / N;
+  if (nlines % TmaCfg<N>::LINES) return false;
+  return axis == 2 || (g.nz % TmaCfg<N>::LINES) == 0;
+}
+
+// one thread: expect the tile's bytes on the mbarrier and start its copy
+template <int N, int AX>
+__device__ __forceinline__ void tma_issue(const Grid& g, const CUtensorMap* map, const float* zsrc, int t,
+                                          uint32_t sdst, uint32_t bar) {
+  using Tc = TmaCfg<N>;
+  mbar_expect_tx(bar, Tc::TILE_BYTES);
+  const int line0 = t * Tc::LINES;
+  if constexpr (AX == 2) {
+    bulk_load(sdst, zsrc + (size_t)line0 * N, Tc::TILE_BYTES, bar);
+  } else {
+    const int k0 = line0 & (g.nz - 1), o = line0 >> g.lz;  // o = i (y pass) or j (x pass)
+#pragma unroll
+    for (int b = 0; b < Tc::NBOX; ++b) {
+      const uint32_t d = sdst + (uint32_t)(b * Tc::BOXN * Tc::LINES * 4);
+      if constexpr (AX == 1) tma_load_3d(d, map, k0, b * Tc::BOXN, o, bar);
+      else tma_load_3d(d, map, k0, o, b * Tc::BOXN, bar);
+    }
+  }
+}
+
+template <int N, int KIND, int AX, class StoreOp, class MulOp>
+__global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                 const float* __restrict__ zsrc, Grid g,
+                                                                 R2RTables<float> tb, StoreOp st, MulOp mul,
+                                                                 int ntiles) {
+  using Cf = PairCfg<N>;
+  using Tc = TmaCfg<N>;
+  constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
+  constexpr int R1 = Cf::R1;
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool xy = (AX != 2);
+  constexpr int ZU = (LP * NQ) / NT;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  const float* S = reinterpret_cast<const float*>(tma_smem);
+  PC* buf = reinterpret_cast<PC*>(tma_smem + Tc::TILE_BYTES);
+  float4* sfft = reinterpret_cast<float4*>(buf + M * PP);
+  float2* spost = reinterpret_cast<float2*>(sfft + M);
+  float2* spre = spost + 2 * (M + 1);
+  const uint32_t bar = smem_u32(spre + 2 * M);
+  const uint32_t sdst = smem_u32(S);
+  const int tid = threadIdx.x;
+  const int lp = tid & (LP - 1), tj = tid >> Cf::LOG2LP;
+
+  pair_tables<N, fwd_in, inv_out>(tb, sfft, spost, spre, tid);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    if ((int)blockIdx.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, blockIdx.x, sdst, bar);
+  }
+  __syncthreads();
+
+  uint32_t parity = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, parity ^= 1u) {
+    const bool ok = mbar_wait_bounded(bar, parity);
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) {
+        if (tb.status) atomicExch(tb.status, 1);
+        mbar_wait_bounded(bar, parity);  // the copy in flight must land before the CTA leaves
+      }
+      return;
+    }
+    const int pair0 = t * LP;
+    // ---- staging tile -> PC buffer ----
+    if constexpr (xy && fwd_in) {
+      // rows p of the tile hold the tile's lines side by side: (A, B) = one float2
+      const float2* S2 = reinterpret_cast<const float2*>(S);
+      PC v[R1];
+#pragma unroll
+      for (int r = 0; r < R1; ++r) {
+        const int m = tj + r * TPL;
+        const int p0 = mk_pos<N>(2 * m), p1 = mk_pos<N>(2 * m + 1);
+        float2 a = S2[p0 * LP + lp], b = S2[p1 * LP + lp];
+        if constexpr (KIND == K_S2) {
+          if (p0 & 1) a = neg2(a);
+          if (p1 & 1) b = neg2(b);
+        }
+        v[r] = pmake(a, b);
+      }
+      PDft<R1>::run(v);
+#pragma unroll
+      for (int r = 0; r < R1; ++r) buf[(tj * R1 + r) * PP + lp] = v[r];
+    } else if constexpr (xy) {
+      const float2* S2 = reinterpret_cast<const float2*>(S);
+      constexpr int NP = (M / 2) / TPL;
+      auto X = [&](int r) -> float2 { return S2[((KIND == K_S3) ? (N - 1 - r) : r) * LP + lp]; };
+      PC z[NP][2];
+      PC zmid = pmake(f2(0.f), f2(0.f));
+#pragma unroll
+      for (int b = 0; b < NP; ++b) {
+        const int k = tj + b * TPL;
+        const float2 xnk = (k == 0) ? f2(0.f) : X(N - k);
+        pair_pre_one(spre, M, k, X(k), xnk, X(M - k), X(M + k), z[b][0], z[b][1]);
+      }
+      if (tj == 0) {
+        const int k = M / 2;
+        const PC U = pmake(X(k), neg2(X(N - k)));
+        zmid = pcomb(spre[2 * k], U, spre[2 * k + 1], U);
+      }
+#pragma unroll
+      for (int b = 0; b < NP; ++b) {
+        const int k = tj + b * TPL;
+        buf[k * PP + lp] = pswap(z[b][0]);
+        if (k > 0) buf[(M - k) * PP + lp] = pswap(z[b][1]);
+      }
+      if (tj == 0) buf[(M / 2) * PP + lp] = pswap(zmid);
+    } else {
+      // z: the tile is its 2 LP lines one after another; four elements per float4
+      const float4* S4 = reinterpret_cast<const float4*>(S);
+#pragma unroll 4
+      for (int c = 0; c < ZU; ++c) {
+        const int u = tid + c * NT;
+        const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+        float4 A = S4[(2 * q) * NQ + a], B = S4[(2 * q + 1) * NQ + a];
+        if constexpr (fwd_in) {
+          if constexpr (KIND == K_S2) {
+            A.y = -A.y; A.w = -A.w;
+            B.y = -B.y; B.w = -B.w;
+          }
+          buf[a * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.z, B.z));
+          buf[(M - 1 - a) * PP + q] = pmake(make_float2(A.w, B.w), make_float2(A.y, B.y));
+        } else if constexpr (KIND == K_S3) {
+          buf[(M - 2 * a - 2) * PP + q] = pmake(make_float2(A.w, B.w), make_float2(A.z, B.z));
+          buf[(M - 2 * a - 1) * PP + q] = pmake(make_float2(A.y, B.y), make_float2(A.x, B.x));
+        } else {
+          buf[(2 * a) * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.y, B.y));
+          buf[(2 * a + 1) * PP + q] = pmake(make_float2(A.z, B.z), make_float2(A.w, B.w));
+        }
+      }
+    }
+    __syncthreads();  // the staging tile is free: start the next one
+    if (tid == 0 && t + (int)gridDim.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar);
+    pair_tail<N, KIND, AX>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
+  }
+}
+
+// ---- host side ----------------------------------------------------------------------
+
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of an nx x ny x nz FP32 array for the x (AX = 0) or y (AX = 1) tiles.
+template <int N, int AX> inline cudaError_t make_pass_map(const Grid& g, const float* base, CUtensorMap* map) {
+  using Tc = TmaCfg<N>;
+  auto enc = tensor_map_encoder();
+  if (!enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[3] = {(cuuint64_t)g.nz, (cuuint64_t)g.ny, (cuuint64_t)g.nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.nz * 4, (cuuint64_t)g.ny * g.nz * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)Tc::LINES, AX == 1 ? (cuuint32_t)Tc::BOXN : 1u,
+                             AX == 0 ? (cuuint32_t)Tc::BOXN : 1u};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+template <int N, int KIND, int AX, class ST, class MUL>
+cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t stream, const float* src, ST st,
+                       MUL mul) {
+  using Tc = TmaCfg<N>;
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  if constexpr (AX != 2) {
+    const cudaError_t e = make_pass_map<N, AX>(g, src, &map);
+    if (e != cudaSuccess) return e;
+  }
+  auto kern = r2r_tma_kernel<N, KIND, AX, ST, MUL>;
+  const size_t smem = Tc::smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, occ = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, PairCfg<N>::NT, smem)) != cudaSuccess) return e;
+  const int ntiles = (int)((g.ng / N) / Tc::LINES);
+  const int blocks = std::min(ntiles, std::max(occ, 1) * sms);
+  kern<<<blocks, PairCfg<N>::NT, smem, stream>>>(map, src, g, tb, st, mul, ntiles);
+  return cudaGetLastError();
+}
+
+}  // namespace swc

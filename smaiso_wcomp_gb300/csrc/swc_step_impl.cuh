@@ -70,6 +70,13 @@ template <typename T> struct LdAmp {
     const T p = psi[idx], a = gx[idx], b = gy[idx], c = gz[idx];
     return sqrt(q02 * (p * p) + (a * a) + (b * b) + (c * c));
   }
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const float4 p = ld4v(psi, idx), a = ld4v(gx, idx), b = ld4v(gy, idx), c = ld4v(gz, idx);
+    auto f = [&](float p_, float a_, float b_, float c_) {
+      return sqrtf((float)q02 * (p_ * p_) + (a_ * a_) + (b_ * b_) + (c_ * c_));
+    };
+    return make_float4(f(p.x, a.x, b.x, c.x), f(p.y, a.y, b.y, c.y), f(p.z, a.z, b.z, c.z), f(p.w, a.w, b.w, c.w));
+  }
 };
 
 // scale * exp(-1.57^2 * 2 * |q|^2) as a product of per-axis tables (REF:1280-1281).
@@ -99,6 +106,12 @@ template <typename T> struct LdLpsi {
     const T mq2 = (a * a) + (b * b) + (c * c);
     return alpha * (q02 - mq2) * (T)psiq[idx];
   }
+  __device__ __forceinline__ float4 quad(int i, int j, int k, long long idx) const {
+    const float ab = (float)qx[i] * (float)qx[i] + (float)qy[j] * (float)qy[j];
+    const float4 c = ld4v(qz, k), p = ld4v(psiq, idx);
+    auto f = [&](float cz, float ps) { return (float)alpha * ((float)q02 - (ab + cz * cz)) * ps; };
+    return make_float4(f(c.x, p.x), f(c.y, p.y), f(c.z, p.z), f(c.w, p.w));
+  }
 };
 
 // relax phase: -|q|^2 alpha (q0^2 - |q|^2) psiq (REF:1356-1357).
@@ -111,6 +124,15 @@ template <typename T> struct LdRelaxLap {
     const T mq2 = (a * a) + (b * b) + (c * c);
     return -mq2 * alpha * (q02 - mq2) * (T)psiq[idx];
   }
+  __device__ __forceinline__ float4 quad(int i, int j, int k, long long idx) const {
+    const float ab = (float)qx[i] * (float)qx[i] + (float)qy[j] * (float)qy[j];
+    const float4 c = ld4v(qz, k), p = ld4v(psiq, idx);
+    auto f = [&](float cz, float ps) {
+      const float mq2 = ab + cz * cz;
+      return -mq2 * (float)alpha * ((float)q02 - mq2) * ps;
+    };
+    return make_float4(f(c.x, p.x), f(c.y, p.y), f(c.z, p.z), f(c.w, p.w));
+  }
 };
 
 // rho * dfDlapPsi (REF:1321).
@@ -118,6 +140,10 @@ template <typename T> struct LdRhoL {
   const double* rho;
   const T* lpsi;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)rho[idx] * lpsi[idx]; }
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const float4 r = ld4v(rho, idx), l = ld4v(lpsi, idx);
+    return make_float4(r.x * l.x, r.y * l.y, r.z * l.z, r.w * l.w);
+  }
 };
 
 // rho - c: the gradients (REF:1191-1219) never read mode 0, so a constant offset
@@ -126,11 +152,28 @@ template <typename T> struct LdOffset {
   const double* p;
   double c;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)(p[idx] - c); }
+  __device__ __forceinline__ float2 pair(int, int, int, long long idx) const {
+    const double2 d = *reinterpret_cast<const double2*>(p + idx);
+    return make_float2((float)(d.x - c), (float)(d.y - c));
+  }
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const double2 d0 = *reinterpret_cast<const double2*>(p + idx);
+    const double2 d1 = *reinterpret_cast<const double2*>(p + idx + 2);
+    return make_float4((float)(d0.x - c), (float)(d0.y - c), (float)(d1.x - c), (float)(d1.y - c));
+  }
 };
 
 template <typename T> struct LdSum2 {
   const T *a, *b;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return a[idx] + b[idx]; }
+  __device__ __forceinline__ float2 pair(int, int, int, long long idx) const {
+    const float2 x = ld2v(a, idx), y = ld2v(b, idx);
+    return make_float2(x.x + y.x, x.y + y.y);
+  }
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const float4 x = ld4v(a, idx), y = ld4v(b, idx);
+    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+  }
 };
 
 // First pass of the Nl transform: density AB2 update (REF:2121-2139) and the real
@@ -149,6 +192,38 @@ template <typename T> struct LdNl {
     const T a = amp[idx];
     const T c = ((T)kp * (T)zeta / (a + (T)0.001)) * ((T)rn - (T)rho0 - (T)kp * a) * psi[idx];
     return -mu[idx] + c - ux * gpx[idx] - uy * gpy[idx] - uz * gpz[idx];
+  }
+  // four consecutive elements with 16-byte loads / stores (FP32 fields, FP64 rho, f_rho);
+  // each element is read, then written, by this thread only: read-only-path loads
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const float4 ux = ld4g(vx, idx), uy = ld4g(vy, idx), uz = ld4g(vz, idx);
+    const float4 gx = ld4g(grx, idx), gy = ld4g(gry, idx), gz = ld4g(grz, idx), dv = ld4g(divv, idx);
+    const float4 m = ld4g(mu, idx), am = ld4g(amp, idx), ps = ld4g(psi, idx);
+    const float4 px = ld4g(gpx, idx), py = ld4g(gpy, idx), pz = ld4g(gpz, idx);
+    const double2 r01 = ld2dg(rho, idx), r23 = ld2dg(rho, idx + 2);
+    const double2 f01 = ld2dg(frho, idx), f23 = ld2dg(frho, idx + 2);
+    double rn[4], sr[4];
+    const float ux_[4] = {ux.x, ux.y, ux.z, ux.w}, uy_[4] = {uy.x, uy.y, uy.z, uy.w}, uz_[4] = {uz.x, uz.y, uz.z, uz.w};
+    const float gx_[4] = {gx.x, gx.y, gx.z, gx.w}, gy_[4] = {gy.x, gy.y, gy.z, gy.w}, gz_[4] = {gz.x, gz.y, gz.z, gz.w};
+    const float dv_[4] = {dv.x, dv.y, dv.z, dv.w}, m_[4] = {m.x, m.y, m.z, m.w}, am_[4] = {am.x, am.y, am.z, am.w};
+    const float ps_[4] = {ps.x, ps.y, ps.z, ps.w}, px_[4] = {px.x, px.y, px.z, px.w};
+    const float py_[4] = {py.x, py.y, py.z, py.w}, pz_[4] = {pz.x, pz.y, pz.z, pz.w};
+    const double r_[4] = {r01.x, r01.y, r23.x, r23.y}, f_[4] = {f01.x, f01.y, f23.x, f23.y};
+    float out[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float srho = -ux_[c] * gx_[c] - uy_[c] * gy_[c] - uz_[c] * gz_[c] - (float)r_[c] * dv_[c];
+      rn[c] = r_[c] + dt * (1.5 * (double)srho - 0.5 * f_[c]);
+      sr[c] = (double)srho;
+      const float a = am_[c];
+      const float cc = ((float)kp * (float)zeta / (a + 0.001f)) * ((float)rn[c] - (float)rho0 - (float)kp * a) * ps_[c];
+      out[c] = -m_[c] + cc - ux_[c] * px_[c] - uy_[c] * py_[c] - uz_[c] * pz_[c];
+    }
+    *reinterpret_cast<double2*>(rho + idx) = make_double2(rn[0], rn[1]);
+    *reinterpret_cast<double2*>(rho + idx + 2) = make_double2(rn[2], rn[3]);
+    *reinterpret_cast<double2*>(frho + idx) = make_double2(sr[0], sr[1]);
+    *reinterpret_cast<double2*>(frho + idx + 2) = make_double2(sr[2], sr[3]);
+    return make_float4(out[0], out[1], out[2], out[3]);
   }
 };
 
@@ -188,6 +263,92 @@ template <typename T> struct StNlUpdate {
     psiq[idx] = pn;
     nlq[idx] = nl;
   }
+  // elements idx, idx + 1 (x/y passes: (i, j, k), (i, j, k + 1)) with vector accesses;
+  // each element is read, then written, by this thread only: read-only-path loads
+  __device__ __forceinline__ void pair(int i, int j, int k, long long idx, float2 v) const {
+    const float2 d = ld2g(dq, idx);
+    const float nl0 = v.x - d.x, nl1 = v.y - d.y;
+    float nlo0 = nl0, nlo1 = nl1;
+    if (!first) {
+      const float2 o = ld2g(nlq, idx);
+      nlo0 = o.x;
+      nlo1 = o.y;
+    }
+    const double2 pq = ld2dg(psiq, idx);
+    const double2 pqo = ld2dg(psiq_old, idx);
+    const double s0 = dtd2 * scale * (3.0 * (double)nl0 - (double)nlo0);
+    const double s1 = dtd2 * scale * (3.0 * (double)nl1 - (double)nlo1);
+    double pn0, pn1;
+    if (increment) {
+      const double2 ic = ld2dg(inv_c2, idx);
+      pn0 = pq.x + (0.5 * (pq.x - pqo.x) + s0) * ic.x;
+      pn1 = pq.y + (0.5 * (pq.y - pqo.y) + s1) * ic.y;
+    } else {
+      const double ab = qx[i] * qx[i] + qy[j] * qy[j];
+      auto upd = [&](double cz, double p, double po, double src) {
+        const double s = q02 - (ab + cz * cz);
+        const double aLin = ep - alpha * (s * s);
+        return ((2.0 - dt * rho_m * aLin) * p - 0.5 * po + src) / (1.5 - dt * rho_m * aLin);
+      };
+      pn0 = upd(qz[k], pq.x, pqo.x, s0);
+      pn1 = upd(qz[k + 1], pq.y, pqo.y, s1);
+    }
+    *reinterpret_cast<double2*>(psiq_old + idx) = pq;
+    *reinterpret_cast<double2*>(psiq + idx) = make_double2(pn0, pn1);
+    st2v(nlq, idx, make_float2(nl0, nl1));
+  }
+};
+
+// Mixed engine: the same CN/AB2 update (increment form, FP64 1/C2 table) moved into
+// the loader of the first pass of psi = DCT-III^3 psiq_new (REF:2170-2197): reads the
+// Nl transform's output nl_hat, writes psiq_old, psiq, nlq and returns (float) psiq_new.
+// Fusing it there spares the Nl transform's last pass the heavy FP64 epilogue and the
+// psi transform a re-read of psiq.
+template <typename T> struct LdNlUpdate {
+  const T *nlw, *dq;
+  T* nlq;
+  double *psiq, *psiq_old;
+  const double* inv_c2;
+  double dtd2, scale;
+  int first;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
+    const T nl = nlw[idx] - dq[idx];
+    const T nlo = first ? nl : nlq[idx];
+    const double pq = psiq[idx], pqo = psiq_old[idx];
+    const double src = dtd2 * scale * (3.0 * (double)nl - (double)nlo);
+    const double pn = pq + (0.5 * (pq - pqo) + src) * inv_c2[idx];
+    psiq_old[idx] = pq;
+    psiq[idx] = pn;
+    nlq[idx] = nl;
+    return (T)pn;
+  }
+  // four consecutive elements; each read, then written, by this thread only
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const float4 w = ld4g(nlw, idx), d = ld4g(dq, idx);
+    float nl[4] = {w.x - d.x, w.y - d.y, w.z - d.z, w.w - d.w};
+    float nlo[4] = {nl[0], nl[1], nl[2], nl[3]};
+    if (!first) {
+      const float4 o = ld4g(nlq, idx);
+      nlo[0] = o.x; nlo[1] = o.y; nlo[2] = o.z; nlo[3] = o.w;
+    }
+    const double2 p01 = ld2dg(psiq, idx), p23 = ld2dg(psiq, idx + 2);
+    const double2 o01 = ld2dg(psiq_old, idx), o23 = ld2dg(psiq_old, idx + 2);
+    const double2 c01 = ld2dg(inv_c2, idx), c23 = ld2dg(inv_c2, idx + 2);
+    const double pq[4] = {p01.x, p01.y, p23.x, p23.y}, pqo[4] = {o01.x, o01.y, o23.x, o23.y};
+    const double ic[4] = {c01.x, c01.y, c23.x, c23.y};
+    double pn[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double src = dtd2 * scale * (3.0 * (double)nl[c] - (double)nlo[c]);
+      pn[c] = pq[c] + (0.5 * (pq[c] - pqo[c]) + src) * ic[c];
+    }
+    *reinterpret_cast<double2*>(psiq_old + idx) = p01;
+    *reinterpret_cast<double2*>(psiq_old + idx + 2) = p23;
+    *reinterpret_cast<double2*>(psiq + idx) = make_double2(pn[0], pn[1]);
+    *reinterpret_cast<double2*>(psiq + idx + 2) = make_double2(pn[2], pn[3]);
+    st4v(nlq, idx, make_float4(nl[0], nl[1], nl[2], nl[3]));
+    return make_float4((float)pn[0], (float)pn[1], (float)pn[2], (float)pn[3]);
+  }
 };
 
 // ---------------------------------------------------------------------------------
@@ -209,37 +370,74 @@ template <typename T> struct S6Args {
   int relax;
 };
 
-template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S6Args<T> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.ng) return;
-  double r = a.rho[idx];
-  const T A = a.amp[idx];
-  T lapR = a.lapR[idx];
-  if (a.relax) {
-    // REF:1371-1374: rho reset to rho_0 + kp A during the relax phase
-    // rho_1 + ((1 - rho_1)/Amp) A with (1 - rho_1)/Amp = kp evaluated once on the host
-    r = a.rho0 + a.kp * (double)A;
-    a.rho[idx] = r;
-    lapR = (T)r * lapR;
+// Four consecutive elements of a field (16-byte aligned): float4, or two double2.
+template <typename T> struct V4 {
+  T v[4];
+  __device__ __forceinline__ void load(const T* p, long long idx) {
+    if constexpr (sizeof(T) == 4) {
+      const float4 q = *reinterpret_cast<const float4*>(p + idx);
+      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+      const double2 q0 = *reinterpret_cast<const double2*>(p + idx);
+      const double2 q1 = *reinterpret_cast<const double2*>(p + idx + 2);
+      v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
   }
-  const T rr = (T)r;
-  const T L = a.lpsi[idx];
-  const T p = a.psi[idx];
-  const T E = (T)0.5 * (L * L);
-  const T t = (T)a.rho0 + (T)a.kp * A;
-  a.fgrad[idx] = (T)0.5 * (T)a.zeta * (rr * rr - t * t);
-  const T mu1 = lapR + rr * L;
-  const T gpx = a.gpx[idx], gpy = a.gpy[idx], gpz = a.gpz[idx];
-  a.Sx[idx] = mu1 * gpx + E * a.grx[idx];
-  a.Sy[idx] = mu1 * gpy + E * a.gry[idx];
-  a.Sz[idx] = mu1 * gpz + E * a.grz[idx];
-  const T p2 = p * p;
-  a.mu[idx] = lapR + rr * (L - (T)a.ep * p - (T)a.beta * (p2 * p) + (T)a.gamma * (p2 * p2 * p));
-  a.ener[idx] = rr * E;
-  const T c = (T)a.kp * (T)a.zeta * (rr - (T)a.rho0 - (T)a.kp * A) / (A + (T)0.001);
-  a.fx[idx] = c * gpx;
-  a.fy[idx] = c * gpy;
-  a.fz[idx] = c * gpz;
+  __device__ __forceinline__ void store(T* p, long long idx) const {
+    if constexpr (sizeof(T) == 4) {
+      *reinterpret_cast<float4*>(p + idx) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+      *reinterpret_cast<double2*>(p + idx) = make_double2(v[0], v[1]);
+      *reinterpret_cast<double2*>(p + idx + 2) = make_double2(v[2], v[3]);
+    }
+  }
+};
+
+// Four consecutive points per thread (n^3 is a multiple of 4: every extent is >= 4).
+template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S6Args<T> a) {
+  const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (idx >= g.ng) return;
+  V4<double> r;
+  V4<T> A, lapR, L, P, gpx, gpy, gpz, grx, gry, grz;
+  r.load(a.rho, idx);
+  A.load(a.amp, idx);
+  lapR.load(a.lapR, idx);
+  L.load(a.lpsi, idx);
+  P.load(a.psi, idx);
+  gpx.load(a.gpx, idx); gpy.load(a.gpy, idx); gpz.load(a.gpz, idx);
+  grx.load(a.grx, idx); gry.load(a.gry, idx); grz.load(a.grz, idx);
+  V4<T> fgrad, ener, Sx, Sy, Sz, fx, fy, fz, mu;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (a.relax) {
+      // REF:1371-1374: rho reset to rho_0 + kp A during the relax phase
+      // rho_1 + ((1 - rho_1)/Amp) A with (1 - rho_1)/Amp = kp evaluated once on the host
+      r.v[c] = a.rho0 + a.kp * (double)A.v[c];
+      lapR.v[c] = (T)r.v[c] * lapR.v[c];
+    }
+    const T rr = (T)r.v[c];
+    const T Lc = L.v[c], p = P.v[c], Ac = A.v[c];
+    const T E = (T)0.5 * (Lc * Lc);
+    const T t = (T)a.rho0 + (T)a.kp * Ac;
+    fgrad.v[c] = (T)0.5 * (T)a.zeta * (rr * rr - t * t);
+    const T mu1 = lapR.v[c] + rr * Lc;
+    Sx.v[c] = mu1 * gpx.v[c] + E * grx.v[c];
+    Sy.v[c] = mu1 * gpy.v[c] + E * gry.v[c];
+    Sz.v[c] = mu1 * gpz.v[c] + E * grz.v[c];
+    const T p2 = p * p;
+    mu.v[c] = lapR.v[c] + rr * (Lc - (T)a.ep * p - (T)a.beta * (p2 * p) + (T)a.gamma * (p2 * p2 * p));
+    ener.v[c] = rr * E;
+    const T cc = (T)a.kp * (T)a.zeta * (rr - (T)a.rho0 - (T)a.kp * Ac) / (Ac + (T)0.001);
+    fx.v[c] = cc * gpx.v[c];
+    fy.v[c] = cc * gpy.v[c];
+    fz.v[c] = cc * gpz.v[c];
+  }
+  if (a.relax) r.store(a.rho, idx);
+  fgrad.store(a.fgrad, idx);
+  Sx.store(a.Sx, idx); Sy.store(a.Sy, idx); Sz.store(a.Sz, idx);
+  mu.store(a.mu, idx);
+  ener.store(a.ener, idx);
+  fx.store(a.fx, idx); fy.store(a.fy, idx); fz.store(a.fz, idx);
 }
 
 // 1/C2 per spectral mode in FP64 (REF:957-958), built once for the mixed engine.
@@ -466,6 +664,7 @@ template <typename T> class StepEngine : public EngineBase {
   size_t tape_steps_ = 0;
   double* adj_ = nullptr;          // adjoint work arrays
   double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
+  int* status_ = nullptr;          // set by a transform pass whose bounded wait ran out
   size_t pgrad_doubles() const { return 8 * (1 + (size_t)((g_.ng + 255) / 256)); }
   bool adj_valid_ = false;         // checkpoints describe the run since swc_set_state
   // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
@@ -480,6 +679,9 @@ template <typename T> class StepEngine : public EngineBase {
     else return tabd_.t[a];
   }
   int enqueue_step(bool relax, bool first, bool diag);
+  int enqueue_part_a(bool relax, bool first, bool diag);  // S1-S5
+  int enqueue_part_b(bool relax, bool first, bool diag);  // S5 tail-S10 (swc_step_part_b.cuh)
+  int enqueue_part_c(bool relax, bool first, bool diag);  // S11-S14 (swc_step_part_c.cuh)
   int run_graph(bool relax, bool first, bool diag);
   void release();
   int field_src(int field, const void** src, bool* is_double);
@@ -579,8 +781,16 @@ template <typename T> int StepEngine<T>::init() {
     *out = ptr;
     return SWC_OK;
   };
+  // status flag of the transform passes' bounded waits (0 = fine)
+  {
+    int rc = dalloc(sizeof(int), (void**)&status_);
+    if (rc) return rc;
+    SWC_CK(cudaMemsetAsync(status_, 0, sizeof(int), stream_));
+  }
   // wavenumbers REF:445-481 and Gaussian factors, per axis
   for (int a = 0; a < 3; ++a) {
+    tab_.t[a].status = status_;
+    tabd_.t[a].status = status_;
     const int n = dims[a];
     std::vector<double> vq(n), vs(n), gq(n), gs(n);
     for (int i = 0; i < n; ++i) {
@@ -656,10 +866,19 @@ int StepEngine<T>::passU(LD ld, ST st, MUL mul) {
     if (rc_) return rc_;   \
   } while (0)
 
+// The step is enqueued in three parts, each compiled in its own translation unit
+// (parts B and C live in swc_step_part_b.cuh / swc_step_part_c.cuh) so the many pass
+// instantiations build in parallel.
 template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bool diag) {
+  SWC_TRY(enqueue_part_a(relax, first, diag));
+  SWC_TRY(enqueue_part_b(relax, first, diag));
+  return enqueue_part_c(relax, first, diag);
+}
+
+// Part A: S1-S5 (gradients, amplitude filter, dfDlapPsi, lapR).
+template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, bool diag) {
   using LP = LdPlain<T, T>;
   using SP = StPlain<T, T>;
-  const unsigned pw_blocks = (unsigned)((g_.ng + 255) / 256);
 
   // S1 + S2 (REF:1104-1250): rhoq = DCT(rho) and the six shifted spectral gradients
   // taken back to real space. With psiq = scale DCT-II^3 psi and the DCT-III/DCT-II pairs
@@ -700,96 +919,6 @@ template <typename T> int StepEngine<T>::enqueue_step(bool relax, bool first, bo
     SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 0>(LP{lapR_}, SP{lapR_})));
-  }
-  // S5 relax tail + S6 (REF:1363-1425)
-  {
-    S6Args<T> a{lapR_, lpsi_, psi_, amp_f_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2], rho_,
-                fgrad_, ener_, S_[0], S_[1], S_[2], f_[0], f_[1], f_[2], mu_,
-                p_.ep, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, amp_, relax ? 1 : 0};
-    s6_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
-    SWC_CK(cudaGetLastError());
-    ++launches_;
-  }
-  // S7 (REF:1427-1457): forward transforms
-  T* cts[2] = {fgrad_, ener_};
-  for (T* b : cts) {
-    SWC_TRY((pass<K_C2, 2>(LP{b}, SP{b})));
-    SWC_TRY((pass<K_C2, 1>(LP{b}, SP{b})));
-    SWC_TRY((pass<K_C2, 0>(LP{b}, SP{b})));
-  }
-  for (int ax = 0; ax < 3; ++ax) {
-    T* bs[2] = {S_[ax], f_[ax]};
-    for (T* b : bs) {
-      if (ax == 2) SWC_TRY((pass<K_S2, 2>(LP{b}, SP{b})));
-      else SWC_TRY((pass<K_C2, 2>(LP{b}, SP{b})));
-      if (ax == 1) SWC_TRY((pass<K_S2, 1>(LP{b}, SP{b})));
-      else SWC_TRY((pass<K_C2, 1>(LP{b}, SP{b})));
-      if (ax == 0) SWC_TRY((pass<K_S2, 0>(LP{b}, SP{b})));
-      else SWC_TRY((pass<K_C2, 0>(LP{b}, SP{b})));
-    }
-  }
-  // S8 + S9 (REF:1468-1974)
-  {
-    StokesArgs<T> a{S_[0], S_[1], S_[2], fgrad_, ener_, vsol_[0], vsol_[1], vsol_[2], virr_[0], virr_[1],
-                    virr_[2], vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2], gq_[0], gq_[1], gq_[2], gs_[0],
-                    gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu), (T)(1.0 / (p_.lambda + 2 * p_.nu)),
-                    p_.nx / p_.ref_ranks};
-    stokes_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
-    SWC_CK(cudaGetLastError());
-    ++launches_;
-  }
-  // S10 (REF:1977-2091)
-  {
-    DivArgs<T> a{virr_[0], virr_[1], virr_[2], f_[0], f_[1], f_[2], divv_, dq_, vq_[0], vq_[1], vq_[2]};
-    div_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
-    SWC_CK(cudaGetLastError());
-    ++launches_;
-  }
-  SWC_TRY((pass<K_C3, 2>(LP{divv_}, SP{divv_})));
-  SWC_TRY((pass<K_C3, 1>(LP{divv_}, SP{divv_})));
-  SWC_TRY((pass<K_C3, 0>(LP{divv_}, SP{divv_})));
-  // S11 (REF:2093-2117): v = vsol + virr to real space; vsol alone on diagnostic steps
-  for (int ax = 0; ax < 3; ++ax) {
-    for (int which = 0; which < (diag ? 2 : 1); ++which) {
-      T* out = which == 0 ? v_[ax] : vsolr_[ax];
-      if (which == 0) {
-        LdSum2<T> ld{vsol_[ax], virr_[ax]};
-        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
-        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
-      } else {
-        LP ld{vsol_[ax]};
-        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
-        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
-      }
-      if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
-      if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
-    }
-  }
-  // S12 + S13 + S14 (REF:2121-2190): rho update, Nl, its DCT, the psiq update
-  {
-    LdNl<T> ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
-               rho_, frho_, p_.dt, kp_, p_.zeta, p_.rho_0};
-    SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
-    SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
-    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], inv_c2_, p_.ep, p_.alpha, p_.q0 * p_.q0,
-                     p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, std::is_same<T, float>::value ? 1 : 0};
-    SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
-  }
-  // S14 (REF:2194-2197): psi = iDCT(psiq_new)
-  T* pout = diag ? psi_new_ : psi_;
-  SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
-  SWC_TRY((pass<K_C3, 1>(LP{pout}, SP{pout})));
-  SWC_TRY((pass<K_C3, 0>(LP{pout}, SP{pout})));
-  if (diag) {
-    DiagArgs<T> a{psi_new_, lpsi_, amp_f_, psi_, psi_old_, energy_, rho_, partial_,
-                  p_.ep, p_.beta, p_.gamma, p_.zeta, p_.rho_0, kp_};
-    diag_kernel<T><<<diag_blocks_, kDiagThreads, 0, stream_>>>(g_, a);
-    SWC_CK(cudaGetLastError());
-    diag_final_kernel<<<1, 32, 0, stream_>>>(partial_, diag_blocks_, dsum_);
-    SWC_CK(cudaGetLastError());
-    launches_ += 2;
   }
   return SWC_OK;
 }
@@ -939,8 +1068,16 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   SWC_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
   last_ms_ = ms;
   double sums[5];
+  int tma_status = 0;
   SWC_CK(cudaMemcpyAsync(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost, stream_));
+  SWC_CK(cudaMemcpyAsync(&tma_status, status_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
   SWC_CK(cudaStreamSynchronize(stream_));
+  if (tma_status) {
+    SWC_CK(cudaMemsetAsync(status_, 0, sizeof(int), stream_));
+    SWC_CK(cudaStreamSynchronize(stream_));
+    set_error("a tile copy of a transform pass did not complete in time (step %lld)", (long long)nloop_);
+    return SWC_ERR_CUDA;
+  }
   // REF:2244-2258
   diag_.sum_abs_dpsi = sums[0];
   diag_.sum_abs_psi = sums[1];

@@ -1,0 +1,64 @@
+// swc_step_part_b.cuh -- part B of the step: S5 relax tail + S6 pointwise terms, the
+// S7 forward transforms, S8-S10 Stokes solve and divergence (compiled by the engine's
+// *_b.cu translation unit only).
+#pragma once
+
+#include "swc_step_impl.cuh"
+
+namespace swc {
+
+template <typename T> int StepEngine<T>::enqueue_part_b(bool relax, bool first, bool diag) {
+  using LP = LdPlain<T, T>;
+  using SP = StPlain<T, T>;
+  const unsigned pw_blocks = (unsigned)((g_.ng + 255) / 256);
+  // S5 relax tail + S6 (REF:1363-1425)
+  {
+    S6Args<T> a{lapR_, lpsi_, psi_, amp_f_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2], rho_,
+                fgrad_, ener_, S_[0], S_[1], S_[2], f_[0], f_[1], f_[2], mu_,
+                p_.ep, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, amp_, relax ? 1 : 0};
+    s6_kernel<T><<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+    ++launches_;
+  }
+  // S7 (REF:1427-1457): forward transforms
+  T* cts[2] = {fgrad_, ener_};
+  for (T* b : cts) {
+    SWC_TRY((pass<K_C2, 2>(LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2, 1>(LP{b}, SP{b})));
+    SWC_TRY((pass<K_C2, 0>(LP{b}, SP{b})));
+  }
+  for (int ax = 0; ax < 3; ++ax) {
+    T* bs[2] = {S_[ax], f_[ax]};
+    for (T* b : bs) {
+      if (ax == 2) SWC_TRY((pass<K_S2, 2>(LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2, 2>(LP{b}, SP{b})));
+      if (ax == 1) SWC_TRY((pass<K_S2, 1>(LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2, 1>(LP{b}, SP{b})));
+      if (ax == 0) SWC_TRY((pass<K_S2, 0>(LP{b}, SP{b})));
+      else SWC_TRY((pass<K_C2, 0>(LP{b}, SP{b})));
+    }
+  }
+  // S8 + S9 (REF:1468-1974)
+  {
+    StokesArgs<T> a{S_[0], S_[1], S_[2], fgrad_, ener_, vsol_[0], vsol_[1], vsol_[2], virr_[0], virr_[1],
+                    virr_[2], vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2], gq_[0], gq_[1], gq_[2], gs_[0],
+                    gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu), (T)(1.0 / (p_.lambda + 2 * p_.nu)),
+                    p_.nx / p_.ref_ranks};
+    stokes_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+    ++launches_;
+  }
+  // S10 (REF:1977-2091)
+  {
+    DivArgs<T> a{virr_[0], virr_[1], virr_[2], f_[0], f_[1], f_[2], divv_, dq_, vq_[0], vq_[1], vq_[2]};
+    div_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+    ++launches_;
+  }
+  SWC_TRY((pass<K_C3, 2>(LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3, 1>(LP{divv_}, SP{divv_})));
+  SWC_TRY((pass<K_C3, 0>(LP{divv_}, SP{divv_})));
+  return SWC_OK;
+}
+
+}  // namespace swc

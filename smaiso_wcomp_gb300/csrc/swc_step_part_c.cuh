@@ -1,0 +1,66 @@
+// swc_step_part_c.cuh -- part C of the step: S11 velocities to real space, S12-S14
+// density update, Nl transform, psiq update, psi back to real space and the diagnostic
+// reductions (compiled by the engine's *_c.cu translation unit only).
+#pragma once
+
+#include "swc_step_impl.cuh"
+
+namespace swc {
+
+template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, bool diag) {
+  using LP = LdPlain<T, T>;
+  using SP = StPlain<T, T>;
+  // S11 (REF:2093-2117): v = vsol + virr to real space; vsol alone on diagnostic steps
+  for (int ax = 0; ax < 3; ++ax) {
+    for (int which = 0; which < (diag ? 2 : 1); ++which) {
+      T* out = which == 0 ? v_[ax] : vsolr_[ax];
+      if (which == 0) {
+        LdSum2<T> ld{vsol_[ax], virr_[ax]};
+        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
+        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
+      } else {
+        LP ld{vsol_[ax]};
+        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
+        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
+      }
+      if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
+      if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
+      else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
+    }
+  }
+  // S12 + S13 + S14 (REF:2121-2197): rho update, Nl, its DCT, the psiq update, psi = iDCT(psiq_new)
+  T* pout = diag ? psi_new_ : psi_;
+  {
+    LdNl<T> ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
+               rho_, frho_, p_.dt, kp_, p_.zeta, p_.rho_0};
+    SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
+    SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
+    if constexpr (std::is_same<T, double>::value) {
+      // FP64 engine: the reference's CN expression in the Nl transform's last pass
+      StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], inv_c2_, p_.ep, p_.alpha,
+                       p_.q0 * p_.q0, p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, 0};
+      SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
+      SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
+    } else {
+      // mixed engine: the increment-form update fused into the psi transform's first pass
+      SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
+      LdNlUpdate<T> lu{nlw_, dq_, nlq_, psiq_, psiq_old_, inv_c2_, p_.dt / 2, scale_, first ? 1 : 0};
+      SWC_TRY((pass<K_C3, 2>(lu, SP{pout})));
+    }
+  }
+  SWC_TRY((pass<K_C3, 1>(LP{pout}, SP{pout})));
+  SWC_TRY((pass<K_C3, 0>(LP{pout}, SP{pout})));
+  if (diag) {
+    DiagArgs<T> a{psi_new_, lpsi_, amp_f_, psi_, psi_old_, energy_, rho_, partial_,
+                  p_.ep, p_.beta, p_.gamma, p_.zeta, p_.rho_0, kp_};
+    diag_kernel<T><<<diag_blocks_, kDiagThreads, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
+    diag_final_kernel<<<1, 32, 0, stream_>>>(partial_, diag_blocks_, dsum_);
+    SWC_CK(cudaGetLastError());
+    launches_ += 2;
+  }
+  return SWC_OK;
+}
+
+}  // namespace swc

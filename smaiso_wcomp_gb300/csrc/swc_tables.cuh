@@ -5,7 +5,7 @@
 #include <vector>
 
 #include "swc_r2r.cuh"
-#include "swc_r2r_fast.cuh"
+#include "swc_r2r_tma.cuh"
 
 namespace swc {
 
@@ -110,31 +110,70 @@ cudaError_t launch_fast(const Grid& g, const R2RTables<U>& tb, cudaStream_t stre
   return cudaGetLastError();
 }
 
-// Launch one axis pass on `stream` (in place or out of place per the functors):
-// the compile-time kernel for line lengths 64..512, the runtime one otherwise.
+template <int N, int KIND, int AX, class LD, class ST, class MUL>
+cudaError_t launch_pair(const Grid& g, const R2RTables<float>& tb, cudaStream_t stream, LD ld, ST st, MUL mul) {
+  using Cf = PairCfg<N>;
+  const size_t smem = Cf::smem_bytes();
+  auto kern = r2r_pair_kernel<N, KIND, AX, LD, ST, MUL>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const unsigned blocks = (unsigned)((g.ng / N) / (2 * Cf::LP));
+  kern<<<blocks, Cf::NT, smem, stream>>>(g, tb, ld, st, mul);
+  return cudaGetLastError();
+}
+
+// Launch one axis pass on `stream` (in place or out of place per the functors): for
+// line lengths 64..512 the compile-time kernels (FP32: two lines per thread with packed
+// arithmetic; FP64: one line per thread group), the runtime one otherwise.
 template <typename U, int KIND, int AX, class LD, class ST, class MUL>
 cudaError_t launch_pass(const Grid& g, const R2RTables<U>& tb, cudaStream_t stream, LD ld, ST st, MUL mul) {
   constexpr int axis = AX;
   const int dims[3] = {g.nx, g.ny, g.nz};
   const int n = dims[axis];
-  if (n == 256 && fast_pass_supported<U, 256>(g, axis))
-    return launch_fast<U, 256, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
-  if (n == 128 && fast_pass_supported<U, 128>(g, axis))
-    return launch_fast<U, 128, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
-  if (n == 512 && fast_pass_supported<U, 512>(g, axis))
-    return launch_fast<U, 512, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
-  if (n == 64 && fast_pass_supported<U, 64>(g, axis))
-    return launch_fast<U, 64, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
-  const PassShape ps = make_shape(g, axis, sizeof(U));
-  const size_t smem = pass_smem_bytes(ps, sizeof(U));
-  auto kern = r2r_pass_kernel<U, KIND, 0, LD, ST, MUL>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+  if constexpr (std::is_same<U, float>::value && std::is_same<LD, LdPlain<float, float>>::value) {
+    // plain FP32 input: TMA-fed persistent pass
+    if (n == 256 && tma_pass_supported<256>(g, axis))
+      return launch_tma<256, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul);
+    if (n == 128 && tma_pass_supported<128>(g, axis))
+      return launch_tma<128, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul);
+    if (n == 512 && tma_pass_supported<512>(g, axis))
+      return launch_tma<512, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul);
+    if (n == 64 && tma_pass_supported<64>(g, axis))
+      return launch_tma<64, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul);
+  } else if constexpr (std::is_same<U, float>::value) {
+    // fused FP32 loaders: two lines per thread, direct loads
+    if (n == 256 && pair_pass_supported<256>(g, axis))
+      return launch_pair<256, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 128 && pair_pass_supported<128>(g, axis))
+      return launch_pair<128, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 512 && pair_pass_supported<512>(g, axis))
+      return launch_pair<512, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 64 && pair_pass_supported<64>(g, axis))
+      return launch_pair<64, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+  } else {
+    if (n == 256 && fast_pass_supported<U, 256>(g, axis))
+      return launch_fast<U, 256, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 128 && fast_pass_supported<U, 128>(g, axis))
+      return launch_fast<U, 128, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 512 && fast_pass_supported<U, 512>(g, axis))
+      return launch_fast<U, 512, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 64 && fast_pass_supported<U, 64>(g, axis))
+      return launch_fast<U, 64, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
   }
-  const unsigned blocks = (unsigned)(ps.nlines / ps.L);
-  kern<<<blocks, ps.L * ps.tpl, smem, stream>>>(g, ps, tb, ld, st, mul);
-  return cudaGetLastError();
+  {
+    const PassShape ps = make_shape(g, axis, sizeof(U));
+    const size_t smem = pass_smem_bytes(ps, sizeof(U));
+    auto kern = r2r_pass_kernel<U, KIND, 0, LD, ST, MUL>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    const unsigned blocks = (unsigned)(ps.nlines / ps.L);
+    kern<<<blocks, ps.L * ps.tpl, smem, stream>>>(g, ps, tb, ld, st, mul);
+    return cudaGetLastError();
+  }
 }
 
 }  // namespace swc

@@ -38,6 +38,32 @@ def test_every_length_and_axis(lib, oracle_mod, n, axis, prec):
         assert err <= 40 * eps * np.log2(8 * n), (kinds, err)
 
 
+@pytest.mark.parametrize("n", [64, 128, 256, 512])
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_fp32_two_line_pass(lib, oracle_mod, n, axis):
+    """FP32 compile-time lengths on every axis and kind, against the oracle, with nz = 64
+    and 512 lines so every axis takes the TMA-fed two-lines-per-thread pass."""
+    shape = [8, 8, 64] if axis != 2 else [8, 64, n]
+    shape[axis] = n
+    a = np.random.default_rng(100 * n + axis).standard_normal(shape)
+    for kinds in [(0, 0, 0), (1, 1, 1), (2, 2, 2), (3, 3, 3), (2, 1, 0), (3, 0, 1), (1, 2, 3)]:
+        ref = oracle_mod.r2r3d(a, kinds)
+        got = R2RPlan(shape, kinds, abi.SWC_PREC_MIXED, lib=lib)(a)
+        err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert err <= 40 * 1.2e-7 * np.log2(8 * n), (kinds, err)
+
+
+def test_misaligned_device_buffer_is_rejected(lib):
+    torch = pytest.importorskip("torch")
+    from smaiso_wcomp_gb300.engine import SwcError
+    t = torch.zeros(8 * 8 * 64 + 4, dtype=torch.float32, device="cuda")
+    plan = R2RPlan((8, 8, 64), (0, 0, 0), abi.SWC_PREC_MIXED, lib=lib)
+    with pytest.raises(SwcError):
+        plan.execute_device(t.data_ptr() + 4, torch.cuda.current_stream().cuda_stream)
+    with pytest.raises(SwcError):
+        plan.execute_axis(2, t.data_ptr() + 4, torch.cuda.current_stream().cuda_stream)
+
+
 @pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
 def test_round_trip_256(lib, prec):
     """Size-independent property at the benchmark size: DCT-III^3(DCT-II^3 x) = (2n)^3 x,

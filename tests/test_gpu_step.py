@@ -65,16 +65,19 @@ def test_fp64_step_parity(lib, oracle_mod, shape, kw, gen, schedule):
     assert de["step"] == do["step"] == sum(schedule)
 
 
-def test_mixed_step_accuracy(lib, oracle_mod):
-    p = abi.default_params(32, 32, 32, rho_0=0.8, divv_switch=10)
+@pytest.mark.parametrize("shape,nsteps", [((32, 32, 32), 60), ((64, 64, 64), 30), ((128, 64, 64), 16)])
+def test_mixed_step_accuracy(lib, oracle_mod, shape, nsteps):
+    """Mixed engine against the FP64 oracle; 64 and 128 point lines run the FP32
+    two-lines-per-thread pass, 32 point lines the runtime-length one."""
+    p = abi.default_params(*shape, rho_0=0.8, divv_switch=10)
     psi, rho = ic.undulated_interface(p)
     o = oracle_mod.Oracle(p)
     o.set_state(psi, rho)
-    o.step(60)
-    pm = abi.default_params(32, 32, 32, rho_0=0.8, divv_switch=10, precision=abi.SWC_PREC_MIXED)
+    o.step(nsteps)
+    pm = abi.default_params(*shape, rho_0=0.8, divv_switch=10, precision=abi.SWC_PREC_MIXED)
     with Engine(pm) as e:
         e.set_state(psi, rho)
-        e.step(60)
+        e.step(nsteps)
         for f in ("psi", "rho"):
             assert rel(e.field(f), o.field(f)) <= 1e-5, f
         for f in ("vx", "vy", "vz"):
