@@ -188,7 +188,9 @@ int swc_step(swc_ctx* ctx, int nsteps);
 /* Read the diagnostics of the last swc_step call. */
 int swc_diagnostics(swc_ctx* ctx, swc_diag* out);
 
-/* Copy one field (SWC_F_*) to host memory as nx*ny*nz doubles. */
+/* Copy one field (SWC_F_*) to host memory as nx*ny*nz doubles. Pinned (page-locked)
+ * host memory gets a direct DMA copy; the mixed engine widens FP32 fields on the
+ * device into a staging buffer it allocates on the first such call. */
 int swc_get_field(swc_ctx* ctx, int field, double* dst);
 
 /* Device pointer of a field in the context's own precision (8-byte elements for

@@ -370,6 +370,15 @@ template <typename T> struct S6Args {
   int relax;
 };
 
+// FP32 -> FP64 copy, four elements per thread (n a multiple of 4).
+static __global__ void __launch_bounds__(256) widen_kernel(const float* src, double* dst, long long n) {
+  const long long i = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= n) return;
+  const float4 v = *reinterpret_cast<const float4*>(src + i);
+  *reinterpret_cast<double2*>(dst + i) = make_double2(v.x, v.y);
+  *reinterpret_cast<double2*>(dst + i + 2) = make_double2(v.z, v.w);
+}
+
 // Four consecutive elements of a field (16-byte aligned): float4, or two double2.
 template <typename T> struct V4 {
   T v[4];
@@ -665,6 +674,7 @@ template <typename T> class StepEngine : public EngineBase {
   double* adj_ = nullptr;          // adjoint work arrays
   double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
   int* status_ = nullptr;          // set by a transform pass whose bounded wait ran out
+  double* stage_ = nullptr;        // FP64 staging of FP32 fields for swc_get_field
   size_t pgrad_doubles() const { return 8 * (1 + (size_t)((g_.ng + 255) / 256)); }
   bool adj_valid_ = false;         // checkpoints describe the run since swc_set_state
   // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
@@ -727,7 +737,8 @@ template <typename T> void StepEngine<T>::release() {
   if (tape_) cudaFree(tape_);
   if (adj_) cudaFree(adj_);
   if (pgrad_) cudaFree(pgrad_);
-  tape_ = adj_ = pgrad_ = nullptr;
+  if (stage_) cudaFree(stage_);
+  tape_ = adj_ = pgrad_ = stage_ = nullptr;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
   for (void* a : allocs_) cudaFree(a);
@@ -1141,10 +1152,21 @@ template <typename T> int StepEngine<T>::get_field(int field, double* dst) {
     SWC_CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     SWC_CK(cudaStreamSynchronize(stream_));
   } else {
-    std::vector<T> tmp(n);
-    SWC_CK(cudaMemcpyAsync(tmp.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+    // FP32 field: widened to FP64 on the device (staging buffer allocated on first use),
+    // then one device-to-host copy straight into the caller's buffer
+    if (!stage_) {
+      if (cudaMalloc(&stage_, n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        stage_ = nullptr;
+        set_error("cudaMalloc of the %zu MB field staging buffer failed", (n * 8) >> 20);
+        return SWC_ERR_OOM;
+      }
+    }
+    widen_kernel<<<(unsigned)((n / 4 + 255) / 256), 256, 0, stream_>>>(reinterpret_cast<const float*>(src), stage_,
+                                                                       (long long)n);
+    SWC_CK(cudaGetLastError());
+    SWC_CK(cudaMemcpyAsync(dst, stage_, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     SWC_CK(cudaStreamSynchronize(stream_));
-    for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i];
   }
   return SWC_OK;
 }
