@@ -33,6 +33,7 @@
 
 #include "swc_engine.h"
 #include "swc_r2r.cuh"
+#include "swc_fpconv.h"
 #include "swc_tables.cuh"
 
 namespace swc {
@@ -97,8 +98,9 @@ template <typename T> struct MulLap {
 };
 
 // alpha (q0^2 - |q|^2) psiq (REF:1302).
-template <typename T> struct LdLpsi {
-  const double* psiq;
+// psiq: the FP64 state (FP64 engine) or its FP32 copy (mixed engine).
+template <typename T, typename P = double> struct LdLpsi {
+  const P* psiq;
   const T *qx, *qy, *qz;
   T alpha, q02;
   __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
@@ -115,8 +117,8 @@ template <typename T> struct LdLpsi {
 };
 
 // relax phase: -|q|^2 alpha (q0^2 - |q|^2) psiq (REF:1356-1357).
-template <typename T> struct LdRelaxLap {
-  const double* psiq;
+template <typename T, typename P = double> struct LdRelaxLap {
+  const P* psiq;
   const T *qx, *qy, *qz;
   T alpha, q02;
   __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
@@ -136,13 +138,19 @@ template <typename T> struct LdRelaxLap {
 };
 
 // rho * dfDlapPsi (REF:1321).
-template <typename T> struct LdRhoL {
-  const double* rho;
+// rho: the FP64 state with off = 0 (FP64 engine) or the mixed engine's FP32 copy
+// rho - off with off = (rho_0 + rho_s)/2.
+template <typename T, typename P = double> struct LdRhoL {
+  const P* rho;
   const T* lpsi;
-  __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return (T)rho[idx] * lpsi[idx]; }
+  T off;
+  __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
+    return ((T)rho[idx] + off) * lpsi[idx];
+  }
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
     const float4 r = ld4v(rho, idx), l = ld4v(lpsi, idx);
-    return make_float4(r.x * l.x, r.y * l.y, r.z * l.z, r.w * l.w);
+    const float o = (float)off;
+    return make_float4((r.x + o) * l.x, (r.y + o) * l.y, (r.z + o) * l.z, (r.w + o) * l.w);
   }
 };
 
@@ -227,6 +235,60 @@ template <typename T> struct LdNl {
   }
 };
 
+// Mixed engine, first pass of the Nl transform: the density AB2 update and Nl of LdNl
+// with the FP32 terms in FP32 and FP64 only where the state is. rho_new = rho +
+// (double) dt (1.5 s - 0.5 f_rho) is one FP64 add; f_rho is stored in FP32 (it is the
+// FP32 source s of the previous step); the FP32 copy rhof = rho - off is refreshed from
+// the FP64 sum, and rho = rhof + off is the FP32 density of the FP32 terms. The
+// conversions run on the integer pipes (swc_fpconv.h): two FP64 adds per point remain.
+struct LdNlMixed {
+  const float *vx, *vy, *vz, *grx, *gry, *grz, *divv, *mu, *amp, *psi, *gpx, *gpy, *gpz;
+  double* rho;
+  float *frho, *rhof;
+  double offd;
+  float dt, kp, zeta, rho0, off;
+  __device__ __forceinline__ float point(float ux, float uy, float uz, float gx, float gy, float gz, float dv,
+                                         float m, float a, float ps, float px, float py, float pz, float rf,
+                                         float fp, double& r, float& s, float& rfn) const {
+    s = -ux * gx - uy * gy - uz * gz - (rf + off) * dv;
+    const float inc = dt * (1.5f * s - 0.5f * fp);
+    r = r + widen_f32(inc);
+    rfn = narrow_f64(r - offd);
+    const float c = (kp * zeta / (a + 0.001f)) * ((rfn + off) - rho0 - kp * a) * ps;
+    return -m + c - ux * px - uy * py - uz * pz;
+  }
+  __device__ __forceinline__ float operator()(int, int, int, long long idx) const {
+    double r = rho[idx];
+    float sr, rfn;
+    const float out = point(vx[idx], vy[idx], vz[idx], grx[idx], gry[idx], grz[idx], divv[idx], mu[idx], amp[idx],
+                            psi[idx], gpx[idx], gpy[idx], gpz[idx], rhof[idx], frho[idx], r, sr, rfn);
+    rho[idx] = r;
+    frho[idx] = sr;
+    rhof[idx] = rfn;
+    return out;
+  }
+  // four consecutive elements; each read, then written, by this thread only
+  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
+    const float4 ux = ld4g(vx, idx), uy = ld4g(vy, idx), uz = ld4g(vz, idx);
+    const float4 gx = ld4g(grx, idx), gy = ld4g(gry, idx), gz = ld4g(grz, idx), dv = ld4g(divv, idx);
+    const float4 m = ld4g(mu, idx), am = ld4g(amp, idx), ps = ld4g(psi, idx);
+    const float4 px = ld4g(gpx, idx), py = ld4g(gpy, idx), pz = ld4g(gpz, idx);
+    const float4 rf = ld4g(rhof, idx), fp = ld4g(frho, idx);
+    const double2 r01 = ld2dg(rho, idx), r23 = ld2dg(rho, idx + 2);
+    double r[4] = {r01.x, r01.y, r23.x, r23.y};
+    float sr[4], rfn[4], o[4];
+    o[0] = point(ux.x, uy.x, uz.x, gx.x, gy.x, gz.x, dv.x, m.x, am.x, ps.x, px.x, py.x, pz.x, rf.x, fp.x, r[0], sr[0], rfn[0]);
+    o[1] = point(ux.y, uy.y, uz.y, gx.y, gy.y, gz.y, dv.y, m.y, am.y, ps.y, px.y, py.y, pz.y, rf.y, fp.y, r[1], sr[1], rfn[1]);
+    o[2] = point(ux.z, uy.z, uz.z, gx.z, gy.z, gz.z, dv.z, m.z, am.z, ps.z, px.z, py.z, pz.z, rf.z, fp.z, r[2], sr[2], rfn[2]);
+    o[3] = point(ux.w, uy.w, uz.w, gx.w, gy.w, gz.w, dv.w, m.w, am.w, ps.w, px.w, py.w, pz.w, rf.w, fp.w, r[3], sr[3], rfn[3]);
+    *reinterpret_cast<double2*>(rho + idx) = make_double2(r[0], r[1]);
+    *reinterpret_cast<double2*>(rho + idx + 2) = make_double2(r[2], r[3]);
+    st4v(frho, idx, make_float4(sr[0], sr[1], sr[2], sr[3]));
+    st4v(rhof, idx, make_float4(rfn[0], rfn[1], rfn[2], rfn[3]));
+    return make_float4(o[0], o[1], o[2], o[3]);
+  }
+};
+
 // Last pass of the Nl transform: Nlq = DCT(Nl) - q.f, then the CN/AB2 update of psiq
 // (REF:2170-2190). FP64 engine: the reference's expression; mixed engine: the same
 // update in increment form psiq + (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
@@ -299,33 +361,42 @@ template <typename T> struct StNlUpdate {
   }
 };
 
-// Mixed engine: the same CN/AB2 update (increment form, FP64 1/C2 table) moved into
-// the loader of the first pass of psi = DCT-III^3 psiq_new (REF:2170-2197): reads the
-// Nl transform's output nl_hat, writes psiq_old, psiq, nlq and returns (float) psiq_new.
-// Fusing it there spares the Nl transform's last pass the heavy FP64 epilogue and the
-// psi transform a re-read of psiq.
-template <typename T> struct LdNlUpdate {
-  const T *nlw, *dq;
-  T* nlq;
+// Mixed engine: the CN/AB2 update of psiq (REF:2170-2190) in increment form, fused into
+// the loader of the first pass of psi = DCT-III^3 psiq_new (REF:2194-2197). It reads the
+// Nl transform's output nl_hat, writes psiq_old, psiq, nlq and the FP32 copy psiqf, and
+// returns psiqf. The increment (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
+// a small correction built from FP32 data, is formed in FP32 with an FP32 1/C2 table;
+// FP64 holds the state: two FP64 adds per point (psiq - psiq_old, psiq + increment),
+// conversions on the integer pipes.
+struct LdNlUpdate {
+  const float *nlw, *dq;
+  float* nlq;
   double *psiq, *psiq_old;
-  const double* inv_c2;
-  double dtd2, scale;
+  const float* inv_c2;
+  float* psiqf;
+  float srcs;  // dt/2 scale
   int first;
-  __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
-    const T nl = nlw[idx] - dq[idx];
-    const T nlo = first ? nl : nlq[idx];
-    const double pq = psiq[idx], pqo = psiq_old[idx];
-    const double src = dtd2 * scale * (3.0 * (double)nl - (double)nlo);
-    const double pn = pq + (0.5 * (pq - pqo) + src) * inv_c2[idx];
+  __device__ __forceinline__ float point(float nl, float nlo, double pq, double pqo, float ic, double& pn) const {
+    const float inc = (0.5f * narrow_f64(pq - pqo) + srcs * (3.0f * nl - nlo)) * ic;
+    pn = pq + widen_f32(inc);
+    return narrow_f64(pn);
+  }
+  __device__ __forceinline__ float operator()(int, int, int, long long idx) const {
+    const float nl = nlw[idx] - dq[idx];
+    const float nlo = first ? nl : nlq[idx];
+    const double pq = psiq[idx];
+    double pn;
+    const float pf = point(nl, nlo, pq, psiq_old[idx], inv_c2[idx], pn);
     psiq_old[idx] = pq;
     psiq[idx] = pn;
     nlq[idx] = nl;
-    return (T)pn;
+    psiqf[idx] = pf;
+    return pf;
   }
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
-    const float4 w = ld4g(nlw, idx), d = ld4g(dq, idx);
-    float nl[4] = {w.x - d.x, w.y - d.y, w.z - d.z, w.w - d.w};
+    const float4 w = ld4g(nlw, idx), d = ld4g(dq, idx), ic = ld4g(inv_c2, idx);
+    const float nl[4] = {w.x - d.x, w.y - d.y, w.z - d.z, w.w - d.w};
     float nlo[4] = {nl[0], nl[1], nl[2], nl[3]};
     if (!first) {
       const float4 o = ld4g(nlq, idx);
@@ -333,21 +404,20 @@ template <typename T> struct LdNlUpdate {
     }
     const double2 p01 = ld2dg(psiq, idx), p23 = ld2dg(psiq, idx + 2);
     const double2 o01 = ld2dg(psiq_old, idx), o23 = ld2dg(psiq_old, idx + 2);
-    const double2 c01 = ld2dg(inv_c2, idx), c23 = ld2dg(inv_c2, idx + 2);
-    const double pq[4] = {p01.x, p01.y, p23.x, p23.y}, pqo[4] = {o01.x, o01.y, o23.x, o23.y};
-    const double ic[4] = {c01.x, c01.y, c23.x, c23.y};
     double pn[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const double src = dtd2 * scale * (3.0 * (double)nl[c] - (double)nlo[c]);
-      pn[c] = pq[c] + (0.5 * (pq[c] - pqo[c]) + src) * ic[c];
-    }
+    float pf[4];
+    pf[0] = point(nl[0], nlo[0], p01.x, o01.x, ic.x, pn[0]);
+    pf[1] = point(nl[1], nlo[1], p01.y, o01.y, ic.y, pn[1]);
+    pf[2] = point(nl[2], nlo[2], p23.x, o23.x, ic.z, pn[2]);
+    pf[3] = point(nl[3], nlo[3], p23.y, o23.y, ic.w, pn[3]);
     *reinterpret_cast<double2*>(psiq_old + idx) = p01;
     *reinterpret_cast<double2*>(psiq_old + idx + 2) = p23;
     *reinterpret_cast<double2*>(psiq + idx) = make_double2(pn[0], pn[1]);
     *reinterpret_cast<double2*>(psiq + idx + 2) = make_double2(pn[2], pn[3]);
     st4v(nlq, idx, make_float4(nl[0], nl[1], nl[2], nl[3]));
-    return make_float4((float)pn[0], (float)pn[1], (float)pn[2], (float)pn[3]);
+    const float4 out = make_float4(pf[0], pf[1], pf[2], pf[3]);
+    st4v(psiqf, idx, out);
+    return out;
   }
 };
 
@@ -368,6 +438,9 @@ template <typename T> struct S6Args {
   T *fgrad, *ener, *Sx, *Sy, *Sz, *fx, *fy, *fz, *mu;
   double ep, beta, gamma, zeta, kp, rho0, amp_eq;
   int relax;
+  T* rhof;      // mixed engine: FP32 copy rho - off (read; written in the relax phase); FP64: null
+  double off;
+  T rho0_t, kp_t, zeta_t, ep_t, beta_t, gamma_t, off_t;  // the coefficients in T, converted on the host
 };
 
 // FP32 -> FP64 copy, four elements per thread (n a multiple of 4).
@@ -377,6 +450,18 @@ static __global__ void __launch_bounds__(256) widen_kernel(const float* src, dou
   const float4 v = *reinterpret_cast<const float4*>(src + i);
   *reinterpret_cast<double2*>(dst + i) = make_double2(v.x, v.y);
   *reinterpret_cast<double2*>(dst + i + 2) = make_double2(v.z, v.w);
+}
+
+// Mixed engine: the FP32 copies of the FP64 state, rhof = rho - off and psiqf = psiq,
+// and the FP32 f_rho from its FP64 form (or zero), after swc_set_state / swc_load.
+static __global__ void __launch_bounds__(256) mixed_copies_kernel(long long n, const double* rho, const double* psiq,
+                                                                  const double* frho, double off, float* rhof,
+                                                                  float* psiqf, float* frhot) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    rhof[i] = narrow_f64(rho[i] - off);
+    psiqf[i] = narrow_f64(psiq[i]);
+    frhot[i] = frho ? narrow_f64(frho[i]) : 0.0f;
+  }
 }
 
 // Four consecutive elements of a field (16-byte aligned): float4, or two double2.
@@ -403,45 +488,68 @@ template <typename T> struct V4 {
 };
 
 // Four consecutive points per thread (n^3 is a multiple of 4: every extent is >= 4).
+// The mixed engine takes its FP32 density from rhof + off and touches the FP64 rho
+// only in the relax phase, where it is reset.
 template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S6Args<T> a) {
+  constexpr bool mixed = sizeof(T) == 4;
   const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
   if (idx >= g.ng) return;
   V4<double> r;
+  V4<T> rf;
   V4<T> A, lapR, L, P, gpx, gpy, gpz, grx, gry, grz;
-  r.load(a.rho, idx);
+  if constexpr (mixed) {
+    if (!a.relax) rf.load(a.rhof, idx);
+  } else {
+    r.load(a.rho, idx);
+  }
   A.load(a.amp, idx);
   lapR.load(a.lapR, idx);
   L.load(a.lpsi, idx);
   P.load(a.psi, idx);
   gpx.load(a.gpx, idx); gpy.load(a.gpy, idx); gpz.load(a.gpz, idx);
   grx.load(a.grx, idx); gry.load(a.gry, idx); grz.load(a.grz, idx);
+  const T rho0 = a.rho0_t, kp = a.kp_t, zeta = a.zeta_t, ep = a.ep_t, beta = a.beta_t, gam = a.gamma_t;
+  const T off = a.off_t;
   V4<T> fgrad, ener, Sx, Sy, Sz, fx, fy, fz, mu;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
+    T rr;
     if (a.relax) {
       // REF:1371-1374: rho reset to rho_0 + kp A during the relax phase
       // rho_1 + ((1 - rho_1)/Amp) A with (1 - rho_1)/Amp = kp evaluated once on the host
-      r.v[c] = a.rho0 + a.kp * (double)A.v[c];
-      lapR.v[c] = (T)r.v[c] * lapR.v[c];
+      if constexpr (mixed) {
+        r.v[c] = a.rho0 + a.kp * widen_f32(A.v[c]);
+        rf.v[c] = narrow_f64(r.v[c] - a.off);
+        rr = rf.v[c] + off;
+      } else {
+        r.v[c] = a.rho0 + a.kp * (double)A.v[c];
+        rr = (T)r.v[c];
+      }
+      lapR.v[c] = rr * lapR.v[c];
+    } else {
+      if constexpr (mixed) rr = rf.v[c] + off;
+      else rr = (T)r.v[c];
     }
-    const T rr = (T)r.v[c];
     const T Lc = L.v[c], p = P.v[c], Ac = A.v[c];
     const T E = (T)0.5 * (Lc * Lc);
-    const T t = (T)a.rho0 + (T)a.kp * Ac;
-    fgrad.v[c] = (T)0.5 * (T)a.zeta * (rr * rr - t * t);
+    const T t = rho0 + kp * Ac;
+    fgrad.v[c] = (T)0.5 * zeta * (rr * rr - t * t);
     const T mu1 = lapR.v[c] + rr * Lc;
     Sx.v[c] = mu1 * gpx.v[c] + E * grx.v[c];
     Sy.v[c] = mu1 * gpy.v[c] + E * gry.v[c];
     Sz.v[c] = mu1 * gpz.v[c] + E * grz.v[c];
     const T p2 = p * p;
-    mu.v[c] = lapR.v[c] + rr * (Lc - (T)a.ep * p - (T)a.beta * (p2 * p) + (T)a.gamma * (p2 * p2 * p));
+    mu.v[c] = lapR.v[c] + rr * (Lc - ep * p - beta * (p2 * p) + gam * (p2 * p2 * p));
     ener.v[c] = rr * E;
-    const T cc = (T)a.kp * (T)a.zeta * (rr - (T)a.rho0 - (T)a.kp * Ac) / (Ac + (T)0.001);
+    const T cc = kp * zeta * (rr - rho0 - kp * Ac) / (Ac + (T)0.001);
     fx.v[c] = cc * gpx.v[c];
     fy.v[c] = cc * gpy.v[c];
     fz.v[c] = cc * gpz.v[c];
   }
-  if (a.relax) r.store(a.rho, idx);
+  if (a.relax) {
+    r.store(a.rho, idx);
+    if constexpr (mixed) rf.store(a.rhof, idx);
+  }
   fgrad.store(a.fgrad, idx);
   Sx.store(a.Sx, idx); Sy.store(a.Sy, idx); Sz.store(a.Sz, idx);
   mu.store(a.mu, idx);
@@ -449,17 +557,19 @@ template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S
   fx.store(a.fx, idx); fy.store(a.fy, idx); fz.store(a.fz, idx);
 }
 
-// 1/C2 per spectral mode in FP64 (REF:957-958), built once for the mixed engine.
-static __global__ void __launch_bounds__(256) inv_c2_kernel(Grid g, const double* qx, const double* qy, const double* qz,
+// 1/C2 per spectral mode (REF:957-958), evaluated in FP64 and stored as O, built once
+// for the mixed engine.
+template <typename O>
+__global__ void __launch_bounds__(256) inv_c2_kernel(Grid g, const double* qx, const double* qy, const double* qz,
                                                      double ep, double alpha, double q02, double dt, double rho_m,
-                                                     double* out) {
+                                                     O* out) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.ng) return;
   const int k = (int)(idx & (g.nz - 1)), j = (int)((idx >> g.lz) & (g.ny - 1)), i = (int)(idx >> (g.ly + g.lz));
   const double mq2 = qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k];
   const double s = q02 - mq2;
   const double aLin = ep - alpha * (s * s);
-  out[idx] = 1.0 / (1.5 - dt * rho_m * aLin);
+  out[idx] = (O)(1.0 / (1.5 - dt * rho_m * aLin));
 }
 
 // S8 + S9 (REF:1479-1974): Stokes solve on the three staggered grids, spectral.
@@ -715,7 +825,11 @@ template <typename T> class StepEngine : public EngineBase {
   T *fgrad_ = nullptr, *ener_ = nullptr, *S_[3] = {}, *f_[3] = {}, *vsol_[3] = {}, *virr_[3] = {};
   T *divv_ = nullptr, *dq_ = nullptr, *v_[3] = {}, *vsolr_[3] = {}, *energy_ = nullptr, *nlw_ = nullptr;
   double *partial_ = nullptr, *dsum_ = nullptr;
-  double* inv_c2_ = nullptr;  // mixed engine: FP64 1/C2 per spectral mode
+  // mixed engine: FP32 1/C2 per spectral mode, FP32 f_rho, and FP32 copies of the FP64
+  // state kept where the state is written: rhof = rho - rho_off_, psiqf = psiq
+  T *inv_c2f_ = nullptr, *frhot_ = nullptr, *rhof_ = nullptr, *psiqf_ = nullptr;
+  double rho_off_ = 0;  // (rho_0 + rho_s)/2 in the mixed engine, 0 in the FP64 engine
+  int refresh_copies(bool have_frho);
   int diag_blocks_ = 0;
   std::map<int, cudaGraphExec_t> graphs_;
   std::map<int, int64_t> graph_kernels_;  // kernel nodes per captured variant
@@ -760,6 +874,7 @@ template <typename T> int StepEngine<T>::init() {
   kp_ = (1 - p_.rho_0) / amp_;
   rho_s_ = kp_ * amp_ + p_.rho_0;
   rho_m_ = rho_s_ / 2;
+  rho_off_ = std::is_same<T, double>::value ? 0.0 : 0.5 * (p_.rho_0 + rho_s_);
   const double pi = 3.14159265358979323846;
   const int dims[3] = {p_.nx, p_.ny, p_.nz};
   double d[3];
@@ -847,9 +962,13 @@ template <typename T> int StepEngine<T>::init() {
   for (double** b : dbufs) SWC_CK(cudaMemsetAsync(*b, 0, nd, stream_));
   SWC_CK(cudaStreamSynchronize(stream_));
   if constexpr (!std::is_same<T, double>::value) {
-    if ((rc = dalloc(nd, (void**)&inv_c2_))) return rc;
-    inv_c2_kernel<<<(unsigned)((g_.ng + 255) / 256), 256, 0, stream_>>>(
-        g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt, rho_m_, inv_c2_);
+    T** mbufs[] = {&inv_c2f_, &frhot_, &rhof_, &psiqf_};
+    for (T** b : mbufs) {
+      if ((rc = dalloc(nt, (void**)b))) return rc;
+      SWC_CK(cudaMemsetAsync(*b, 0, nt, stream_));
+    }
+    inv_c2_kernel<T><<<(unsigned)((g_.ng + 255) / 256), 256, 0, stream_>>>(
+        g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt, rho_m_, inv_c2f_);
     SWC_CK(cudaGetLastError());
     SWC_CK(cudaStreamSynchronize(stream_));
   }
@@ -898,15 +1017,20 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
   // for f = psi (REF:1190-1219) and f = rho (REF:1191-1219, where -scale Vs rhoq gives
   // the same 1/(2 n_a)). The mixed engine transforms rho - (rho_0 + rho_s)/2: the
   // gradients never read mode 0, and FP32 then resolves the small variations.
-  const double rho_off = std::is_same<T, double>::value ? 0.0 : 0.5 * (p_.rho_0 + rho_s_);
   {
     const T cx = (T)(1.0 / (2.0 * g_.nx)), cy = (T)(1.0 / (2.0 * g_.ny)), cz = (T)(1.0 / (2.0 * g_.nz));
     SWC_TRY((pass<K_DERIV, 2>(LP{psi_}, SP{gp_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
     SWC_TRY((pass<K_DERIV, 1>(LP{psi_}, SP{gp_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
     SWC_TRY((pass<K_DERIV, 0>(LP{psi_}, SP{gp_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
-    SWC_TRY((pass<K_DERIV, 2>(LdOffset<T>{rho_, rho_off}, SP{gr_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
-    SWC_TRY((pass<K_DERIV, 1>(LdOffset<T>{rho_, rho_off}, SP{gr_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
-    SWC_TRY((pass<K_DERIV, 0>(LdOffset<T>{rho_, rho_off}, SP{gr_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
+    if constexpr (std::is_same<T, double>::value) {
+      SWC_TRY((pass<K_DERIV, 2>(LdOffset<T>{rho_, 0.0}, SP{gr_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
+      SWC_TRY((pass<K_DERIV, 1>(LdOffset<T>{rho_, 0.0}, SP{gr_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
+      SWC_TRY((pass<K_DERIV, 0>(LdOffset<T>{rho_, 0.0}, SP{gr_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
+    } else {  // the FP32 copy rho - rho_off_, kept by the density update
+      SWC_TRY((pass<K_DERIV, 2>(LP{rhof_}, SP{gr_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
+      SWC_TRY((pass<K_DERIV, 1>(LP{rhof_}, SP{gr_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
+      SWC_TRY((pass<K_DERIV, 0>(LP{rhof_}, SP{gr_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
+    }
   }
   // S3 (REF:1254-1289): amplitude, Gaussian filter
   SWC_TRY((pass<K_C2, 2>(LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
@@ -916,18 +1040,27 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
   SWC_TRY((pass<K_C3, 2>(LP{amp_f_}, SP{amp_f_})));
   // S4 (REF:1293-1308): dfDlapPsi
   const T alpha = (T)p_.alpha, q02 = (T)(p_.q0 * p_.q0);
-  SWC_TRY((pass<K_C3, 2>(LdLpsi<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
+  if constexpr (std::is_same<T, double>::value)
+    SWC_TRY((pass<K_C3, 2>(LdLpsi<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
+  else
+    SWC_TRY((pass<K_C3, 2>(LdLpsi<T, T>{psiqf_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
   SWC_TRY((pass<K_C3, 1>(LP{lpsi_}, SP{lpsi_})));
   SWC_TRY((pass<K_C3, 0>(LP{lpsi_}, SP{lpsi_})));
   // S5 (REF:1312-1380)
   if (!relax) {
-    SWC_TRY((pass<K_C2, 2>(LdRhoL<T>{rho_, lpsi_}, SP{lapR_})));
+    if constexpr (std::is_same<T, double>::value)
+      SWC_TRY((pass<K_C2, 2>(LdRhoL<T>{rho_, lpsi_, (T)0}, SP{lapR_})));
+    else
+      SWC_TRY((pass<K_C2, 2>(LdRhoL<T, T>{rhof_, lpsi_, (T)rho_off_}, SP{lapR_})));
     SWC_TRY((pass<K_C2, 1>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_FILT, 0>(LP{lapR_}, SP{lapR_}, MulLap<T>{vq_[0], vq_[1], vq_[2], (T)scale_})));
     SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 2>(LP{lapR_}, SP{lapR_})));
   } else {
-    SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
+    if constexpr (std::is_same<T, double>::value)
+      SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
+    else
+      SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T, T>{psiqf_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 0>(LP{lapR_}, SP{lapR_})));
   }
@@ -973,6 +1106,18 @@ struct StScaleD {
   __device__ __forceinline__ void operator()(int, int, int, long long idx, double v) const { p[idx] = s * v; }
 };
 
+// Mixed engine: rebuild the FP32 copies of the FP64 state (and f_rho from its FP64
+// form after swc_load, zero after swc_set_state). No-op for the FP64 engine.
+template <typename T> int StepEngine<T>::refresh_copies(bool have_frho) {
+  if constexpr (!std::is_same<T, double>::value) {
+    mixed_copies_kernel<<<1024, 256, 0, stream_>>>(g_.ng, rho_, psiq_, have_frho ? frho_ : nullptr, rho_off_, rhof_,
+                                                  psiqf_, frhot_);
+    SWC_CK(cudaGetLastError());
+  }
+  (void)have_frho;
+  return SWC_OK;
+}
+
 template <typename T> int StepEngine<T>::set_state(const double* psi, const double* rho) {
   SWC_CK(cudaSetDevice(p_.device));
   const size_t nd = (size_t)g_.ng * sizeof(double), nt = (size_t)g_.ng * sizeof(T);
@@ -994,6 +1139,7 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   SWC_TRY((pass<K_C3, 1>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
   SWC_TRY((pass<K_C3, 0>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, nt, cudaMemcpyDeviceToDevice, stream_));  // REF:1010
+  SWC_TRY(refresh_copies(false));
   if (p_.adjoint_ckpt > 0) SWC_TRY(save_ckpt(0));
   adj_valid_ = p_.adjoint_ckpt > 0;
   SWC_CK(cudaStreamSynchronize(stream_));
@@ -1124,7 +1270,15 @@ template <typename T> int StepEngine<T>::field_src(int field, const void** src, 
     case SWC_F_PSIQ: *src = psiq_; *is_double = true; break;
     case SWC_F_PSIQ_OLD: *src = psiq_old_; *is_double = true; break;
     case SWC_F_NLQ: *src = nlq_; break;
-    case SWC_F_FRHO: *src = frho_; *is_double = true; break;
+    case SWC_F_FRHO:  // the mixed engine keeps f_rho (an FP32 source term) in FP32
+      if constexpr (std::is_same<T, double>::value) {
+        *src = frho_;
+        *is_double = true;
+      } else {
+        *src = frhot_;
+        *is_double = false;
+      }
+      break;
     case SWC_F_LPSI: *src = lpsi_; break;
     case SWC_F_MU: *src = mu_; break;
     case SWC_F_GPSIX: *src = gp_[0]; break;
@@ -1205,6 +1359,11 @@ template <typename T> int StepEngine<T>::save(const char* path) {
   h.elem = (int)sizeof(T); h.nloop = nloop_;
   bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
   const size_t n = (size_t)g_.ng;
+  if constexpr (!std::is_same<T, double>::value) {  // the file holds f_rho in FP64 for both engines
+    widen_kernel<<<(unsigned)((n / 4 + 255) / 256), 256, 0, stream_>>>(frhot_, frho_, (long long)n);
+    SWC_CK(cudaGetLastError());
+    SWC_CK(cudaStreamSynchronize(stream_));
+  }
   std::vector<char> buf(n * sizeof(double));
   const void* dsrc[] = {psiq_, psiq_old_, rho_, frho_};
   for (const void* s : dsrc) {
@@ -1268,6 +1427,7 @@ template <typename T> int StepEngine<T>::load(const char* path) {
     return SWC_ERR_IO;
   }
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, n * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  SWC_TRY(refresh_copies(true));
   SWC_CK(cudaStreamSynchronize(stream_));
   adj_valid_ = false;  // the checkpoints no longer describe this trajectory
   nloop_ = h.nloop;

@@ -15,7 +15,8 @@ template <typename T> int StepEngine<T>::enqueue_part_b(bool relax, bool first, 
   {
     S6Args<T> a{lapR_, lpsi_, psi_, amp_f_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2], rho_,
                 fgrad_, ener_, S_[0], S_[1], S_[2], f_[0], f_[1], f_[2], mu_,
-                p_.ep, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, amp_, relax ? 1 : 0};
+                p_.ep, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, amp_, relax ? 1 : 0, rhof_, rho_off_,
+                (T)p_.rho_0, (T)kp_, (T)p_.zeta, (T)p_.ep, (T)p_.beta, (T)p_.gamma, (T)rho_off_};
     s6_kernel<T><<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
     ++launches_;

@@ -31,23 +31,26 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
   }
   // S12 + S13 + S14 (REF:2121-2197): rho update, Nl, its DCT, the psiq update, psi = iDCT(psiq_new)
   T* pout = diag ? psi_new_ : psi_;
-  {
+  if constexpr (std::is_same<T, double>::value) {
+    // FP64 engine: the reference's expressions; the CN update in the Nl transform's last pass
     LdNl<T> ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
                rho_, frho_, p_.dt, kp_, p_.zeta, p_.rho_0};
     SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
     SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
-    if constexpr (std::is_same<T, double>::value) {
-      // FP64 engine: the reference's CN expression in the Nl transform's last pass
-      StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], inv_c2_, p_.ep, p_.alpha,
-                       p_.q0 * p_.q0, p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, 0};
-      SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
-      SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
-    } else {
-      // mixed engine: the increment-form update fused into the psi transform's first pass
-      SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
-      LdNlUpdate<T> lu{nlw_, dq_, nlq_, psiq_, psiq_old_, inv_c2_, p_.dt / 2, scale_, first ? 1 : 0};
-      SWC_TRY((pass<K_C3, 2>(lu, SP{pout})));
-    }
+    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], nullptr, p_.ep, p_.alpha,
+                     p_.q0 * p_.q0, p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, 0};
+    SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
+    SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
+  } else {
+    // mixed engine: FP64-lean density update, the CN update fused into the psi transform
+    LdNlMixed ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
+                 rho_, frhot_, rhof_, rho_off_, (float)p_.dt, (float)kp_, (float)p_.zeta, (float)p_.rho_0,
+                 (float)rho_off_};
+    SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
+    SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
+    SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
+    LdNlUpdate lu{nlw_, dq_, nlq_, psiq_, psiq_old_, inv_c2f_, psiqf_, (float)(p_.dt / 2 * scale_), first ? 1 : 0};
+    SWC_TRY((pass<K_C3, 2>(lu, SP{pout})));
   }
   SWC_TRY((pass<K_C3, 1>(LP{pout}, SP{pout})));
   SWC_TRY((pass<K_C3, 0>(LP{pout}, SP{pout})));
