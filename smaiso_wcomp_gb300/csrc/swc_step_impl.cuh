@@ -467,6 +467,11 @@ static __global__ void __launch_bounds__(256) mixed_copies_kernel(long long n, c
 // Four consecutive elements of a field (16-byte aligned): float4, or two double2.
 template <typename T> struct V4 {
   T v[4];
+  __device__ __forceinline__ static V4 zero() {
+    V4 r;
+    r.v[0] = r.v[1] = r.v[2] = r.v[3] = (T)0;
+    return r;
+  }
   __device__ __forceinline__ void load(const T* p, long long idx) {
     if constexpr (sizeof(T) == 4) {
       const float4 q = *reinterpret_cast<const float4*>(p + idx);
@@ -582,67 +587,121 @@ template <typename T> struct StokesArgs {
   int block;  // x-slab size of the reference decomposition (REF:299)
 };
 
+// Four consecutive points along z per thread, with 32-bit indices (n^3 <= 2^30). The
+// staggered neighbours at k-1 / k+1 come from the aligned 4-vector of the neighbouring
+// row plus one scalar at its edge; every per-point expression is the one-point form.
 template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid g, StokesArgs<T> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.ng) return;
-  int i, j, k;
-  decompose(g, idx, i, j, k);
-  const long long sx = 1LL << (g.ly + g.lz), sy = g.nz;
-  const T Sxc = a.Sx[idx], Syc = a.Sy[idx], Szc = a.Sz[idx];
-  const T qxi = a.vqx[i], qyj = a.vqy[j], qzk = a.vqz[k];
+  const int idx = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (idx >= (int)g.ng) return;
+  const int k0 = idx & (g.nz - 1), j = (idx >> g.lz) & (g.ny - 1), i = idx >> (g.ly + g.lz);
+  const int sx = 1 << (g.ly + g.lz), sy = g.nz;
+  const bool has_next = k0 + 4 < g.nz;  // k0 + 4 is in this row
+  V4<T> Sxc, Syc, Szc, qz, szv, gqz, gsz;
+  Sxc.load(a.Sx, idx);
+  Syc.load(a.Sy, idx);
+  Szc.load(a.Sz, idx);
+  qz.load(a.vqz, k0);
+  szv.load(a.vsz, k0);
+  gqz.load(a.gqz, k0);
+  gsz.load(a.gsz, k0);
+  const T qxi = a.vqx[i], qyj = a.vqy[j];
   // v_x on the x-sine grid, i < nx-1 (REF:1581-1699)
-  T vs = 0, vi = 0;
+  V4<T> vs, vi;
   if (i < g.nx - 1) {
     const T sxi = a.vsx[i];
-    const T Sy = (j != 0) ? a.Sy[idx + sx - sy] : (T)0;
-    const T Sz = (k != 0) ? a.Sz[idx + sx - 1] : (T)0;
-    const T dot = sxi * Sxc + qyj * Sy + qzk * Sz;
-    const T mq2 = sxi * sxi + qyj * qyj + qzk * qzk;
-    const T inv = (T)1 / mq2;
-    const T CM1 = a.scale * inv, CM2 = sxi * inv;
-    const long long n1 = idx + sx;
-    const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i + 1] * a.gqy[j] * a.gqz[k]);
-    vs = (CM1 * a.inv_nu) * (Sxc - CM2 * dot);
-    vi = (CM1 * a.inv_lam2nu) * (sxi * fg + CM2 * dot * (a.gsx[i] * a.gqy[j] * a.gqz[k]));
+    V4<T> Sy1, Szn, F1, E1;
+    if (j != 0) Sy1.load(a.Sy, idx + sx - sy);
+    else Sy1 = V4<T>::zero();
+    Szn.load(a.Sz, idx + sx);
+    const T Szp = (k0 != 0) ? a.Sz[idx + sx - 1] : (T)0;
+    F1.load(a.fgrad, idx + sx);
+    E1.load(a.ener, idx + sx);
+    const T Gx = a.gqx[i + 1] * a.gqy[j], Gsx = a.gsx[i] * a.gqy[j];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const T Sz = (c == 0) ? Szp : Szn.v[c - 1];
+      const T dot = sxi * Sxc.v[c] + qyj * Sy1.v[c] + qz.v[c] * Sz;
+      const T mq2 = sxi * sxi + qyj * qyj + qz.v[c] * qz.v[c];
+      const T inv = (T)1 / mq2;
+      const T CM1 = a.scale * inv, CM2 = sxi * inv;
+      const T fg = F1.v[c] + E1.v[c] * (Gx * gqz.v[c]);
+      vs.v[c] = (CM1 * a.inv_nu) * (Sxc.v[c] - CM2 * dot);
+      vi.v[c] = (CM1 * a.inv_lam2nu) * (sxi * fg + CM2 * dot * (Gsx * gqz.v[c]));
+    }
+  } else {
+    vs = V4<T>::zero();
+    vi = V4<T>::zero();
   }
-  a.vsolx[idx] = vs;
-  a.virrx[idx] = vi;
+  vs.store(a.vsolx, idx);
+  vi.store(a.virrx, idx);
   // v_y, v_z for j < ny-1, k < nz-1 (REF:1758-1974); other modes stay 0
-  T ys = 0, yi = 0, zs = 0, zi = 0;
-  if (j < g.ny - 1 && k < g.nz - 1) {
-    const T syj = a.vsy[j], szk = a.vsz[k];
-    {
-      const T Sx = (i > 0) ? a.Sx[idx - sx + sy] : (T)0;
-      const T Sz = (k != 0) ? a.Sz[idx + sy - 1] : (T)0;
-      const T dot = qxi * Sx + syj * Syc + qzk * Sz;
-      const T mq2 = qxi * qxi + syj * syj + qzk * qzk;
-      const T inv = (T)1 / mq2;
-      const T CM1 = a.scale * inv, CM2 = syj * inv;
-      const long long n1 = idx + sy;
-      const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i] * a.gqy[j + 1] * a.gqz[k]);
-      ys = (CM1 * a.inv_nu) * (Syc - CM2 * dot);
-      yi = (CM1 * a.inv_lam2nu) * (syj * fg + CM2 * dot * (a.gqx[i] * a.gsy[j] * a.gqz[k]));
+  V4<T> ys = V4<T>::zero(), yi = V4<T>::zero(), zs = V4<T>::zero(), zi = V4<T>::zero();
+  if (j < g.ny - 1) {
+    const T syj = a.vsy[j];
+    V4<T> Sx2, Szn2, F2, E2, Sxm, Sym, F3, E3;
+    if (i > 0) Sx2.load(a.Sx, idx - sx + sy);
+    else Sx2 = V4<T>::zero();
+    Szn2.load(a.Sz, idx + sy);
+    const T Szp2 = (k0 != 0) ? a.Sz[idx + sy - 1] : (T)0;
+    F2.load(a.fgrad, idx + sy);
+    E2.load(a.ener, idx + sy);
+    // z: Sx[idx - sx + 1], Sy[idx - sy + 1], fgrad/ener[idx + 1] (k + 1 in the same row)
+    T Sxn = (T)0, Syn = (T)0;
+    if (i > 0) {
+      Sxm.load(a.Sx, idx - sx);
+      if (has_next) Sxn = a.Sx[idx - sx + 4];
+    } else {
+      Sxm = V4<T>::zero();
     }
-    {
-      const T Sx = (i > 0) ? a.Sx[idx - sx + 1] : (T)0;
-      const T Sy = (j != 0) ? a.Sy[idx - sy + 1] : (T)0;
-      const T dot = qxi * Sx + qyj * Sy + szk * Szc;
-      const T mq2 = qxi * qxi + qyj * qyj + szk * szk;
-      const T inv = (T)1 / mq2;
-      const T CM1 = a.scale * inv, CM2 = szk * inv;
-      const long long n1 = idx + 1;
-      const T fg = a.fgrad[n1] + a.ener[n1] * (a.gqx[i] * a.gqy[j] * a.gqz[k + 1]);
-      // REF:1932: off the first slab of a rank, the k = 0, j > 0 modes use CM1y's filter
-      const bool q1 = (k == 0) && (j > 0) && (i % a.block != 0);
-      const T G = q1 ? (a.gqx[i] * a.gsy[j] * a.gqz[k]) : (a.gqx[i] * a.gqy[j] * a.gsz[k]);
-      zs = (CM1 * a.inv_nu) * (Szc - CM2 * dot);
-      zi = (CM1 * a.inv_lam2nu) * (szk * fg + CM2 * dot * G);
+    if (j != 0) {
+      Sym.load(a.Sy, idx - sy);
+      if (has_next) Syn = a.Sy[idx - sy + 4];
+    } else {
+      Sym = V4<T>::zero();
+    }
+    const T Fn = has_next ? a.fgrad[idx + 4] : (T)0, En = has_next ? a.ener[idx + 4] : (T)0;
+    F3.load(a.fgrad, idx);
+    E3.load(a.ener, idx);
+    const T Gy = a.gqx[i] * a.gqy[j + 1], Gsy = a.gqx[i] * a.gsy[j], Gz = a.gqx[i] * a.gqy[j];
+    const bool off_first_slab = (i % a.block) != 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int k = k0 + c;
+      if (k < g.nz - 1) {
+        const T szk = szv.v[c];
+        {
+          const T Sz = (c == 0) ? Szp2 : Szn2.v[c - 1];
+          const T dot = qxi * Sx2.v[c] + syj * Syc.v[c] + qz.v[c] * Sz;
+          const T mq2 = qxi * qxi + syj * syj + qz.v[c] * qz.v[c];
+          const T inv = (T)1 / mq2;
+          const T CM1 = a.scale * inv, CM2 = syj * inv;
+          const T fg = F2.v[c] + E2.v[c] * (Gy * gqz.v[c]);
+          ys.v[c] = (CM1 * a.inv_nu) * (Syc.v[c] - CM2 * dot);
+          yi.v[c] = (CM1 * a.inv_lam2nu) * (syj * fg + CM2 * dot * (Gsy * gqz.v[c]));
+        }
+        {
+          const T Sx = (c < 3) ? Sxm.v[c + 1] : Sxn;
+          const T Sy = (c < 3) ? Sym.v[c + 1] : Syn;
+          const T dot = qxi * Sx + qyj * Sy + szk * Szc.v[c];
+          const T mq2 = qxi * qxi + qyj * qyj + szk * szk;
+          const T inv = (T)1 / mq2;
+          const T CM1 = a.scale * inv, CM2 = szk * inv;
+          const T f1 = (c < 3) ? F3.v[c + 1] : Fn, e1 = (c < 3) ? E3.v[c + 1] : En;
+          const T gz1 = (c < 3) ? gqz.v[c + 1] : a.gqz[k + 1];
+          const T fg = f1 + e1 * (Gz * gz1);
+          // REF:1932: off the first slab of a rank, the k = 0, j > 0 modes use CM1y's filter
+          const bool q1 = (k == 0) && (j > 0) && off_first_slab;
+          const T G = q1 ? (Gsy * gqz.v[c]) : (Gz * gsz.v[c]);
+          zs.v[c] = (CM1 * a.inv_nu) * (Szc.v[c] - CM2 * dot);
+          zi.v[c] = (CM1 * a.inv_lam2nu) * (szk * fg + CM2 * dot * G);
+        }
+      }
     }
   }
-  a.vsoly[idx] = ys;
-  a.virry[idx] = yi;
-  a.vsolz[idx] = zs;
-  a.virrz[idx] = zi;
+  ys.store(a.vsoly, idx);
+  yi.store(a.virry, idx);
+  zs.store(a.vsolz, idx);
+  zi.store(a.virrz, idx);
 }
 
 // S10 (REF:2042-2079): div v and q.f on the cosine grid (q.f without `scale`).

@@ -45,7 +45,7 @@ template <typename T> int StepEngine<T>::enqueue_part_b(bool relax, bool first, 
                     virr_[2], vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2], gq_[0], gq_[1], gq_[2], gs_[0],
                     gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu), (T)(1.0 / (p_.lambda + 2 * p_.nu)),
                     p_.nx / p_.ref_ranks};
-    stokes_kernel<T><<<pw_blocks, 256, 0, stream_>>>(g_, a);
+    stokes_kernel<T><<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
     ++launches_;
   }
