@@ -372,7 +372,7 @@ def main():
     fp64_flops = (2.5 * np.log2(N) + 8.0) * N ** 3
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "traffic": PASS_TRAFFIC.get("fp32"),
-                "kernel": "r2r_fast_kernel<float, 256> (one DCT-II axis pass, 256^3, steady state of 8 fields, mean of z/y/x)",
+                "kernel": "r2r_tma_kernel<256, C2> (one FP32 DCT-II axis pass, 256^3, steady state of 8 fields, mean of z/y/x)",
                 "pass_ms_zyx": axes_ms, "alg_bytes_per_launch": alg,
                 "peak_source": f"{peak_kind} hbm_gbs"}
     line = {
@@ -410,9 +410,10 @@ def main():
         pg.destroy_process_group()
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, mean of its x/z/y passes,
-# from the committed ncu capture profiles/r2r_pass_fp32_n256_256cubed.md.
-PASS_TRAFFIC = {"fp32": 74.3e6}
+# DRAM bytes (read + write) per launch of the dominant kernel in the steady state that
+# pass_roofline times (mean of its z/y/x passes), from the ncu capture with
+# --cache-control none summarised in profiles/r2r_tma_fp32_n256_256cubed.md.
+PASS_TRAFFIC = {"fp32": 133.0e6}
 
 
 def working_set_gb():

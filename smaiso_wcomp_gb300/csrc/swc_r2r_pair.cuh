@@ -186,6 +186,16 @@ template <int AX, class MUL> __device__ __forceinline__ float2 mul_ab(const MUL&
   if constexpr (AX != 2) return make_float2(mul(i, j, k), mul(i, j, k + 1));
   else return make_float2(mul(i, j, k), mul(i, j + 1, k));
 }
+// elements k, k+1 of one z line (the pair form stores idx, idx + 1)
+template <class ST>
+__device__ __forceinline__ void st_z2(const ST& st, int i, int j, int k, long long idx, float2 v) {
+  if constexpr (HasStPair<ST>::value) {
+    st.pair(i, j, k, idx, v);
+  } else {
+    st(i, j, k, idx, v.x);
+    st(i, j, k + 1, idx + 1, v.y);
+  }
+}
 // elements k .. k+3 of one z line
 template <class LD> __device__ __forceinline__ float4 ld_q(const LD& ld, int i, int j, int k, long long idx) {
   if constexpr (HasLdQuad<LD>::value) return ld.quad(i, j, k, idx);
@@ -494,16 +504,17 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
     pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
   }
 
-  // ---------------- z store (float4 per line) ----------------
+  // ---------------- z store ----------------
+  if constexpr (inv_out) {
+    // Makhoul order, float4 per line: x_4a = slot a .im, x_4a+1 = slot M-1-a .re,
+    // x_4a+2 = slot a .re, x_4a+3 = slot M-1-a .im (rows a, M-1-a: odd pitch, no conflicts)
 #pragma unroll 1
-  for (int c0 = 0; c0 < ZU; c0 += ZC) {
-    float4 oa[ZC], ob[ZC];
+    for (int c0 = 0; c0 < ZU; c0 += ZC) {
+      float4 oa[ZC], ob[ZC];
 #pragma unroll
-    for (int c = 0; c < ZC; ++c) {
-      const int u = tid + (c0 + c) * NT;
-      const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
-      if constexpr (inv_out) {
-        // x_4a = slot a .im, x_4a+1 = slot M-1-a .re, x_4a+2 = slot a .re, x_4a+3 = slot M-1-a .im
+      for (int c = 0; c < ZC; ++c) {
+        const int u = tid + (c0 + c) * NT;
+        const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
         const PC sa = buf[a * PP + q], sb = buf[(M - 1 - a) * PP + q];
         oa[c] = make_float4(sa.im.x, sb.re.x, sa.re.x, sb.im.x);
         ob[c] = make_float4(sa.im.y, sb.re.y, sa.re.y, sb.im.y);
@@ -511,22 +522,34 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
           oa[c].y = -oa[c].y; oa[c].w = -oa[c].w;
           ob[c].y = -ob[c].y; ob[c].w = -ob[c].w;
         }
-      } else {
-        // natural order: slot 2a = (y_4a, y_4a+1), slot 2a+1 = (y_4a+2, y_4a+3)
-        const PC s0 = buf[(2 * a) * PP + q], s1 = buf[(2 * a + 1) * PP + q];
-        oa[c] = make_float4(s0.re.x, s0.im.x, s1.re.x, s1.im.x);
-        ob[c] = make_float4(s0.re.y, s0.im.y, s1.re.y, s1.im.y);
+      }
+#pragma unroll
+      for (int c = 0; c < ZC; ++c) {
+        const int u = tid + (c0 + c) * NT;
+        const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+        const int la = 2 * (pair0 + q);
+        const int i = la >> g.ly, j = la & (g.ny - 1);
+        const long long idx = (long long)(la * N + 4 * a);
+        st_q(st, i, j, 4 * a, idx, oa[c]);
+        st_q(st, i, j + 1, 4 * a, idx + N, ob[c]);
       }
     }
-#pragma unroll
-    for (int c = 0; c < ZC; ++c) {
-      const int u = tid + (c0 + c) * NT;
-      const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+  } else {
+    // natural order, one slot (y_2s, y_2s+1) per unit and float2 per line: consecutive
+    // lanes read consecutive rows of the odd pitch (no bank conflicts)
+    constexpr int SU = (LP * M) / NT;
+    constexpr int LOG2M = (M == 32) ? 5 : (M == 64) ? 6 : (M == 128) ? 7 : 8;
+    static_assert((1 << LOG2M) == M && SU * NT == LP * M, "z slot units");
+#pragma unroll 4
+    for (int c = 0; c < SU; ++c) {
+      const int u = tid + c * NT;
+      const int sl = u & (M - 1), q = u >> LOG2M;
+      const PC v = buf[sl * PP + q];
       const int la = 2 * (pair0 + q);
       const int i = la >> g.ly, j = la & (g.ny - 1);
-      const long long idx = (long long)(la * N + 4 * a);
-      st_q(st, i, j, 4 * a, idx, oa[c]);
-      st_q(st, i, j + 1, 4 * a, idx + N, ob[c]);
+      const long long idx = (long long)(la * N + 2 * sl);
+      st_z2(st, i, j, 2 * sl, idx, make_float2(v.re.x, v.im.x));
+      st_z2(st, i, j + 1, 2 * sl, idx + N, make_float2(v.re.y, v.im.y));
     }
   }
 }

@@ -190,26 +190,40 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
       }
       if (tj == 0) buf[(M / 2) * PP + lp] = pswap(zmid);
     } else {
-      // z: the tile is its 2 LP lines one after another; four elements per float4
-      const float4* S4 = reinterpret_cast<const float4*>(S);
+      if constexpr (fwd_in) {
+        // z: the tile is its 2 LP lines one after another; four elements per float4
+        const float4* S4 = reinterpret_cast<const float4*>(S);
 #pragma unroll 4
-      for (int c = 0; c < ZU; ++c) {
-        const int u = tid + c * NT;
-        const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
-        float4 A = S4[(2 * q) * NQ + a], B = S4[(2 * q + 1) * NQ + a];
-        if constexpr (fwd_in) {
+        for (int c = 0; c < ZU; ++c) {
+          const int u = tid + c * NT;
+          const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
+          float4 A = S4[(2 * q) * NQ + a], B = S4[(2 * q + 1) * NQ + a];
           if constexpr (KIND == K_S2) {
             A.y = -A.y; A.w = -A.w;
             B.y = -B.y; B.w = -B.w;
           }
           buf[a * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.z, B.z));
           buf[(M - 1 - a) * PP + q] = pmake(make_float2(A.w, B.w), make_float2(A.y, B.y));
-        } else if constexpr (KIND == K_S3) {
-          buf[(M - 2 * a - 2) * PP + q] = pmake(make_float2(A.w, B.w), make_float2(A.z, B.z));
-          buf[(M - 2 * a - 1) * PP + q] = pmake(make_float2(A.y, B.y), make_float2(A.x, B.x));
-        } else {
-          buf[(2 * a) * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.y, B.y));
-          buf[(2 * a + 1) * PP + q] = pmake(make_float2(A.z, B.z), make_float2(A.w, B.w));
+        }
+      } else {
+        // inverse kinds: one slot (two reals) per unit, consecutive lanes on consecutive
+        // rows of the odd pitch; DST-III reads the line reversed
+        const float2* S2 = reinterpret_cast<const float2*>(S);
+        constexpr int SU = (LP * M) / NT;
+        constexpr int LOG2M = (M == 32) ? 5 : (M == 64) ? 6 : (M == 128) ? 7 : 8;
+        static_assert((1 << LOG2M) == M && SU * NT == LP * M, "z slot units");
+#pragma unroll 4
+        for (int c = 0; c < SU; ++c) {
+          const int u = tid + c * NT;
+          const int sl = u & (M - 1), q = u >> LOG2M;
+          if constexpr (KIND == K_S3) {
+            // slot s = (X_2s, X_2s+1) = (x_{N-1-2s}, x_{N-2-2s}) = swapped float2 M-1-s
+            const float2 A = S2[(2 * q) * M + (M - 1 - sl)], B = S2[(2 * q + 1) * M + (M - 1 - sl)];
+            buf[sl * PP + q] = pmake(make_float2(A.y, B.y), make_float2(A.x, B.x));
+          } else {
+            const float2 A = S2[(2 * q) * M + sl], B = S2[(2 * q + 1) * M + sl];
+            buf[sl * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.y, B.y));
+          }
         }
       }
     }
