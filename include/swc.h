@@ -283,6 +283,13 @@ int swc_r2r_execute_axis(swc_r2r_plan* plan, int axis, void* dev_inout, void* st
  * data is double on the host for both precisions. */
 int swc_r2r_execute_host(swc_r2r_plan* plan, const double* in, double* out);
 
+/* Test support for the bounded waits of the FP32 TMA-fed passes (no counterpart in the
+ * reference): every tile wait of this plan expects extra_tx_bytes (0..65536) more bytes
+ * than its copy delivers, so it runs out after max_polls (1..2^22) mbarrier polls; the
+ * CTA then sets the plan's status flag and returns, and the next swc_r2r_execute_host
+ * reports SWC_ERR_CUDA. (0, 1 << 22) restores normal operation. */
+int swc_r2r_plan_set_wait_test(swc_r2r_plan* plan, int extra_tx_bytes, int max_polls);
+
 #ifdef __cplusplus
 }
 #endif

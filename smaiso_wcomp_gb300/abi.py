@@ -41,7 +41,7 @@ EXPORTS = [
     "swc_get_field", "swc_field_device_ptr", "swc_get_step", "swc_last_step_ms",
     "swc_last_step_launches", "swc_device_fma_peak", "swc_diagnostics_noalloc",
     "swc_backward", "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
-    "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host",
+    "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host", "swc_r2r_plan_set_wait_test",
 ]
 
 
@@ -152,6 +152,7 @@ def load_library(path=None):
         "swc_r2r_execute": (ctypes.c_int, [vp, vp, vp]),
         "swc_r2r_execute_axis": (ctypes.c_int, [vp, ctypes.c_int, vp, vp]),
         "swc_r2r_execute_host": (ctypes.c_int, [vp, dp, dp]),
+        "swc_r2r_plan_set_wait_test": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

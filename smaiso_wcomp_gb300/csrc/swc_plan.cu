@@ -178,6 +178,18 @@ int swc_r2r_execute_axis(swc_r2r_plan* p, int axis, void* dev_inout, void* strea
   return SWC_OK;
 }
 
+int swc_r2r_plan_set_wait_test(swc_r2r_plan* p, int extra_tx_bytes, int max_polls) {
+  if (!p || extra_tx_bytes < 0 || extra_tx_bytes > 65536 || max_polls < 1 || max_polls > (1 << 22)) {
+    set_error("bad plan or wait-test arguments");
+    return SWC_ERR_BAD_PARAM;
+  }
+  for (int a = 0; a < 3; ++a) {
+    p->tf[a].wait_extra_tx = p->td[a].wait_extra_tx = extra_tx_bytes;
+    p->tf[a].max_polls = p->td[a].max_polls = max_polls;
+  }
+  return SWC_OK;
+}
+
 int swc_r2r_execute_host(swc_r2r_plan* p, const double* in, double* out) {
   if (!p || !in || !out) { set_error("NULL argument"); return SWC_ERR_BAD_PARAM; }
   const size_t n = (size_t)p->g.ng;

@@ -29,6 +29,8 @@ template <typename T> struct R2RTables {
   const cx_t<T>* post;  // DCT-II post-twiddles: post[2k] = c_k, post[2k+1] = d_k, k = 0..M
   const cx_t<T>* pre;   // DCT-III pre-twiddles : pre[2k] = a_k, pre[2k+1] = b_k, k < M
   int* status;          // device flag set to 1 when a pass's bounded wait runs out (or null)
+  int max_polls = 1 << 22;  // bound of each wait of the TMA-fed pass (mbarrier polls)
+  int wait_extra_tx = 0;    // test support: extra bytes each tile wait expects (0 = none)
 };
 
 struct PassShape {

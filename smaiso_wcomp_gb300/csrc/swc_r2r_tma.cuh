@@ -6,9 +6,10 @@
 // (cp.async.bulk) for z passes, whose 2 LP lines are one block of memory -- issued by
 // one thread as soon as the previous tile has left the staging buffer, so the DRAM
 // read of tile t+1 overlaps the transform and the stores of tile t. Completion is an
-// mbarrier transaction count; every wait is bounded: a wait that runs out sets the
-// tables' status flag and the CTA returns after one more bounded wait for its copy in
-// flight.
+// mbarrier transaction count; every wait is bounded (tables' max_polls): a wait that
+// runs out sets the tables' status flag and the CTA returns after one more bounded wait
+// for its copy in flight. Test support: wait_extra_tx makes every wait expect more bytes
+// than its copy delivers, so the wait runs out while the copy itself is a valid one.
 // Used for plain FP32 loads (LdPlain<float, float>), any store/multiplier.
 #pragma once
 
@@ -21,8 +22,6 @@
 #include "swc_r2r_pair.cuh"
 
 namespace swc {
-
-constexpr int kTmaWaitIters = 1 << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -44,8 +43,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-  for (int it = 0; it < kTmaWaitIters; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int max_polls) {
+  for (int it = 0; it < max_polls; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -87,9 +86,9 @@ template <int N> inline bool tma_pass_supported(const Grid& g, int axis) {
 // one thread: expect the tile's bytes on the mbarrier and start its copy
 template <int N, int AX>
 __device__ __forceinline__ void tma_issue(const Grid& g, const CUtensorMap* map, const float* zsrc, int t,
-                                          uint32_t sdst, uint32_t bar) {
+                                          uint32_t sdst, uint32_t bar, int extra_tx) {
   using Tc = TmaCfg<N>;
-  mbar_expect_tx(bar, Tc::TILE_BYTES);
+  mbar_expect_tx(bar, Tc::TILE_BYTES + extra_tx);
   const int line0 = t * Tc::LINES;
   if constexpr (AX == 2) {
     bulk_load(sdst, zsrc + (size_t)line0 * N, Tc::TILE_BYTES, bar);
@@ -131,17 +130,17 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   pair_tables<N, fwd_in, inv_out>(tb, sfft, spost, spre, tid);
   if (tid == 0) {
     mbar_init(bar, 1);
-    if ((int)blockIdx.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, blockIdx.x, sdst, bar);
+    if ((int)blockIdx.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, blockIdx.x, sdst, bar, tb.wait_extra_tx);
   }
   __syncthreads();
 
   uint32_t parity = 0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x, parity ^= 1u) {
-    const bool ok = mbar_wait_bounded(bar, parity);
+    const bool ok = mbar_wait_bounded(bar, parity, tb.max_polls);
     if (!__syncthreads_and(ok)) {
       if (tid == 0) {
         if (tb.status) atomicExch(tb.status, 1);
-        mbar_wait_bounded(bar, parity);  // the copy in flight must land before the CTA leaves
+        mbar_wait_bounded(bar, parity, tb.max_polls);  // the copy in flight must land before the CTA leaves
       }
       return;
     }
@@ -228,7 +227,8 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
       }
     }
     __syncthreads();  // the staging tile is free: start the next one
-    if (tid == 0 && t + (int)gridDim.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar);
+    if (tid == 0 && t + (int)gridDim.x < ntiles)
+      tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx);
     pair_tail<N, KIND, AX>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
   }
 }

@@ -148,6 +148,10 @@ class R2RPlan:
         _check(self.lib, self.lib.swc_r2r_execute(self._h, ctypes.c_void_p(dev_ptr), ctypes.c_void_p(stream)),
                "swc_r2r_execute")
 
+    def set_wait_test(self, extra_tx_bytes, max_polls):
+        _check(self.lib, self.lib.swc_r2r_plan_set_wait_test(self._h, int(extra_tx_bytes), int(max_polls)),
+               "swc_r2r_plan_set_wait_test")
+
     def execute_axis(self, axis, dev_ptr, stream=None):
         _check(self.lib, self.lib.swc_r2r_execute_axis(self._h, int(axis), ctypes.c_void_p(dev_ptr),
                                                        ctypes.c_void_p(stream)), "swc_r2r_execute_axis")

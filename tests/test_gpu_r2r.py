@@ -85,3 +85,21 @@ def test_execute_on_device_buffer(lib):
     plan.execute_device(t.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     np.testing.assert_allclose(t.cpu().numpy(), plan(a), rtol=0, atol=1e-12 * np.abs(plan(a)).max())
+
+
+def test_tma_wait_that_runs_out_reports_status_and_recovers(lib, oracle_mod):
+    """The TMA-fed pass's bounded wait: a wait that expects 16 bytes more than its copy
+    delivers runs out after 4096 polls, the CTA sets the status flag and returns, the host
+    reads SWC_ERR_CUDA; the context stays usable and the next run is correct."""
+    from smaiso_wcomp_gb300.engine import SwcError
+    shape = (256, 64, 64)  # all three axes take the TMA-fed pass
+    a = np.random.default_rng(11).standard_normal(shape)
+    plan = R2RPlan(shape, (0, 0, 0), abi.SWC_PREC_MIXED, lib=lib)
+    plan.set_wait_test(16, 4096)
+    with pytest.raises(SwcError) as ei:
+        plan(a)
+    assert "did not complete" in str(ei.value)
+    plan.set_wait_test(0, 1 << 22)
+    ref = oracle_mod.r2r3d(a, (0, 0, 0))
+    got = plan(a)
+    assert np.max(np.abs(got - ref)) <= 1e-5 * np.max(np.abs(ref))
