@@ -171,19 +171,6 @@ template <typename T> struct LdOffset {
   }
 };
 
-template <typename T> struct LdSum2 {
-  const T *a, *b;
-  __device__ __forceinline__ T operator()(int, int, int, long long idx) const { return a[idx] + b[idx]; }
-  __device__ __forceinline__ float2 pair(int, int, int, long long idx) const {
-    const float2 x = ld2v(a, idx), y = ld2v(b, idx);
-    return make_float2(x.x + y.x, x.y + y.y);
-  }
-  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
-    const float4 x = ld4v(a, idx), y = ld4v(b, idx);
-    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
-  }
-};
-
 // First pass of the Nl transform: density AB2 update (REF:2121-2139) and the real
 // space Nl of REF:2153-2160 without the grad.f term (subtracted in spectral space).
 template <typename T> struct LdNl {
@@ -585,6 +572,8 @@ template <typename T> struct StokesArgs {
   const T *gqx, *gqy, *gqz, *gsx, *gsy, *gsz;  // exp(-1.57^2 2 q^2) per axis
   T scale, inv_nu, inv_lam2nu;  // 1/nu, 1/(lambda + 2 nu)
   int block;  // x-slab size of the reference decomposition (REF:299)
+  T *vsumx, *vsumy, *vsumz;  // v_sol + v_irr per component, the input of the S11 transforms
+  int write_vsol;            // v_sol itself only when it is transformed for output
 };
 
 // Four consecutive points along z per thread, with 32-bit indices (n^3 <= 2^30). The
@@ -632,8 +621,11 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
     vs = V4<T>::zero();
     vi = V4<T>::zero();
   }
-  vs.store(a.vsolx, idx);
+  if (a.write_vsol) vs.store(a.vsolx, idx);
   vi.store(a.virrx, idx);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) vs.v[c] = vs.v[c] + vi.v[c];
+  vs.store(a.vsumx, idx);
   // v_y, v_z for j < ny-1, k < nz-1 (REF:1758-1974); other modes stay 0
   V4<T> ys = V4<T>::zero(), yi = V4<T>::zero(), zs = V4<T>::zero(), zi = V4<T>::zero();
   if (j < g.ny - 1) {
@@ -698,10 +690,19 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
       }
     }
   }
-  ys.store(a.vsoly, idx);
+  if (a.write_vsol) {
+    ys.store(a.vsoly, idx);
+    zs.store(a.vsolz, idx);
+  }
   yi.store(a.virry, idx);
-  zs.store(a.vsolz, idx);
   zi.store(a.virrz, idx);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    ys.v[c] = ys.v[c] + yi.v[c];
+    zs.v[c] = zs.v[c] + zi.v[c];
+  }
+  ys.store(a.vsumy, idx);
+  zs.store(a.vsumz, idx);
 }
 
 // S10 (REF:2042-2079): div v and q.f on the cosine grid (q.f without `scale`).

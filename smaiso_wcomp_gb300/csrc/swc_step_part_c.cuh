@@ -10,16 +10,13 @@ namespace swc {
 template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, bool diag) {
   using LP = LdPlain<T, T>;
   using SP = StPlain<T, T>;
-  // S11 (REF:2093-2117): v = vsol + virr to real space; vsol alone on diagnostic steps
+  // S11 (REF:2093-2117): v = vsol + virr (summed by the Stokes kernel into v_) to real
+  // space in place; vsol alone on diagnostic steps
   for (int ax = 0; ax < 3; ++ax) {
     for (int which = 0; which < (diag ? 2 : 1); ++which) {
       T* out = which == 0 ? v_[ax] : vsolr_[ax];
-      if (which == 0) {
-        LdSum2<T> ld{vsol_[ax], virr_[ax]};
-        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
-        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
-      } else {
-        LP ld{vsol_[ax]};
+      {
+        LP ld{which == 0 ? v_[ax] : vsol_[ax]};
         if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
         else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
       }
