@@ -16,8 +16,12 @@
 
 #include "swc_r2r_fast.cuh"
 
-#ifndef SWC_PAIR_NT
-#define SWC_PAIR_NT 128
+// Radix plan of the 256-point lines: 1 = 16 x 8 (8 threads per line pair, 128-thread
+// CTAs), 2 = 8 x 4 x 4 (16 threads per line pair, 256-thread CTAs: twice the warps for
+// the same tile, one more shared-memory exchange). Measured on GB300 at 256^3: plan 1
+// 0.0289 ms per pass, plan 2 0.0314 ms.
+#ifndef SWC_PAIR_PLAN256
+#define SWC_PAIR_PLAN256 1
 #endif
 
 namespace swc {
@@ -116,9 +120,14 @@ template <> struct PDft<1> {
 template <int N> struct PairCfg {
   using F = FastCfg<float, N>;
   static constexpr int M = N / 2;
-  static constexpr int R1 = F::R1, R2 = F::R2;
+  static constexpr bool P3 = (N == 256 && SWC_PAIR_PLAN256 == 2);
+  // Stockham radices (R3 = 1: two stages)
+  static constexpr int R1 = P3 ? 8 : F::R1, R2 = P3 ? 4 : F::R2, R3 = P3 ? 4 : 1;
+  static_assert(R1 * R2 * R3 == M, "radix plan");
+  static constexpr int RL = (R3 > 1) ? R3 : R2;            // last stage's radix
+  static constexpr int NSL = (R3 > 1) ? R1 * R2 : R1;      // and its Stockham span
   static constexpr int TPL = M / R1;          // threads per line pair
-  static constexpr int NT = SWC_PAIR_NT;      // threads per CTA
+  static constexpr int NT = P3 ? 256 : 128;   // threads per CTA
   static constexpr int LP = NT / TPL;         // line pairs per CTA
   static constexpr int PP = LP + 1;           // PC row pitch (staggers banks for the z phases)
   static constexpr int NQ = N / 4;            // float4 per line
@@ -382,14 +391,14 @@ __device__ __forceinline__ void pair_post_store(const Grid& g, int lineA, const 
   }
 }
 
-// x/y inverse kinds: the last radix-R2 stage with both lines' outputs stored straight
+// x/y inverse kinds: the last Stockham stage with both lines' outputs stored straight
 // to global memory (slot m holds the swapped z_m: v_2m = .im, v_2m+1 = .re, v_q at
 // position mk_pos(q), negated at odd positions for DST-III).
 template <int N, int KIND, int AX, class ST>
 __device__ __forceinline__ void pair_last_store(const Grid& g, int lineA, const PC* buf, const float4* tw, int lp,
                                                 int tj, const ST& st) {
   using Cf = PairCfg<N>;
-  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, R = Cf::R2, NS = Cf::R1;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, R = Cf::RL, NS = Cf::NSL;
   constexpr int NB = M / R, PER = NB / TPL, STRIDE = M / R, TSTEP = M / (NS * R);
   PC v[PER][R];
 #pragma unroll
@@ -466,6 +475,7 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   // ---------------- forward FFT + post ----------------
   if constexpr (fwd_in) {
     pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
+    if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R3, R1 * Cf::R2, TPL, PP>(buf, sfft, lp, tj);
     if constexpr (xy && KIND != K_FILT && KIND != K_DERIV) {
       pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
       return;
@@ -497,11 +507,12 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   // ---------------- inverse FFT ----------------
   if constexpr (inv_out) {
     pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
+    if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
     if constexpr (xy) {
       pair_last_store<N, KIND, AX>(g, lineA, buf, sfft, lp, tj, st);
       return;
     }
-    pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
+    pair_stage<M, Cf::RL, Cf::NSL, TPL, PP>(buf, sfft, lp, tj);
   }
 
   // ---------------- z store ----------------
