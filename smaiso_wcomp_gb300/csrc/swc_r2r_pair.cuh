@@ -258,8 +258,10 @@ __device__ __forceinline__ void pair_stage(PC* buf, const float4* tw, int lp, in
 }
 
 // DCT-II post-processing on (k, M-k) pairs into the real layout, natural order
-// (reversed for DST-II), times the filter multiplier for K_FILT.
-template <int N, int KIND, int AX, class MUL>
+// (reversed for DST-II), times the filter multiplier for K_FILT. ROWS: one row of
+// LP + 1 float2 per position instead (the z store's layout: conflict-free writes here
+// and reads there).
+template <int N, int KIND, int AX, class MUL, bool ROWS = false>
 __device__ __forceinline__ void pair_post(const Grid& g, int lineA, PC* buf, const float2* post, int lp, int tj,
                                           const MUL& mul) {
   using Cf = PairCfg<N>;
@@ -295,7 +297,8 @@ __device__ __forceinline__ void pair_post(const Grid& g, int lineA, PC* buf, con
       v = mul2(v, mul_ab<AX>(mul, i, j, kk));
     }
     const int o = (KIND == K_S2) ? (N - 1 - pos) : pos;
-    rb2[rpi<PP>(o, lp)] = v;
+    if constexpr (ROWS) rb2[o * PP + lp] = v;
+    else rb2[rpi<PP>(o, lp)] = v;
   };
 #pragma unroll
   for (int b = 0; b < NP; ++b) {
@@ -480,7 +483,8 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
       pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
       return;
     }
-    pair_post<N, (KIND == K_DERIV ? K_C2 : KIND), AX, MulOp>(g, lineA, buf, spost, lp, tj, mul);
+    constexpr bool rows = !xy && !inv_out;  // z forward kinds: the z store reads position rows
+    pair_post<N, (KIND == K_DERIV ? K_C2 : KIND), AX, MulOp, rows>(g, lineA, buf, spost, lp, tj, mul);
     if constexpr (KIND == K_DERIV) {
       // w_i = mul(i) u_{i+1} (w_{N-1} = 0), stored reversed as the DST-III input
       constexpr int PER = N / TPL;
@@ -546,21 +550,21 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
       }
     }
   } else {
-    // natural order, one slot (y_2s, y_2s+1) per unit and float2 per line: consecutive
-    // lanes read consecutive rows of the odd pitch (no bank conflicts)
-    constexpr int SU = (LP * M) / NT;
-    constexpr int LOG2M = (M == 32) ? 5 : (M == 64) ? 6 : (M == 128) ? 7 : 8;
-    static_assert((1 << LOG2M) == M && SU * NT == LP * M, "z slot units");
+    // natural order from the position rows of pair_post: one position per unit,
+    // consecutive lanes on consecutive rows (8-byte stride mod 128: no bank conflicts)
+    constexpr int PU = (LP * N) / NT;
+    constexpr int LOG2N = (N == 64) ? 6 : (N == 128) ? 7 : (N == 256) ? 8 : 9;
+    static_assert((1 << LOG2N) == N && PU * NT == LP * N, "z position units");
 #pragma unroll 4
-    for (int c = 0; c < SU; ++c) {
+    for (int c = 0; c < PU; ++c) {
       const int u = tid + c * NT;
-      const int sl = u & (M - 1), q = u >> LOG2M;
-      const PC v = buf[sl * PP + q];
+      const int pos = u & (N - 1), q = u >> LOG2N;
+      const float2 v = rb2[pos * PP + q];
       const int la = 2 * (pair0 + q);
       const int i = la >> g.ly, j = la & (g.ny - 1);
-      const long long idx = (long long)(la * N + 2 * sl);
-      st_z2(st, i, j, 2 * sl, idx, make_float2(v.re.x, v.im.x));
-      st_z2(st, i, j + 1, 2 * sl, idx + N, make_float2(v.re.y, v.im.y));
+      const long long idx = (long long)(la * N + pos);
+      st(i, j, pos, idx, v.x);
+      st(i, j + 1, pos, idx + N, v.y);
     }
   }
 }
