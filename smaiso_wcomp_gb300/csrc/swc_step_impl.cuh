@@ -734,30 +734,63 @@ template <typename T> struct DiagArgs {
   const double* rho;
   double* partial;  // 5 doubles per block
   double ep, beta, gamma, zeta, rho0, kp;
+  const T* rhof;  // mixed engine: FP32 copy rho - off for the per-point terms (FP64: null)
+  // the coefficients in T, converted on the host: -ep/2, beta/4, gamma/6, zeta/2, rho_0, kp, off
+  T c_ep, c_beta, c_gamma, c_zeta, rho0_t, kp_t, off_t;
 };
 constexpr int kDiagThreads = 256;
 
+// Kahan-compensated FP32 accumulation: sum + value, the lost low part kept in c.
+__device__ __forceinline__ void kahan_add(float& sum, float& c, float v) {
+  const float y = v - c;
+  const float t = sum + y;
+  c = (t - sum) - y;
+  sum = t;
+}
+
+// FP64 engine: every per-point term and accumulation in FP64. Mixed engine: the
+// per-point terms in FP32 (its psi, L and A are FP32) with compensated FP32 partial sums
+// per thread (error <= 2 eps sum|x| over ~100 points), then FP64 across threads and
+// blocks; the density sum (mass) stays FP64, rho being FP64 state; the non-finite count
+// is an integer count (bit tests).
 template <typename T> __global__ void __launch_bounds__(kDiagThreads) diag_kernel(Grid g, DiagArgs<T> a) {
+  constexpr bool mixed = sizeof(T) == 4;
   __shared__ double sh[5][kDiagThreads / 32];
   double s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+  float f0 = 0.f, k0 = 0.f, f1 = 0.f, k1 = 0.f, f3 = 0.f, k3 = 0.f;
+  int nf = 0;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < g.ng;
        idx += (long long)gridDim.x * blockDim.x) {
-    // per-point terms in the work precision T (FP32 in the mixed engine: its psi, L and
-    // A are FP32), every accumulation in FP64
     const T pn = a.psi_new[idx], po = a.psi[idx], L = a.lpsi[idx], A = a.amp[idx];
     const double r = a.rho[idx];
-    s0 += (double)fabs(pn - po);
-    s1 += (double)fabs(pn);
-    s2 += r;
     const T p2 = pn * pn;
-    const T e = (T)(-0.5 * a.ep) * p2 + (T)0.5 * (L * L) - (T)(0.25 * a.beta) * (p2 * p2) +
-                (T)(a.gamma / 6) * (p2 * p2 * p2);
-    const T d = (T)r - (T)a.rho0 - (T)a.kp * A;
-    s3 += (double)((T)r * e + (T)(0.5 * a.zeta) * (d * d));
-    s4 += (double)(!isfinite(pn)) + (double)(!isfinite(r));
+    const T e = a.c_ep * p2 + (T)0.5 * (L * L) - a.c_beta * (p2 * p2) + a.c_gamma * (p2 * p2 * p2);
+    if constexpr (mixed) {
+      const T rr = a.rhof[idx] + a.off_t;
+      const T d = rr - a.rho0_t - a.kp_t * A;
+      kahan_add(f0, k0, fabsf(pn - po));
+      kahan_add(f1, k1, fabsf(pn));
+      s2 += r;
+      kahan_add(f3, k3, rr * e + a.c_zeta * (d * d));
+      const uint32_t pb = f32_bits(pn), rh = (uint32_t)__double2hiint(r);
+      nf += (((pb >> 23) & 0xffu) == 0xffu) + (((rh >> 20) & 0x7ffu) == 0x7ffu);
+    } else {
+      s0 += (double)fabs(pn - po);
+      s1 += (double)fabs(pn);
+      s2 += r;
+      const T d = (T)r - a.rho0_t - a.kp_t * A;
+      s3 += (double)((T)r * e + a.c_zeta * (d * d));
+      s4 += (double)(!isfinite(pn)) + (double)(!isfinite(r));
+    }
     a.energy[idx] = (T)e;
-    a.psi_old[idx] = a.psi[idx];
-    a.psi[idx] = a.psi_new[idx];
+    a.psi_old[idx] = po;
+    a.psi[idx] = pn;
+  }
+  if constexpr (mixed) {
+    s0 = (double)f0 - (double)k0;
+    s1 = (double)f1 - (double)k1;
+    s3 = (double)f3 - (double)k3;
+    s4 = (double)nf;
   }
   double v[5] = {s0, s1, s2, s3, s4};
 #pragma unroll

@@ -53,7 +53,9 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
   SWC_TRY((pass<K_C3, 0>(LP{pout}, SP{pout})));
   if (diag) {
     DiagArgs<T> a{psi_new_, lpsi_, amp_f_, psi_, psi_old_, energy_, rho_, partial_,
-                  p_.ep, p_.beta, p_.gamma, p_.zeta, p_.rho_0, kp_};
+                  p_.ep, p_.beta, p_.gamma, p_.zeta, p_.rho_0, kp_, rhof_,
+                  (T)(-0.5 * p_.ep), (T)(0.25 * p_.beta), (T)(p_.gamma / 6), (T)(0.5 * p_.zeta),
+                  (T)p_.rho_0, (T)kp_, (T)rho_off_};
     diag_kernel<T><<<diag_blocks_, kDiagThreads, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
     diag_final_kernel<<<1, 32, 0, stream_>>>(partial_, diag_blocks_, dsum_);
