@@ -244,6 +244,10 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
     return SWC_ERR_STATE;
   }
   SWC_CK(cudaSetDevice(p_.device));
+  if (vsol_pending_) {  // the recompute below reuses the spectral v_sol buffers
+    SWC_TRY(transform_vsol());
+    vsol_pending_ = false;
+  }
   SWC_CK(cudaStreamSynchronize(stream_));
   const size_t ng = (size_t)g_.ng;
   const int64_t Tn = nloop_;

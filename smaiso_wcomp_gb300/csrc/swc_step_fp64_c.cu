@@ -5,4 +5,6 @@
 
 namespace swc {
 template int StepEngine<double>::enqueue_part_c(bool relax, bool first, bool diag);
+template int StepEngine<double>::inverse_velocity(int ax, double* in, double* out);
+template int StepEngine<double>::transform_vsol();
 }  // namespace swc

@@ -895,6 +895,8 @@ template <typename T> class StepEngine : public EngineBase {
   int enqueue_part_a(bool relax, bool first, bool diag);  // S1-S5
   int enqueue_part_b(bool relax, bool first, bool diag);  // S5 tail-S10 (swc_step_part_b.cuh)
   int enqueue_part_c(bool relax, bool first, bool diag);  // S11-S14 (swc_step_part_c.cuh)
+  int inverse_velocity(int ax, T* in, T* out);             // (swc_step_part_c.cuh)
+  int transform_vsol();                                    // (swc_step_part_c.cuh)
   int run_graph(bool relax, bool first, bool diag);
   void release();
   int field_src(int field, const void** src, bool* is_double);
@@ -930,6 +932,7 @@ template <typename T> class StepEngine : public EngineBase {
   int64_t launches_ = 0;  // running count while a variant is captured
   bool have_state_ = false;
   bool have_vsol_ = false;
+  bool vsol_pending_ = false;  // spectral v_sol of the last step not yet in real space
   int64_t nloop_ = 0;
   swc_diag diag_{};
   double last_ms_ = 0;
@@ -1239,6 +1242,7 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   nloop_ = 0;
   have_state_ = true;
   have_vsol_ = false;
+  vsol_pending_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
   return SWC_OK;
 }
@@ -1339,6 +1343,7 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   diag_.step = nloop_;
   diag_.nonfinite = (int64_t)sums[4];
   have_vsol_ = true;
+  vsol_pending_ = true;
   if (diag_.nonfinite) {
     set_error("non-finite psi/rho after step %lld (%lld values)", (long long)nloop_, (long long)diag_.nonfinite);
     return SWC_ERR_NONFINITE;
@@ -1348,6 +1353,12 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
 
 template <typename T> int StepEngine<T>::field_src(int field, const void** src, bool* is_double) {
   *is_double = false;
+  if ((field == SWC_F_VSOLX || field == SWC_F_VSOLY || field == SWC_F_VSOLZ) && vsol_pending_) {
+    SWC_CK(cudaSetDevice(p_.device));
+    SWC_TRY(transform_vsol());
+    SWC_CK(cudaStreamSynchronize(stream_));
+    vsol_pending_ = false;
+  }
   switch (field) {
     case SWC_F_PSI: *src = psi_; break;
     case SWC_F_RHO: *src = rho_; *is_double = true; break;
@@ -1526,6 +1537,7 @@ template <typename T> int StepEngine<T>::load(const char* path) {
   nloop_ = h.nloop;
   have_state_ = true;
   have_vsol_ = false;
+  vsol_pending_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
   diag_.step = nloop_;
   return SWC_OK;

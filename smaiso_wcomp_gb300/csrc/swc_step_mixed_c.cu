@@ -5,4 +5,6 @@
 
 namespace swc {
 template int StepEngine<float>::enqueue_part_c(bool relax, bool first, bool diag);
+template int StepEngine<float>::inverse_velocity(int ax, float* in, float* out);
+template int StepEngine<float>::transform_vsol();
 }  // namespace swc

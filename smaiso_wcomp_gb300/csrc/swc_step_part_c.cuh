@@ -7,25 +7,35 @@
 
 namespace swc {
 
+// The staggered inverse transform of one velocity component (REF:2093-2117): DST-III
+// along its own axis, DCT-III along the other two.
+template <typename T> int StepEngine<T>::inverse_velocity(int ax, T* in, T* out) {
+  using LP = LdPlain<T, T>;
+  using SP = StPlain<T, T>;
+  if (ax == 2) SWC_TRY((pass<K_S3, 2>(LP{in}, SP{out})));
+  else SWC_TRY((pass<K_C3, 2>(LP{in}, SP{out})));
+  if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
+  else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
+  if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
+  else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
+  return SWC_OK;
+}
+
+// v_sol of the last step to real space, when a v_sol field is read (REF:2099-2117):
+// the Stokes kernel keeps spectral v_sol on the last step of each swc_step call.
+template <typename T> int StepEngine<T>::transform_vsol() {
+  const int64_t keep = launches_;
+  for (int ax = 0; ax < 3; ++ax) SWC_TRY(inverse_velocity(ax, vsol_[ax], vsolr_[ax]));
+  launches_ = keep;
+  return SWC_OK;
+}
+
 template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, bool diag) {
   using LP = LdPlain<T, T>;
   using SP = StPlain<T, T>;
   // S11 (REF:2093-2117): v = vsol + virr (summed by the Stokes kernel into v_) to real
-  // space in place; vsol alone on diagnostic steps
-  for (int ax = 0; ax < 3; ++ax) {
-    for (int which = 0; which < (diag ? 2 : 1); ++which) {
-      T* out = which == 0 ? v_[ax] : vsolr_[ax];
-      {
-        LP ld{which == 0 ? v_[ax] : vsol_[ax]};
-        if (ax == 2) SWC_TRY((pass<K_S3, 2>(ld, SP{out})));
-        else SWC_TRY((pass<K_C3, 2>(ld, SP{out})));
-      }
-      if (ax == 1) SWC_TRY((pass<K_S3, 1>(LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3, 1>(LP{out}, SP{out})));
-      if (ax == 0) SWC_TRY((pass<K_S3, 0>(LP{out}, SP{out})));
-      else SWC_TRY((pass<K_C3, 0>(LP{out}, SP{out})));
-    }
-  }
+  // space in place; v_sol alone is transformed on demand (transform_vsol)
+  for (int ax = 0; ax < 3; ++ax) SWC_TRY(inverse_velocity(ax, v_[ax], v_[ax]));
   // S12 + S13 + S14 (REF:2121-2197): rho update, Nl, its DCT, the psiq update, psi = iDCT(psiq_new)
   T* pout = diag ? psi_new_ : psi_;
   if constexpr (std::is_same<T, double>::value) {
