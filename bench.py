@@ -50,6 +50,9 @@ def parse():
                     help="also run both engines this many steps from the initial state and report psi/rho error")
     ap.add_argument("--grad-steps", type=int, default=40,
                     help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
+    ap.add_argument("--workload", choices=["undulated", "dislocations"], default="undulated",
+                    help="dislocations: the 512x512x256 layer-dislocation configuration, reported as "
+                         "its own JSON line (mixed and FP64 steps/s, mixed-vs-FP64 errors)")
     ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
                     help="profiling mode: run only this engine's warm-up + timed steps and print its timing")
     return ap.parse_args()
@@ -254,6 +257,41 @@ def accuracy_run(steps, device=0):
             "energy_rel": abs(out[1][2]["energy"] - out[0][2]["energy"]) / abs(out[0][2]["energy"])}
 
 
+def dislocation_run(steps, warmup, acc_steps, device=0):
+    """512x512x256 layer-dislocation workload (16 seeded edge-dislocation cores below a
+    flat interface, density ratio 0.8): mixed and FP64 steps/s, and the mixed engine's
+    psi / rho / v relative L2 error against the FP64 engine after acc_steps steps."""
+    from smaiso_wcomp_gb300 import abi, ic
+    from smaiso_wcomp_gb300.engine import Engine
+    shape = (512, 512, 256)
+    base = abi.default_params(*shape, rho_0=0.8)
+    psi, rho = ic.dislocations(base)
+    res = {"workload": "layer dislocations 512x512x256, 16 cores, density ratio 0.8, dt 1e-3",
+           "points": int(np.prod(shape))}
+    fields = {}
+    for prec, name in ((abi.SWC_PREC_MIXED, "mixed"), (abi.SWC_PREC_FP64, "fp64")):
+        p = abi.default_params(*shape, rho_0=0.8, precision=prec, device=device)
+        with Engine(p) as e:
+            e.set_state(psi, rho)
+            e.step(acc_steps)
+            fields[name] = {f: e.field(f) for f in ("psi", "rho", "vx", "vy", "vz")}
+            n = steps if prec == abi.SWC_PREC_MIXED else max(5, steps // 10)
+            e.step(warmup)
+            e.step(n)   # graph-launched steps, CUDA events on the context's stream
+            ms = e.last_step_ms() / n
+        res[f"{name}_steps_per_s"] = 1e3 / ms
+        res[f"{name}_ms_per_step"] = ms
+    res["grid_point_steps_per_s"] = res["mixed_steps_per_s"] * res["points"]
+    res["mixed_over_fp64"] = res["mixed_steps_per_s"] / res["fp64_steps_per_s"]
+    a, b = fields["mixed"], fields["fp64"]
+    rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))  # noqa: E731
+    vn = np.sqrt(sum(np.linalg.norm(b[c]) ** 2 for c in ("vx", "vy", "vz")))
+    dv = np.sqrt(sum(np.linalg.norm(a[c] - b[c]) ** 2 for c in ("vx", "vy", "vz")))
+    res["errors_after_steps"] = acc_steps
+    res["psi_rel_l2"], res["rho_rel_l2"], res["v_rel_l2"] = rel(a["psi"], b["psi"]), rel(a["rho"], b["rho"]), float(dv / vn)
+    return res
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -310,6 +348,9 @@ def main():
         pg = dist
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
+    if args.workload == "dislocations":
+        print(json.dumps(dislocation_run(args.steps, args.warmup, args.accuracy_steps or 50, local)), flush=True)
+        return
     if args.only == "pass":
         ms, per_axis, alg = pass_roofline(abi.SWC_PREC_MIXED, reps=args.steps)
         print(json.dumps({"only": "pass", "ms_per_pass": ms, "pass_ms_zyx": per_axis,

@@ -162,3 +162,24 @@ def test_full_size_fp64_vs_mixed_256(lib):
         e.close()
     assert out[0][1]["nonfinite"] == 0 and out[1][1]["nonfinite"] == 0
     assert rel(out[1][0], out[0][0]) <= 1e-5
+
+
+def test_dislocations_512x512x256_mixed_vs_fp64(lib):
+    """The 512x512x256 layer-dislocation workload (16 seeded edge dislocations below a
+    flat interface): both engines run 8 steps from the same state; the mixed engine's
+    psi, rho and v stay within the FP32-transform error of the FP64 engine."""
+    p64 = abi.default_params(512, 512, 256, rho_0=0.8)
+    psi, rho = ic.dislocations(p64)
+    out = {}
+    for prec in (abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED):
+        with Engine(abi.default_params(512, 512, 256, rho_0=0.8, precision=prec)) as e:
+            e.set_state(psi, rho)
+            e.step(8)
+            assert e.diagnostics()["nonfinite"] == 0
+            out[prec] = {f: e.field(f) for f in ("psi", "rho", "vx", "vy", "vz")}
+    a, b = out[abi.SWC_PREC_MIXED], out[abi.SWC_PREC_FP64]
+    assert rel(a["psi"], b["psi"]) <= 1e-5
+    assert rel(a["rho"], b["rho"]) <= 1e-6
+    vn = np.sqrt(sum(np.linalg.norm(b[c]) ** 2 for c in ("vx", "vy", "vz")))
+    dv = np.sqrt(sum(np.linalg.norm(a[c] - b[c]) ** 2 for c in ("vx", "vy", "vz")))
+    assert dv <= 1e-3 * vn
