@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define SWC_ABI_VERSION 1
+#define SWC_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------- */
 enum {
@@ -116,7 +116,16 @@ typedef struct swc_params {
   int adjoint_ckpt;   /* 0: no adjoint. K > 0 (FP64 engine): swc_step keeps a state
                          checkpoint every K steps so swc_backward can recompute the
                          trajectory; device memory = (steps/K + 1) states of 6 N^3
-                         doubles + one segment tape of K x 22 N^3 doubles. */
+                         doubles + one segment tape of K x 24 N^3 doubles.
+                         -1 (FP64 engine): binomial checkpointing -- swc_step keeps only
+                         the initial state and swc_backward reverses the trajectory with
+                         a binomial recompute schedule over as many 6 N^3-double state
+                         snapshots as fit under adjoint_cap_gb, with a one-step tape. */
+  double adjoint_cap_gb; /* adjoint_ckpt = -1: device memory cap of the context during
+                            swc_backward, in GB (1e9 B), engine arrays included; <= 0:
+                            the device's free memory at the call less 1 GB. */
+  int adjoint_snapshots; /* adjoint_ckpt = -1: at most this many snapshots (<= 0: as
+                            many as fit under the cap) */
 } swc_params;
 
 /* Gradients returned by swc_backward: dL/d(coefficient) of the coefficients the
@@ -128,6 +137,8 @@ typedef struct swc_grad {
   double nu;     /* d/d nu      (REF:249) */
   double rho_0;  /* d/d rho_0   (REF:251; the density ratio rho_i/rho_s, rho_s = 1) */
   int64_t steps; /* steps differentiated (nLoop at the call) */
+  int64_t forward_steps;  /* forward steps rerun by the call (recompute and tape) */
+  int64_t snapshots;      /* state snapshot slots used (binomial mode; 0 otherwise) */
 } swc_grad;
 
 /* Diagnostics of the last step of a swc_step call (smaiso-wcomp.cpp:2202-2262). */

@@ -53,7 +53,8 @@ class SwcParams(ctypes.Structure):
         ("nu", ctypes.c_double), ("lambda_", ctypes.c_double), ("zeta", ctypes.c_double),
         ("rho_0", ctypes.c_double), ("divv_switch", ctypes.c_int), ("load", ctypes.c_int),
         ("ref_ranks", ctypes.c_int), ("precision", ctypes.c_int), ("device", ctypes.c_int),
-        ("watchdog_s", ctypes.c_double), ("adjoint_ckpt", ctypes.c_int),
+        ("watchdog_s", ctypes.c_double), ("adjoint_ckpt", ctypes.c_int), ("adjoint_cap_gb", ctypes.c_double),
+        ("adjoint_snapshots", ctypes.c_int),
     ]
 
 
@@ -71,7 +72,8 @@ class SwcDiag(ctypes.Structure):
 
 class SwcGrad(ctypes.Structure):
     _fields_ = [("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("gamma", ctypes.c_double),
-                ("nu", ctypes.c_double), ("rho_0", ctypes.c_double), ("steps", ctypes.c_int64)]
+                ("nu", ctypes.c_double), ("rho_0", ctypes.c_double), ("steps", ctypes.c_int64),
+                ("forward_steps", ctypes.c_int64), ("snapshots", ctypes.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -93,7 +95,7 @@ def default_params(nx, ny=None, nz=None, **overrides):
     p = SwcParams(nx=nx, ny=ny, nz=nz, nw=8, dt=0.001, alpha=1.0, beta=2.0, gamma=1.0,
                   ep=-0.001, q0=1.0, nu=1.0, lambda_=1.0, zeta=1.0, rho_0=0.01,
                   divv_switch=50, load=0, ref_ranks=2, precision=SWC_PREC_FP64, device=0,
-                  watchdog_s=0.0, adjoint_ckpt=0)
+                  watchdog_s=0.0, adjoint_ckpt=0, adjoint_cap_gb=0.0, adjoint_snapshots=0)
     for k, v in overrides.items():
         setattr(p, "lambda_" if k == "lambda" else k, v)
     return p

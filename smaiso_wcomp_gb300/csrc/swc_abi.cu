@@ -106,8 +106,8 @@ int validate_params(const swc_params* p) {
     set_error("ref_ranks=%d must be >= 1 and divide nx=%d", p->ref_ranks, p->nx);
     return SWC_ERR_BAD_PARAM;
   }
-  if (p->adjoint_ckpt < 0 || (p->adjoint_ckpt > 0 && p->precision != SWC_PREC_FP64)) {
-    set_error("adjoint_ckpt must be >= 0 and needs precision SWC_PREC_FP64");
+  if (p->adjoint_ckpt < -1 || (p->adjoint_ckpt != 0 && p->precision != SWC_PREC_FP64)) {
+    set_error("adjoint_ckpt must be -1 (binomial), 0 or K > 0, and needs precision SWC_PREC_FP64");
     return SWC_ERR_BAD_PARAM;
   }
   if (p->divv_switch < 0 || (p->precision != SWC_PREC_FP64 && p->precision != SWC_PREC_MIXED) || p->device < 0) {
@@ -184,6 +184,8 @@ int swc_default_params(swc_params* p, int nx, int ny, int nz) {
   p->device = 0;
   p->watchdog_s = 0.0;
   p->adjoint_ckpt = 0;
+  p->adjoint_cap_gb = 0.0;
+  p->adjoint_snapshots = 0;
   return SWC_OK;
 }
 

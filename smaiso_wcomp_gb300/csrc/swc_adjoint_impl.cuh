@@ -1,12 +1,16 @@
 // swc_adjoint_impl.cuh -- the discrete adjoint of the FP64 time step and the
 // segmented recompute behind swc_backward (included by the FP64 engine only).
 //
-// Trajectory: swc_step kept the state every K = adjoint_ckpt steps (swc_set_state
-// kept step 0). swc_backward walks the segments from the last: it restores the
-// segment's first state, reruns its steps keeping a tape of the intermediates each
-// adjoint step reads, then applies the adjoint steps in reverse. Device memory:
-// (T/K + 1) checkpoints of 6 N^3 doubles + K tape slots of kTape N^3 doubles + the
-// adjoint work arrays (kAdj N^3 doubles).
+// Trajectory, two schedules. K = adjoint_ckpt > 0: swc_step kept the state every K
+// steps (swc_set_state kept step 0); swc_backward walks the segments from the last,
+// restores the segment's first state, reruns its steps keeping a tape of the
+// intermediates each adjoint step reads, then applies the adjoint steps in reverse.
+// Device memory: (T/K + 2) checkpoints of 6 N^3 doubles + K tape slots of kTape N^3
+// doubles + the adjoint work arrays (kAdj N^3 doubles). adjoint_ckpt = -1: binomial
+// checkpointing (Griewank's schedule): only the initial state is kept by the forward;
+// with s snapshot slots and t the least integer with C(s + t, t) >= T, the reversal
+// rerun each forward step at most t times plus once for the tape, the tape holds one
+// step, and s is the largest count that fits under adjoint_cap_gb.
 #pragma once
 
 #include "swc_adjoint_kernels.cuh"
@@ -231,14 +235,81 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   return SWC_OK;
 }
 
+// Step n (1-based) from the loaded state n-1 with its tape (slot 0), then its adjoint.
+template <typename T> int StepEngine<T>::tape_and_adjoint(int64_t n) {
+  const size_t ng = (size_t)g_.ng;
+  double* tp = tape_;
+  SWC_CK(cudaMemcpyAsync(tp + TP_RHOIN * ng, rho_, ng * 8, cudaMemcpyDeviceToDevice, stream_));
+  const bool relax = !(n > p_.divv_switch || p_.load == 1);
+  SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old and v_sol
+  const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
+                            amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
+                            vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
+  for (int q = 0; q < kTape; ++q)
+    if (src[q]) SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src[q], ng * 8, cudaMemcpyDeviceToDevice, stream_));
+  ++fwd_steps_;
+  return adjoint_step(0, relax, n == 1);
+}
+
+// k plain forward steps from the loaded state `from` (steps from+1 .. from+k).
+template <typename T> int StepEngine<T>::advance(int64_t from, int64_t k) {
+  for (int64_t n = from + 1; n <= from + k; ++n) {
+    const bool relax = !(n > p_.divv_switch || p_.load == 1);
+    SWC_TRY(run_graph(relax, n == 1, false));
+  }
+  fwd_steps_ += k;
+  return SWC_OK;
+}
+
+// C(s + t, t): the most steps s snapshot slots reverse with each step rerun <= t times
+// (saturating).
+static inline int64_t binomial_reach(int64_t s, int64_t t) {
+  double c = 1.0;
+  for (int64_t i = 1; i <= t; ++i) {
+    c = c * (double)(s + i) / (double)i;
+    if (c > 9.0e18) return INT64_MAX;
+  }
+  return (int64_t)(c + 0.5);
+}
+
+// Reverse steps l+1 .. l+n given state l in checkpoint slot sl, with nfree snapshot slots
+// ff, ff+1, ... free: place one snapshot where the binomial split puts it, reverse the
+// right part with one slot less, then the left part with the slot back.
+template <typename T>
+int StepEngine<T>::reverse_binomial(int64_t l, int64_t n, size_t sl, size_t ff, int64_t nfree) {
+  if (n <= 0) return SWC_OK;
+  if (n == 1) {
+    SWC_TRY(restore_ckpt(sl));
+    return tape_and_adjoint(l + 1);
+  }
+  if (nfree == 0) {
+    for (int64_t k = n; k >= 1; --k) {
+      SWC_TRY(restore_ckpt(sl));
+      SWC_TRY(advance(l, k - 1));
+      SWC_TRY(tape_and_adjoint(l + k));
+    }
+    return SWC_OK;
+  }
+  int64_t t = 1;
+  while (binomial_reach(nfree, t) < n) ++t;
+  const int64_t right = std::min<int64_t>(n - 1, binomial_reach(nfree - 1, t));
+  const int64_t m = n - right;
+  SWC_TRY(restore_ckpt(sl));
+  SWC_TRY(advance(l, m));
+  SWC_TRY(save_ckpt(ff));
+  SWC_TRY(reverse_binomial(l + m, right, ff, ff + 1, nfree - 1));
+  return reverse_binomial(l, m, sl, ff, nfree);
+}
+
 template <typename T>
 int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double* dpsi0, double* drho0,
                                  swc_grad* out) {
   const int K = p_.adjoint_ckpt;
-  if (K <= 0) {
-    set_error("swc_backward needs params.adjoint_ckpt > 0 at swc_create");
+  if (K == 0) {
+    set_error("swc_backward needs params.adjoint_ckpt > 0 or -1 at swc_create");
     return SWC_ERR_BAD_PARAM;
   }
+  const bool binomial = K < 0;
   if (!have_state_ || !adj_valid_) {
     set_error("swc_backward: no trajectory from swc_set_state to differentiate");
     return SWC_ERR_STATE;
@@ -251,10 +322,32 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
   SWC_CK(cudaStreamSynchronize(stream_));
   const size_t ng = (size_t)g_.ng;
   const int64_t Tn = nloop_;
-  SWC_TRY(adjoint_alloc((size_t)(Tn < K ? (Tn > 0 ? Tn : 1) : K)));
+  SWC_TRY(adjoint_alloc(binomial ? 1 : (size_t)(Tn < K ? (Tn > 0 ? Tn : 1) : K)));
   // the final state, restored when the call returns (slot past the trajectory's)
-  const size_t last_slot = (size_t)(Tn / K) + 1;
+  const size_t last_slot = binomial ? 1 : (size_t)(Tn / K) + 1;
   SWC_TRY(save_ckpt(last_slot));
+  int64_t nsnap = 0;
+  if (binomial) {
+    // snapshot slots under the cap: engine arrays + adjoint work + tape + slots 0, 1 + s
+    const size_t slot_bytes = 6 * ng * sizeof(double);
+    const size_t used = engine_bytes_ + (size_t)kAdj * ng * 8 + pgrad_doubles() * 8 + (size_t)kTape * ng * 8 +
+                        ckpt_.size() * slot_bytes;
+    double cap = p_.adjoint_cap_gb * 1e9;
+    if (cap <= 0) {
+      size_t fr = 0, tot = 0;
+      SWC_CK(cudaMemGetInfo(&fr, &tot));
+      cap = (double)used + (double)fr - 1e9;
+    }
+    if (cap < (double)used) {
+      set_error("adjoint_cap_gb %.3f is below the %.3f GB the reversal needs before any snapshot",
+                p_.adjoint_cap_gb, (double)used / 1e9);
+      return SWC_ERR_OOM;
+    }
+    nsnap = (int64_t)((cap - (double)used) / (double)slot_bytes);
+    nsnap = std::min<int64_t>(nsnap, std::max<int64_t>(Tn - 1, 0));  // one per step is the most useful
+    if (p_.adjoint_snapshots > 0) nsnap = std::min<int64_t>(nsnap, p_.adjoint_snapshots);
+  }
+  fwd_steps_ = 0;
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
   SWC_CK(cudaMemsetAsync(adj_, 0, (size_t)kAdj * ng * sizeof(double), stream_));
   SWC_CK(cudaMemsetAsync(pgrad_, 0, pgrad_doubles() * sizeof(double), stream_));
@@ -269,25 +362,30 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
     SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_PSI)}, StW{g_, AJ(AJ_Q), wh, 0})));
   }
   if (drho) SWC_CK(cudaMemcpyAsync(AJ(AJ_R), drho, ng * 8, cudaMemcpyHostToDevice, stream_));
-  // segments [s0, s1), last first
-  const int64_t nseg = (Tn + K - 1) / K;
-  for (int64_t sg = nseg - 1; sg >= 0; --sg) {
-    const int64_t s0 = sg * K, s1 = std::min<int64_t>(s0 + K, Tn);
-    SWC_TRY(restore_ckpt((size_t)sg));
-    for (int64_t n = s0 + 1; n <= s1; ++n) {
-      double* tp = tape_ + (size_t)(n - s0 - 1) * kTape * ng;
-      SWC_CK(cudaMemcpyAsync(tp + TP_RHOIN * ng, rho_, ng * 8, cudaMemcpyDeviceToDevice, stream_));
-      const bool relax = !(n > p_.divv_switch || p_.load == 1);
-      SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old
-      const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
-                                amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
-                                vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
-      for (int q = 0; q < kTape; ++q)
-        if (src[q]) SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src[q], ng * 8, cudaMemcpyDeviceToDevice, stream_));
-    }
-    for (int64_t n = s1; n > s0; --n) {
-      const bool relax = !(n > p_.divv_switch || p_.load == 1);
-      SWC_TRY(adjoint_step((size_t)(n - s0 - 1), relax, n == 1));
+  if (binomial) {
+    SWC_TRY(reverse_binomial(0, Tn, 0, 2, nsnap));
+  } else {
+    // segments [s0, s1), last first
+    const int64_t nseg = (Tn + K - 1) / K;
+    for (int64_t sg = nseg - 1; sg >= 0; --sg) {
+      const int64_t s0 = sg * K, s1 = std::min<int64_t>(s0 + K, Tn);
+      SWC_TRY(restore_ckpt((size_t)sg));
+      for (int64_t n = s0 + 1; n <= s1; ++n) {
+        double* tp = tape_ + (size_t)(n - s0 - 1) * kTape * ng;
+        SWC_CK(cudaMemcpyAsync(tp + TP_RHOIN * ng, rho_, ng * 8, cudaMemcpyDeviceToDevice, stream_));
+        const bool relax = !(n > p_.divv_switch || p_.load == 1);
+        SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old
+        const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
+                                  amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
+                                  vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
+        for (int q = 0; q < kTape; ++q)
+          if (src[q]) SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src[q], ng * 8, cudaMemcpyDeviceToDevice, stream_));
+        ++fwd_steps_;
+      }
+      for (int64_t n = s1; n > s0; --n) {
+        const bool relax = !(n > p_.divv_switch || p_.load == 1);
+        SWC_TRY(adjoint_step((size_t)(n - s0 - 1), relax, n == 1));
+      }
     }
   }
   // swc_set_state: psiq0 = scale DCT-II^3 psi0 = psiq_old0  =>  psi0_bar = scale DCT-III^3 D0 (Q_bar + Qo_bar)
@@ -324,6 +422,8 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
   out->nu = pg[PG_NU];
   out->rho_0 = pg[PG_RHO0] + pg[PG_KP] * dkp_drho0;
   out->steps = Tn;
+  out->forward_steps = fwd_steps_;
+  out->snapshots = nsnap;
   return SWC_OK;
 }
 

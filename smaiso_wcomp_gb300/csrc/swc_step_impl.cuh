@@ -871,6 +871,11 @@ template <typename T> class StepEngine : public EngineBase {
   int backward_fp64(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
   int adjoint_step(size_t slot, bool relax, bool first);
   int adjoint_alloc(size_t tape_steps);
+  int tape_and_adjoint(int64_t n);                        // step n from the loaded state n-1
+  int advance(int64_t from, int64_t k);                   // k plain steps from state `from`
+  int reverse_binomial(int64_t l, int64_t n, size_t sl, size_t ff, int64_t nfree);
+  int64_t fwd_steps_ = 0;          // forward steps rerun by the current swc_backward
+  size_t engine_bytes_ = 0;        // device bytes of the engine's own arrays
   std::vector<double*> ckpt_;      // state at steps 0, K, 2K, ... (6 arrays each)
   double* tape_ = nullptr;         // forward intermediates of one segment
   size_t tape_steps_ = 0;
@@ -990,6 +995,7 @@ template <typename T> int StepEngine<T>::init() {
       return SWC_ERR_OOM;
     }
     allocs_.push_back(ptr);
+    engine_bytes_ += bytes;
     *out = ptr;
     return SWC_OK;
   };
@@ -1236,8 +1242,8 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   SWC_TRY((pass<K_C3, 0>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, nt, cudaMemcpyDeviceToDevice, stream_));  // REF:1010
   SWC_TRY(refresh_copies(false));
-  if (p_.adjoint_ckpt > 0) SWC_TRY(save_ckpt(0));
-  adj_valid_ = p_.adjoint_ckpt > 0;
+  if (p_.adjoint_ckpt != 0) SWC_TRY(save_ckpt(0));
+  adj_valid_ = p_.adjoint_ckpt != 0;
   SWC_CK(cudaStreamSynchronize(stream_));
   nloop_ = 0;
   have_state_ = true;

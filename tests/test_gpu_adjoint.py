@@ -22,10 +22,11 @@ def run(p, psi0, rho0, nsteps, wp, wr):
         return loss(e, wp, wr)
 
 
-CASES = [  # shape, divv_switch, steps, checkpoint interval: relax + normal phase, several segments
+CASES = [  # shape, divv_switch, steps, checkpoint interval (-1: binomial): relax + normal phase
     ((16, 16, 32), 3, 6, 2),
     ((16, 8, 16), 2, 5, 4),
     ((8, 16, 16), 0, 3, 1),
+    ((16, 16, 16), 2, 7, -1),
 ]
 
 
@@ -90,3 +91,45 @@ def test_torch_gradcheck_through_the_shim(lib):
                      requires_grad=True)
     f = lambda x, c: StepFunction.apply(x, c, base, 2, rho0, 1)  # noqa: E731
     assert torch.autograd.gradcheck(f, (x, c), eps=1e-6, atol=1e-7, rtol=1e-5, fast_mode=True)
+
+
+@pytest.mark.parametrize("snapshots", [0, 1, 2, 4, 12])
+def test_binomial_schedule_matches_segments(lib, snapshots):
+    """Binomial checkpointing (adjoint_ckpt = -1) with 0, 1, 2, 4 and 12 snapshot slots
+    reverses the same trajectory as the fixed-interval schedule: the same gradients
+    (the recompute is deterministic), with each forward step rerun at most t times plus
+    once for the tape, t the least integer with C(s + t, t) >= T."""
+    shape, ds, nsteps = (16, 16, 32), 4, 13
+    rng = np.random.default_rng(3)
+    wp, wr = rng.standard_normal(shape), rng.standard_normal(shape)
+    grads = {}
+    for ckpt in (3, -1):
+        p = abi.default_params(*shape, rho_0=0.8, divv_switch=ds, adjoint_ckpt=ckpt, ref_ranks=2,
+                               adjoint_snapshots=snapshots if ckpt < 0 else 0)
+        psi0, rho0 = ic.undulated_interface(p, sigma=1e-2)
+        with Engine(p) as e:
+            e.set_state(psi0, rho0)
+            e.step(nsteps)
+            grads[ckpt] = e.backward(dpsi=wp, drho=wr, want_psi0=True, want_rho0=True)
+    a, b = grads[-1], grads[3]
+    s = min(snapshots, nsteps - 1) if snapshots > 0 else nsteps - 1
+    assert a["snapshots"] == s
+    t = 1
+    while __import__("math").comb(s + t, t) < nsteps:
+        t += 1
+    assert nsteps <= a["forward_steps"] <= (t + 1) * nsteps
+    assert b["forward_steps"] == nsteps
+    for key in ("psi0", "rho0"):
+        assert np.linalg.norm(a[key] - b[key]) <= 1e-12 * np.linalg.norm(b[key]), key
+    for name in COEFFS:
+        assert abs(a[name] - b[name]) <= 1e-12 * max(abs(b[name]), 1e-30), name
+
+
+def test_binomial_cap_too_small_is_rejected(lib):
+    from smaiso_wcomp_gb300.engine import SwcError
+    p = abi.default_params(16, 16, 16, adjoint_ckpt=-1, adjoint_cap_gb=1e-6)
+    with Engine(p) as e:
+        e.set_state(np.zeros((16, 16, 16)))
+        e.step(3)
+        with pytest.raises(SwcError):
+            e.backward(dpsi=np.ones((16, 16, 16)))
