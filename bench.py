@@ -50,7 +50,8 @@ def parse():
                     help="also run both engines this many steps from the initial state and report psi/rho error")
     ap.add_argument("--grad-steps", type=int, default=40,
                     help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
-    ap.add_argument("--workload", choices=["undulated", "dislocations"], default="undulated",
+    ap.add_argument("--workload", choices=["undulated", "dislocations", "adjoint128", "adjoint256"],
+                    default="undulated",
                     help="dislocations: the 512x512x256 layer-dislocation configuration, reported as "
                          "its own JSON line (mixed and FP64 steps/s, mixed-vs-FP64 errors)")
     ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
@@ -239,6 +240,93 @@ def gradient_forward_ratio(steps, ckpt=20, n=128):
             "dL_dalpha": g["alpha"]}
 
 
+CAL_COEFFS = ("alpha", "beta", "gamma", "nu", "rho_0")
+
+
+def calibration_adjoint(which):
+    """The calibration-adjoint configurations, FP64 forward + FP64 adjoint:
+    adjoint128 -- 128^3, 400 steps, checkpoints every 20 steps; adjoint256 -- 256^3,
+    2000 steps, binomial checkpoint/recompute under a 40 GB device-memory cap. Undulated
+    interface, density ratio 0.8. psi_target comes from a run whose five coefficients are
+    scaled by 1 + U(-0.1, 0.1) (seeded); loss L = ||psi(T) - psi_target||^2 (the
+    interface free-energy term of the configuration is left out: lambda = 0). Reports the
+    gradient/forward wall-time ratio, the gradient and, for adjoint128, its error against
+    central finite differences of the FP64 forward (h = 1e-6 relative)."""
+    from smaiso_wcomp_gb300 import abi, ic
+    from smaiso_wcomp_gb300.engine import Engine
+    n, steps = (128, 400) if which == "adjoint128" else (256, 2000)
+    mode = dict(adjoint_ckpt=20) if which == "adjoint128" else dict(adjoint_ckpt=-1, adjoint_cap_gb=40.0)
+    base = abi.default_params(n, rho_0=0.8)
+    psi0, rho0 = ic.undulated_interface(base)
+    u = ic.uniform01(1004, np.arange(len(CAL_COEFFS), dtype=np.uint64))
+    tgt = abi.default_params(n, rho_0=0.8)
+    for c, x in zip(CAL_COEFFS, u):
+        setattr(tgt, c, getattr(tgt, c) * (1.0 + 0.2 * (x - 0.5)))
+    with Engine(tgt) as e:
+        e.set_state(psi0, rho0)
+        e.step(steps)
+        psi_t = e.field("psi")
+
+    def forward(q):
+        with Engine(q) as e:
+            e.set_state(psi0, rho0)
+            e.step(steps)
+            d = e.field("psi") - psi_t
+            return float(np.sum(d * d))
+
+    p = abi.default_params(n, rho_0=0.8, **mode)
+    with Engine(p) as e:
+        e.set_state(psi0, rho0)     # warm-up: graphs, adjoint buffers
+        e.step(2)
+        e.backward(dpsi=np.zeros((n, n, n)))
+        e.set_state(psi0, rho0)
+        t0 = time.perf_counter()
+        e.step(steps)
+        psi_T = e.field("psi")
+        t1 = time.perf_counter()
+        g = e.backward(dpsi=2.0 * (psi_T - psi_t), want_psi0=True)
+        t2 = time.perf_counter()
+    res = {"workload": f"calibration adjoint {n}^3, {steps} steps, FP64 forward + FP64 adjoint, "
+                       + ("checkpoints every 20 steps" if which == "adjoint128" else
+                          "binomial checkpoint/recompute under a 40 GB cap"),
+           "gradient_forward_ratio": (t2 - t1) / (t1 - t0), "forward_s": t1 - t0, "backward_s": t2 - t1,
+           "forward_steps_rerun": g["forward_steps"], "snapshots": g["snapshots"],
+           "gradient": {c: g[c] for c in CAL_COEFFS}}
+    if which == "adjoint128":
+        # central differences with the configuration's h = 1e-6 (relative), and 4th-order
+        # central differences with h = 1e-3 (relative): at h = 1e-6 the FP64 roundoff of
+        # L over 400 steps (~1e-13 |L|) divided by 2h dominates for the small gradients
+        def at(c, x):
+            q = abi.default_params(n, rho_0=0.8)
+            setattr(q, c, x)
+            return forward(q)
+        fd, fd4 = {}, {}
+        for c in CAL_COEFFS:
+            v = getattr(p, c)
+            h = 1e-6 * abs(v)
+            fd[c] = (at(c, v + h) - at(c, v - h)) / (2 * h)
+            h = 1e-3 * abs(v)
+            fd4[c] = (8 * (at(c, v + h) - at(c, v - h)) - (at(c, v + 2 * h) - at(c, v - 2 * h))) / (12 * h)
+        res["fd4_h1e-3"] = fd4
+        res["rel_err_vs_fd4"] = {c: abs(g[c] - fd4[c]) / max(abs(fd4[c]), 1e-300) for c in CAL_COEFFS}
+        d = ic.gaussian_noise((n, n, n), 77, 1.0)
+        with Engine(abi.default_params(n, rho_0=0.8)) as e:
+            def fpsi(x):
+                e.set_state(psi0 + x * d, rho0)
+                e.step(steps)
+                r = e.field("psi") - psi_t
+                return float(np.sum(r * r))
+            fd_psi = (fpsi(1e-6) - fpsi(-1e-6)) / 2e-6
+            h = 1e-3
+            fd4_psi = (8 * (fpsi(h) - fpsi(-h)) - (fpsi(2 * h) - fpsi(-2 * h))) / (12 * h)
+        res["fd"] = fd
+        res["rel_err_vs_fd"] = {c: abs(g[c] - fd[c]) / max(abs(fd[c]), 1e-300) for c in CAL_COEFFS}
+        ad_psi = float(np.sum(g["psi0"] * d))
+        res["psi0_directional"] = {"adjoint": ad_psi, "fd": fd_psi, "rel_err": abs(ad_psi - fd_psi) / abs(fd_psi),
+                                   "fd4_h1e-3": fd4_psi, "rel_err_vs_fd4": abs(ad_psi - fd4_psi) / abs(fd4_psi)}
+    return res
+
+
 def accuracy_run(steps, device=0):
     """Both engines `steps` steps from the same state; relative L2 of psi and rho."""
     from smaiso_wcomp_gb300 import abi
@@ -348,6 +436,9 @@ def main():
         pg = dist
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
+    if args.workload in ("adjoint128", "adjoint256"):
+        print(json.dumps(calibration_adjoint(args.workload)), flush=True)
+        return
     if args.workload == "dislocations":
         print(json.dumps(dislocation_run(args.steps, args.warmup, args.accuracy_steps or 50, local)), flush=True)
         return
