@@ -50,7 +50,7 @@ def parse():
                     help="also run both engines this many steps from the initial state and report psi/rho error")
     ap.add_argument("--grad-steps", type=int, default=40,
                     help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
-    ap.add_argument("--workload", choices=["undulated", "dislocations", "adjoint128", "adjoint256"],
+    ap.add_argument("--workload", choices=["undulated", "dislocations", "adjoint128", "adjoint256", "adjoint256_fp64"],
                     default="undulated",
                     help="dislocations: the 512x512x256 layer-dislocation configuration, reported as "
                          "its own JSON line (mixed and FP64 steps/s, mixed-vs-FP64 errors)")
@@ -244,9 +244,10 @@ CAL_COEFFS = ("alpha", "beta", "gamma", "nu", "rho_0")
 
 
 def calibration_adjoint(which):
-    """The calibration-adjoint configurations, FP64 forward + FP64 adjoint:
-    adjoint128 -- 128^3, 400 steps, checkpoints every 20 steps; adjoint256 -- 256^3,
-    2000 steps, binomial checkpoint/recompute under a 40 GB device-memory cap. Undulated
+    """The calibration-adjoint configurations: adjoint128 -- FP64 forward + FP64 adjoint,
+    128^3, 400 steps, checkpoints every 20 steps; adjoint256 -- mixed forward + FP32
+    adjoint, 256^3, 2000 steps, binomial checkpoint/recompute under a 40 GB device-memory
+    cap (adjoint256_fp64: the same with the FP64 engine). Undulated
     interface, density ratio 0.8. psi_target comes from a run whose five coefficients are
     scaled by 1 + U(-0.1, 0.1) (seeded); loss L = ||psi(T) - psi_target||^2 (the
     interface free-energy term of the configuration is left out: lambda = 0). Reports the
@@ -255,11 +256,13 @@ def calibration_adjoint(which):
     from smaiso_wcomp_gb300 import abi, ic
     from smaiso_wcomp_gb300.engine import Engine
     n, steps = (128, 400) if which == "adjoint128" else (256, 2000)
+    prec = abi.SWC_PREC_MIXED if which == "adjoint256" else abi.SWC_PREC_FP64
     mode = dict(adjoint_ckpt=20) if which == "adjoint128" else dict(adjoint_ckpt=-1, adjoint_cap_gb=40.0)
+    mode["precision"] = prec
     base = abi.default_params(n, rho_0=0.8)
     psi0, rho0 = ic.undulated_interface(base)
     u = ic.uniform01(1004, np.arange(len(CAL_COEFFS), dtype=np.uint64))
-    tgt = abi.default_params(n, rho_0=0.8)
+    tgt = abi.default_params(n, rho_0=0.8, precision=prec)
     for c, x in zip(CAL_COEFFS, u):
         setattr(tgt, c, getattr(tgt, c) * (1.0 + 0.2 * (x - 0.5)))
     with Engine(tgt) as e:
@@ -286,11 +289,14 @@ def calibration_adjoint(which):
         t1 = time.perf_counter()
         g = e.backward(dpsi=2.0 * (psi_T - psi_t), want_psi0=True)
         t2 = time.perf_counter()
-    res = {"workload": f"calibration adjoint {n}^3, {steps} steps, FP64 forward + FP64 adjoint, "
+    res = {"workload": f"calibration adjoint {n}^3, {steps} steps, "
+                       + ("mixed forward + FP32 adjoint, " if prec == abi.SWC_PREC_MIXED else
+                          "FP64 forward + FP64 adjoint, ")
                        + ("checkpoints every 20 steps" if which == "adjoint128" else
                           "binomial checkpoint/recompute under a 40 GB cap"),
            "gradient_forward_ratio": (t2 - t1) / (t1 - t0), "forward_s": t1 - t0, "backward_s": t2 - t1,
            "forward_steps_rerun": g["forward_steps"], "snapshots": g["snapshots"],
+           "adjoint_step_over_forward_step": ((t2 - t1) - g["forward_steps"] * (t1 - t0) / steps) / (t1 - t0),
            "gradient": {c: g[c] for c in CAL_COEFFS}}
     if which == "adjoint128":
         # central differences with the configuration's h = 1e-6 (relative), and 4th-order
@@ -317,13 +323,13 @@ def calibration_adjoint(which):
                 r = e.field("psi") - psi_t
                 return float(np.sum(r * r))
             fd_psi = (fpsi(1e-6) - fpsi(-1e-6)) / 2e-6
-            h = 1e-3
+            h = 1e-4
             fd4_psi = (8 * (fpsi(h) - fpsi(-h)) - (fpsi(2 * h) - fpsi(-2 * h))) / (12 * h)
         res["fd"] = fd
         res["rel_err_vs_fd"] = {c: abs(g[c] - fd[c]) / max(abs(fd[c]), 1e-300) for c in CAL_COEFFS}
         ad_psi = float(np.sum(g["psi0"] * d))
         res["psi0_directional"] = {"adjoint": ad_psi, "fd": fd_psi, "rel_err": abs(ad_psi - fd_psi) / abs(fd_psi),
-                                   "fd4_h1e-3": fd4_psi, "rel_err_vs_fd4": abs(ad_psi - fd4_psi) / abs(fd4_psi)}
+                                   "fd4_h1e-4": fd4_psi, "rel_err_vs_fd4": abs(ad_psi - fd4_psi) / abs(fd4_psi)}
     return res
 
 
@@ -436,7 +442,7 @@ def main():
         pg = dist
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
-    if args.workload in ("adjoint128", "adjoint256"):
+    if args.workload in ("adjoint128", "adjoint256", "adjoint256_fp64"):
         print(json.dumps(calibration_adjoint(args.workload)), flush=True)
         return
     if args.workload == "dislocations":

@@ -115,12 +115,14 @@ typedef struct swc_params {
   double watchdog_s;  /* host watchdog per swc_step call in seconds (<=0: none) */
   int adjoint_ckpt;   /* 0: no adjoint. K > 0 (FP64 engine): swc_step keeps a state
                          checkpoint every K steps so swc_backward can recompute the
-                         trajectory; device memory = (steps/K + 1) states of 6 N^3
-                         doubles + one segment tape of K x 24 N^3 doubles.
-                         -1 (FP64 engine): binomial checkpointing -- swc_step keeps only
-                         the initial state and swc_backward reverses the trajectory with
-                         a binomial recompute schedule over as many 6 N^3-double state
-                         snapshots as fit under adjoint_cap_gb, with a one-step tape. */
+                         trajectory; device memory = (steps/K + 2) states of 3 N^3
+                         doubles + 3 N^3 values + one segment tape of K x 24 N^3 values
+                         (values: double in the FP64 engine, float in the mixed one,
+                         whose adjoint runs in FP32).
+                         -1: binomial checkpointing -- swc_step keeps only the initial
+                         state and swc_backward reverses the trajectory with a binomial
+                         recompute schedule over as many state snapshots as fit under
+                         adjoint_cap_gb, with a one-step tape. */
   double adjoint_cap_gb; /* adjoint_ckpt = -1: device memory cap of the context during
                             swc_backward, in GB (1e9 B), engine arrays included; <= 0:
                             the device's free memory at the call less 1 GB. */
@@ -260,8 +262,9 @@ int swc_diagnostics_noalloc(const swc_params* p, const double* psi, const double
  * update). Recomputes the trajectory segment by segment from the checkpoints kept
  * by swc_step (params.adjoint_ckpt). Outputs dL/dpsi0 and dL/drho0 with respect to
  * the arrays passed to swc_set_state (host, nx*ny*nz doubles, either may be NULL)
- * and the coefficient gradients in *grad. FP64 engine only; the context's state is
- * the state at step T again when the call returns. */
+ * and the coefficient gradients in *grad. The FP64 engine differentiates in FP64, the
+ * mixed engine in FP32 (on its own trajectory); the context's state is the state at
+ * step T again when the call returns. */
 int swc_backward(swc_ctx* ctx, const double* dL_dpsi, const double* dL_drho, double* dL_dpsi0,
                  double* dL_drho0, swc_grad* grad);
 

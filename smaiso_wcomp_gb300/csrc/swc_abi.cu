@@ -106,8 +106,8 @@ int validate_params(const swc_params* p) {
     set_error("ref_ranks=%d must be >= 1 and divide nx=%d", p->ref_ranks, p->nx);
     return SWC_ERR_BAD_PARAM;
   }
-  if (p->adjoint_ckpt < -1 || (p->adjoint_ckpt != 0 && p->precision != SWC_PREC_FP64)) {
-    set_error("adjoint_ckpt must be -1 (binomial), 0 or K > 0, and needs precision SWC_PREC_FP64");
+  if (p->adjoint_ckpt < -1) {
+    set_error("adjoint_ckpt must be -1 (binomial), 0 or K > 0");
     return SWC_ERR_BAD_PARAM;
   }
   if (p->divv_switch < 0 || (p->precision != SWC_PREC_FP64 && p->precision != SWC_PREC_MIXED) || p->device < 0) {

@@ -34,20 +34,20 @@ enum {
 template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_steps) {
   const size_t ng = (size_t)g_.ng;
   if (!adj_) {
-    if (cudaMalloc(&adj_, (size_t)kAdj * ng * sizeof(double)) != cudaSuccess ||
+    if (cudaMalloc(&adj_, (size_t)kAdj * ng * sizeof(T)) != cudaSuccess ||
         cudaMalloc(&pgrad_, pgrad_doubles() * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
-      set_error("cudaMalloc of the adjoint work arrays failed (%zu MB)", (kAdj * ng * 8) >> 20);
+      set_error("cudaMalloc of the adjoint work arrays failed (%zu MB)", (kAdj * ng * sizeof(T)) >> 20);
       return SWC_ERR_OOM;
     }
   }
   if (tape_steps_ < tape_steps) {
     if (tape_) cudaFree(tape_);
     tape_ = nullptr;
-    if (cudaMalloc(&tape_, tape_steps * (size_t)kTape * ng * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&tape_, tape_steps * (size_t)kTape * ng * sizeof(T)) != cudaSuccess) {
       cudaGetLastError();
       tape_steps_ = 0;
-      set_error("cudaMalloc of the adjoint tape failed (%zu MB)", (tape_steps * kTape * ng * 8) >> 20);
+      set_error("cudaMalloc of the adjoint tape failed (%zu MB)", (tape_steps * kTape * ng * sizeof(T)) >> 20);
       return SWC_ERR_OOM;
     }
     tape_steps_ = tape_steps;
@@ -58,77 +58,79 @@ template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_steps) {
 template <typename T>
 int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   const size_t ng = (size_t)g_.ng;
-  const double* tp = tape_ + slot * (size_t)kTape * ng;
+  const T* tp = tape_ + slot * (size_t)kTape * ng;
   auto TP = [&](int q) { return tp + (size_t)q * ng; };
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
   const unsigned blocks = (unsigned)((g_.ng + 255) / 256);
-  const AdjScalars sc{p_.ep, p_.alpha, p_.beta, p_.gamma, p_.zeta, kp_, p_.rho_0, p_.q0 * p_.q0, p_.dt,
-                      p_.dt / 2, rho_m_, scale_, p_.nu, p_.lambda + 2 * p_.nu};
-  using LP = LdPlain<double, double>;
-  using SP = StPlain<double, double>;
-  const AxisWeights w2{{0, 0, 0}, 2.0}, wh{{0, 0, 0}, 0.5};
-  auto sine_w = [](int ax, double w) { AxisWeights a{{ax == 0, ax == 1, ax == 2}, w}; return a; };
+  const AdjScalars<T> sc{(T)p_.ep, (T)p_.alpha, (T)p_.beta, (T)p_.gamma, (T)p_.zeta, (T)kp_, (T)p_.rho_0,
+                         (T)(p_.q0 * p_.q0), (T)p_.dt, (T)(p_.dt / 2), (T)rho_m_, (T)scale_, (T)p_.nu,
+                         (T)(p_.lambda + 2 * p_.nu)};
+  using LP = LdPlain<T, T>;
+  using SP = StPlain<T, T>;
+  const AxisWeights<T> w2{{0, 0, 0}, (T)2.0}, wh{{0, 0, 0}, (T)0.5};
+  auto sine_w = [](int ax, double w) { AxisWeights<T> a{{ax == 0, ax == 1, ax == 2}, (T)w}; return a; };
 
   // (1) CN/AB2 update (REF:2177-2190)
-  adj_cn_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], sc, first ? 1 : 0, TP(TP_QOLD),
+  adj_cn_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], sc, first ? 1 : 0, TP(TP_QOLD),
                                              TP(TP_QNEW), AJ(AJ_Q), AJ(AJ_QO), AJ(AJ_NLO), AJ(AJ_NL), pgrad_);
   SWC_CK(cudaGetLastError());
   // (2) grad.f subtracted in spectral space, then Nl-hat = DCT-II^3 Nl -> Nl_bar = DCT-III^3 D0 Nlq_bar
-  adj_dq_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], AJ(AJ_NL), AJ(AJ_FX), AJ(AJ_FY),
+  adj_dq_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], AJ(AJ_NL), AJ(AJ_FX), AJ(AJ_FY),
                                              AJ(AJ_FZ));
   SWC_CK(cudaGetLastError());
-  SWC_TRY((pass<K_C3, 2>(LdW{g_, AJ(AJ_NL), w2}, SP{AJ(AJ_NL)})));
+  SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, AJ(AJ_NL), w2}, SP{AJ(AJ_NL)})));
   SWC_TRY((pass<K_C3, 1>(LP{AJ(AJ_NL)}, SP{AJ(AJ_NL)})));
   SWC_TRY((pass<K_C3, 0>(LP{AJ(AJ_NL)}, SP{AJ(AJ_NL)})));
   // (3) density update + Nl in real space (REF:2121-2160)
   {
-    AdjNlArgs a{AJ(AJ_NL), TP(TP_PSI), TP(TP_A), TP(TP_RHOIN), TP(TP_RHONEW), TP(TP_VX), TP(TP_VY), TP(TP_VZ),
+    AdjNlArgs<T> a{AJ(AJ_NL), TP(TP_PSI), TP(TP_A), TP(TP_RHOIN), TP(TP_RHONEW), TP(TP_VX), TP(TP_VY), TP(TP_VZ),
                 TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ), TP(TP_GRX), TP(TP_GRY), TP(TP_GRZ), TP(TP_DIVV),
                 adj_ + AJ_R * ng, adj_ + AJ_F * ng, adj_ + AJ_MU * ng, adj_ + AJ_A * ng, adj_ + AJ_PSI * ng,
                 adj_ + AJ_VX * ng, adj_ + AJ_VY * ng, adj_ + AJ_VZ * ng, adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng,
                 adj_ + AJ_GPZ * ng, adj_ + AJ_GRX * ng, adj_ + AJ_GRY * ng, adj_ + AJ_GRZ * ng,
                 adj_ + AJ_DIVV * ng, pgrad_, sc, relax ? 1 : 0};
-    adj_nl_kernel<<<blocks, 256, 0, stream_>>>(g_, a);
+    adj_nl_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
   }
   // (4) divv = DCT-III^3 divv-hat -> divv-hat_bar = D0^-1 DCT-II^3 divv_bar;
   //     v_a = inverse mixed of v-hat_a -> v-hat_bar = W^-1 forward-mixed(v_bar)
   SWC_TRY((pass<K_C2, 2>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
   SWC_TRY((pass<K_C2, 1>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
-  SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_DIVV)}, StW{g_, adj_ + AJ_DIVV * ng, wh, 0})));
+  SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_DIVV)}, StW<T>{g_, adj_ + AJ_DIVV * ng, wh, 0})));
   {
-    double* bv[3] = {adj_ + AJ_VX * ng, adj_ + AJ_VY * ng, adj_ + AJ_VZ * ng};
+    T* bv[3] = {adj_ + AJ_VX * ng, adj_ + AJ_VY * ng, adj_ + AJ_VZ * ng};
     SWC_TRY((pass<K_C2, 2>(LP{bv[0]}, SP{bv[0]})));
     SWC_TRY((pass<K_C2, 1>(LP{bv[0]}, SP{bv[0]})));
-    SWC_TRY((pass<K_S2, 0>(LP{bv[0]}, StW{g_, bv[0], sine_w(0, 0.5), 0})));
+    SWC_TRY((pass<K_S2, 0>(LP{bv[0]}, StW<T>{g_, bv[0], sine_w(0, 0.5), 0})));
     SWC_TRY((pass<K_C2, 2>(LP{bv[1]}, SP{bv[1]})));
     SWC_TRY((pass<K_S2, 1>(LP{bv[1]}, SP{bv[1]})));
-    SWC_TRY((pass<K_C2, 0>(LP{bv[1]}, StW{g_, bv[1], sine_w(1, 0.5), 0})));
+    SWC_TRY((pass<K_C2, 0>(LP{bv[1]}, StW<T>{g_, bv[1], sine_w(1, 0.5), 0})));
     SWC_TRY((pass<K_S2, 2>(LP{bv[2]}, SP{bv[2]})));
     SWC_TRY((pass<K_C2, 1>(LP{bv[2]}, SP{bv[2]})));
-    SWC_TRY((pass<K_C2, 0>(LP{bv[2]}, StW{g_, bv[2], sine_w(2, 0.5), 0})));
+    SWC_TRY((pass<K_C2, 0>(LP{bv[2]}, StW<T>{g_, bv[2], sine_w(2, 0.5), 0})));
   }
   // (5) Stokes solve + divergence (REF:1468-2078)
   {
-    AdjStokesArgs a{AJ(AJ_VX), AJ(AJ_VY), AJ(AJ_VZ), AJ(AJ_DIVV), TP(TP_VSX), TP(TP_VSY), TP(TP_VSZ), TP(TP_VIX),
+    AdjStokesArgs<T> a{AJ(AJ_VX), AJ(AJ_VY), AJ(AJ_VZ), AJ(AJ_DIVV), TP(TP_VSX), TP(TP_VSY), TP(TP_VSZ), TP(TP_VIX),
                     TP(TP_VIY), TP(TP_VIZ), adj_ + AJ_DOTX * ng, adj_ + AJ_DOTY * ng, adj_ + AJ_DOTZ * ng,
                     adj_ + AJ_SDX * ng, adj_ + AJ_SDY * ng, adj_ + AJ_SDZ * ng, adj_ + AJ_FGPX * ng,
                     adj_ + AJ_FGPY * ng, adj_ + AJ_FGPZ * ng, vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2],
-                    gq_[0], gq_[1], gq_[2], gs_[0], gs_[1], gs_[2], scale_, 1.0 / p_.nu,
-                    1.0 / (p_.lambda + 2 * p_.nu), p_.nu, p_.lambda + 2 * p_.nu, p_.nx / p_.ref_ranks, pgrad_};
-    adj_stokes1_kernel<<<blocks, 256, 0, stream_>>>(g_, a);
+                    gq_[0], gq_[1], gq_[2], gs_[0], gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu),
+                    (T)(1.0 / (p_.lambda + 2 * p_.nu)), (T)p_.nu, (T)(p_.lambda + 2 * p_.nu), p_.nx / p_.ref_ranks,
+                    pgrad_};
+    adj_stokes1_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
-    AdjStokes2Args b{AJ(AJ_DOTX), AJ(AJ_DOTY), AJ(AJ_DOTZ), AJ(AJ_SDX), AJ(AJ_SDY), AJ(AJ_SDZ), AJ(AJ_FGPX),
+    AdjStokes2Args<T> b{AJ(AJ_DOTX), AJ(AJ_DOTY), AJ(AJ_DOTZ), AJ(AJ_SDX), AJ(AJ_SDY), AJ(AJ_SDZ), AJ(AJ_FGPX),
                      AJ(AJ_FGPY), AJ(AJ_FGPZ), adj_ + AJ_SX * ng, adj_ + AJ_SY * ng, adj_ + AJ_SZ * ng,
                      adj_ + AJ_FG * ng, adj_ + AJ_E * ng, vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2],
                      gq_[0], gq_[1], gq_[2]};
-    adj_stokes2_kernel<<<blocks, 256, 0, stream_>>>(g_, b);
+    adj_stokes2_kernel<T><<<blocks, 256, 0, stream_>>>(g_, b);
     SWC_CK(cudaGetLastError());
   }
   // (6) forward transforms of S7 (REF:1427-1457) transposed: DCT-II^T = DCT-III D0,
   //     DST-II^T = DST-III DL, applied in place to the spectral cotangents
-  auto cos_t = [&](double* b) -> int {
-    SWC_TRY((pass<K_C3, 2>(LdW{g_, b, w2}, SP{b})));
+  auto cos_t = [&](T* b) -> int {
+    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, b, w2}, SP{b})));
     SWC_TRY((pass<K_C3, 1>(LP{b}, SP{b})));
     SWC_TRY((pass<K_C3, 0>(LP{b}, SP{b})));
     return SWC_OK;
@@ -136,119 +138,164 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   SWC_TRY(cos_t(adj_ + AJ_FG * ng));
   SWC_TRY(cos_t(adj_ + AJ_E * ng));
   for (int c = 0; c < 2; ++c) {
-    double* bx = adj_ + (c == 0 ? AJ_SX : AJ_FX) * ng;
-    double* by = adj_ + (c == 0 ? AJ_SY : AJ_FY) * ng;
-    double* bz = adj_ + (c == 0 ? AJ_SZ : AJ_FZ) * ng;
-    SWC_TRY((pass<K_C3, 2>(LdW{g_, bx, sine_w(0, 2.0)}, SP{bx})));
+    T* bx = adj_ + (c == 0 ? AJ_SX : AJ_FX) * ng;
+    T* by = adj_ + (c == 0 ? AJ_SY : AJ_FY) * ng;
+    T* bz = adj_ + (c == 0 ? AJ_SZ : AJ_FZ) * ng;
+    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, bx, sine_w(0, 2.0)}, SP{bx})));
     SWC_TRY((pass<K_C3, 1>(LP{bx}, SP{bx})));
     SWC_TRY((pass<K_S3, 0>(LP{bx}, SP{bx})));
-    SWC_TRY((pass<K_C3, 2>(LdW{g_, by, sine_w(1, 2.0)}, SP{by})));
+    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, by, sine_w(1, 2.0)}, SP{by})));
     SWC_TRY((pass<K_S3, 1>(LP{by}, SP{by})));
     SWC_TRY((pass<K_C3, 0>(LP{by}, SP{by})));
-    SWC_TRY((pass<K_S3, 2>(LdW{g_, bz, sine_w(2, 2.0)}, SP{bz})));
+    SWC_TRY((pass<K_S3, 2>(LdW<T>{g_, bz, sine_w(2, 2.0)}, SP{bz})));
     SWC_TRY((pass<K_C3, 1>(LP{bz}, SP{bz})));
     SWC_TRY((pass<K_C3, 0>(LP{bz}, SP{bz})));
   }
   // (7) S6 and the relax reset (REF:1363-1425)
   {
-    AdjS6Args a{AJ(AJ_FG), AJ(AJ_E), AJ(AJ_SX), AJ(AJ_SY), AJ(AJ_SZ), AJ(AJ_FX), AJ(AJ_FY), AJ(AJ_FZ), AJ(AJ_MU),
+    AdjS6Args<T> a{AJ(AJ_FG), AJ(AJ_E), AJ(AJ_SX), AJ(AJ_SY), AJ(AJ_SZ), AJ(AJ_FX), AJ(AJ_FY), AJ(AJ_FZ), AJ(AJ_MU),
                 TP(TP_LAPR), TP(TP_RHOIN), TP(TP_L), TP(TP_PSI), TP(TP_A), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ),
                 TP(TP_GRX), TP(TP_GRY), TP(TP_GRZ), adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng, adj_ + AJ_GPZ * ng,
                 adj_ + AJ_GRX * ng, adj_ + AJ_GRY * ng, adj_ + AJ_GRZ * ng, adj_ + AJ_A * ng, adj_ + AJ_PSI * ng,
                 adj_ + AJ_R * ng, adj_ + AJ_LAPR * ng, adj_ + AJ_L * ng, pgrad_, sc, relax ? 1 : 0};
-    adj_s6_kernel<<<blocks, 256, 0, stream_>>>(g_, a);
+    adj_s6_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
   }
   // (8) S5 (REF:1312-1380)
-  double* blap = adj_ + AJ_LAPR * ng;
+  T* blap = adj_ + AJ_LAPR * ng;
   if (!relax) {
     // lapR = Delta_s(rho L), Delta_s = DCT-III^3 (-scale q^2) DCT-II^3 is symmetric
     SWC_TRY((pass<K_C2, 2>(LP{blap}, SP{blap})));
     SWC_TRY((pass<K_C2, 1>(LP{blap}, SP{blap})));
-    SWC_TRY((pass<K_FILT, 0>(LP{blap}, SP{blap}, MulLap<double>{vq_[0], vq_[1], vq_[2], scale_})));
+    SWC_TRY((pass<K_FILT, 0>(LP{blap}, SP{blap}, MulLap<T>{vq_[0], vq_[1], vq_[2], (T)scale_})));
     SWC_TRY((pass<K_C3, 1>(LP{blap}, SP{blap})));
-    SWC_TRY((pass<K_C3, 2>(LP{blap}, StAdjLap{TP(TP_L), TP(TP_RHOIN), adj_ + AJ_R * ng, adj_ + AJ_L * ng})));
+    SWC_TRY((pass<K_C3, 2>(LP{blap}, StAdjLap<T>{TP(TP_L), TP(TP_RHOIN), adj_ + AJ_R * ng, adj_ + AJ_L * ng})));
   } else {
     // lapR_raw = DCT-III^3 (-q^2 alpha (q0^2 - q^2) psiq)
     SWC_TRY((pass<K_C2, 2>(LP{blap}, SP{blap})));
     SWC_TRY((pass<K_C2, 1>(LP{blap}, SP{blap})));
-    SWC_TRY((pass<K_C2, 0>(LP{blap}, StW{g_, blap, wh, 0})));
-    adj_acc_spec_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], 1, p_.alpha, p_.q0 * p_.q0,
+    SWC_TRY((pass<K_C2, 0>(LP{blap}, StW<T>{g_, blap, wh, 0})));
+    adj_acc_spec_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], 1, p_.alpha, p_.q0 * p_.q0,
                                                      blap, TP(TP_QOLD), AJ(AJ_Q), pgrad_);
     SWC_CK(cudaGetLastError());
   }
   // (9) dfDlapPsi = DCT-III^3 (alpha (q0^2 - q^2) psiq)  (REF:1293-1308)
   {
-    double* bl = adj_ + AJ_L * ng;
+    T* bl = adj_ + AJ_L * ng;
     SWC_TRY((pass<K_C2, 2>(LP{bl}, SP{bl})));
     SWC_TRY((pass<K_C2, 1>(LP{bl}, SP{bl})));
-    SWC_TRY((pass<K_C2, 0>(LP{bl}, StW{g_, bl, wh, 0})));
-    adj_acc_spec_kernel<<<blocks, 256, 0, stream_>>>(g_, vqd_[0], vqd_[1], vqd_[2], 0, p_.alpha, p_.q0 * p_.q0, bl,
+    SWC_TRY((pass<K_C2, 0>(LP{bl}, StW<T>{g_, bl, wh, 0})));
+    adj_acc_spec_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], 0, p_.alpha, p_.q0 * p_.q0, bl,
                                                      TP(TP_QOLD), AJ(AJ_Q), pgrad_);
     SWC_CK(cudaGetLastError());
   }
   // (10) amplitude filter A = F(A_raw) (symmetric) and A_raw = |psi, grad psi| (REF:1254-1289)
   {
-    double* bA = adj_ + AJ_A * ng;
+    T* bA = adj_ + AJ_A * ng;
     SWC_TRY((pass<K_C2, 2>(LP{bA}, SP{bA})));
     SWC_TRY((pass<K_C2, 1>(LP{bA}, SP{bA})));
-    SWC_TRY((pass<K_FILT, 0>(LP{bA}, SP{bA}, MulGauss<double>{gq_[0], gq_[1], gq_[2], scale_})));
+    SWC_TRY((pass<K_FILT, 0>(LP{bA}, SP{bA}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
     SWC_TRY((pass<K_C3, 1>(LP{bA}, SP{bA})));
-    SWC_TRY((pass<K_C3, 2>(LP{bA}, StAdjAmp{TP(TP_PSI), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ), adj_ + AJ_PSI * ng,
+    SWC_TRY((pass<K_C3, 2>(LP{bA}, StAdjAmp<T>{TP(TP_PSI), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ), adj_ + AJ_PSI * ng,
                                             adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng, adj_ + AJ_GPZ * ng,
-                                            p_.q0 * p_.q0})));
+                                            (T)(p_.q0 * p_.q0)})));
   }
   // (11) gradients (REF:1166-1250): grad_a = inverse-mixed(-fac Vs shift X); transpose =
   //      forward-mixed, output weights, then the shifted scatter into X_bar
-  SWC_CK(cudaMemsetAsync(adj_ + AJ_RQ * ng, 0, ng * sizeof(double), stream_));
+  SWC_CK(cudaMemsetAsync(adj_ + AJ_RQ * ng, 0, ng * sizeof(T), stream_));
   const long long sx = 1LL << (g_.ly + g_.lz), sy = g_.nz;
   for (int which = 0; which < 2; ++which) {
-    double* target = which == 0 ? adj_ + AJ_Q * ng : adj_ + AJ_RQ * ng;
-    const double fac = which == 0 ? 1.0 : scale_;
-    double* bgx = adj_ + (which == 0 ? AJ_GPX : AJ_GRX) * ng;
-    double* bgy = adj_ + (which == 0 ? AJ_GPY : AJ_GRY) * ng;
-    double* bgz = adj_ + (which == 0 ? AJ_GPZ : AJ_GRZ) * ng;
+    T* target = which == 0 ? adj_ + AJ_Q * ng : adj_ + AJ_RQ * ng;
+    const T fac = which == 0 ? (T)1.0 : (T)scale_;
+    T* bgx = adj_ + (which == 0 ? AJ_GPX : AJ_GRX) * ng;
+    T* bgy = adj_ + (which == 0 ? AJ_GPY : AJ_GRY) * ng;
+    T* bgz = adj_ + (which == 0 ? AJ_GPZ : AJ_GRZ) * ng;
     SWC_TRY((pass<K_C2, 2>(LP{bgx}, SP{bgx})));
     SWC_TRY((pass<K_C2, 1>(LP{bgx}, SP{bgx})));
-    SWC_TRY((pass<K_S2, 0>(LP{bgx}, StAdjGrad{g_, target, vs_[0], fac, 0, sx, sine_w(0, 0.5)})));
+    SWC_TRY((pass<K_S2, 0>(LP{bgx}, StAdjGrad<T>{g_, target, vs_[0], fac, 0, sx, sine_w(0, 0.5)})));
     SWC_TRY((pass<K_C2, 2>(LP{bgy}, SP{bgy})));
     SWC_TRY((pass<K_S2, 1>(LP{bgy}, SP{bgy})));
-    SWC_TRY((pass<K_C2, 0>(LP{bgy}, StAdjGrad{g_, target, vs_[1], fac, 1, sy, sine_w(1, 0.5)})));
+    SWC_TRY((pass<K_C2, 0>(LP{bgy}, StAdjGrad<T>{g_, target, vs_[1], fac, 1, sy, sine_w(1, 0.5)})));
     SWC_TRY((pass<K_S2, 2>(LP{bgz}, SP{bgz})));
     SWC_TRY((pass<K_C2, 1>(LP{bgz}, SP{bgz})));
-    SWC_TRY((pass<K_C2, 0>(LP{bgz}, StAdjGrad{g_, target, vs_[2], fac, 2, 1, sine_w(2, 0.5)})));
+    SWC_TRY((pass<K_C2, 0>(LP{bgz}, StAdjGrad<T>{g_, target, vs_[2], fac, 2, 1, sine_w(2, 0.5)})));
   }
   // (12) rho-hat = DCT-II^3 rho (REF:1104-1106): rho_bar += DCT-III^3 D0 rhoq_bar
   {
-    double* rq = adj_ + AJ_RQ * ng;
-    SWC_TRY((pass<K_C3, 2>(LdW{g_, rq, w2}, SP{rq})));
+    T* rq = adj_ + AJ_RQ * ng;
+    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, rq, w2}, SP{rq})));
     SWC_TRY((pass<K_C3, 1>(LP{rq}, SP{rq})));
-    SWC_TRY((pass<K_C3, 0>(LP{rq}, StAcc{adj_ + AJ_R * ng})));
+    SWC_TRY((pass<K_C3, 0>(LP{rq}, StAcc<T>{adj_ + AJ_R * ng})));
   }
   // (13) the step's psi = DCT-III^3 psiq: psiq_bar += D0^-1 DCT-II^3 psi_bar
   {
-    double* bp = adj_ + AJ_PSI * ng;
+    T* bp = adj_ + AJ_PSI * ng;
     SWC_TRY((pass<K_C2, 2>(LP{bp}, SP{bp})));
     SWC_TRY((pass<K_C2, 1>(LP{bp}, SP{bp})));
-    SWC_TRY((pass<K_C2, 0>(LP{bp}, StW{g_, adj_ + AJ_Q * ng, wh, 1})));
+    SWC_TRY((pass<K_C2, 0>(LP{bp}, StW<T>{g_, adj_ + AJ_Q * ng, wh, 1})));
+  }
+  return SWC_OK;
+}
+
+// Host FP64 field <-> device field of the engine's precision (the mixed engine goes
+// through the FP64 staging buffer and narrows / widens on the device).
+template <typename T> int StepEngine<T>::host_to_field(const double* src, T* dst) {
+  const size_t ng = (size_t)g_.ng;
+  if constexpr (std::is_same<T, double>::value) {
+    SWC_CK(cudaMemcpyAsync(dst, src, ng * 8, cudaMemcpyHostToDevice, stream_));
+  } else {
+    SWC_TRY(stage_alloc());
+    SWC_CK(cudaMemcpyAsync(stage_, src, ng * 8, cudaMemcpyHostToDevice, stream_));
+    narrow_kernel<<<(unsigned)((ng / 4 + 255) / 256), 256, 0, stream_>>>(stage_, dst, (long long)ng);
+    SWC_CK(cudaGetLastError());
+  }
+  return SWC_OK;
+}
+template <typename T> int StepEngine<T>::field_to_host(const T* src, double* dst) {
+  const size_t ng = (size_t)g_.ng;
+  if constexpr (std::is_same<T, double>::value) {
+    SWC_CK(cudaMemcpyAsync(dst, src, ng * 8, cudaMemcpyDeviceToHost, stream_));
+  } else {
+    SWC_TRY(stage_alloc());
+    widen_kernel<<<(unsigned)((ng / 4 + 255) / 256), 256, 0, stream_>>>(src, stage_, (long long)ng);
+    SWC_CK(cudaGetLastError());
+    SWC_CK(cudaMemcpyAsync(dst, stage_, ng * 8, cudaMemcpyDeviceToHost, stream_));
   }
   return SWC_OK;
 }
 
 // Step n (1-based) from the loaded state n-1 with its tape (slot 0), then its adjoint.
 template <typename T> int StepEngine<T>::tape_and_adjoint(int64_t n) {
+  SWC_TRY(record_tape(tape_, n));
+  const bool relax = !(n > p_.divv_switch || p_.load == 1);
+  return adjoint_step(0, relax, n == 1);
+}
+
+// Run step n (1-based) from the loaded state n-1 and copy the fields its adjoint reads
+// into the tape slot tp; the mixed engine's FP64 state fields are narrowed to FP32.
+template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n) {
   const size_t ng = (size_t)g_.ng;
-  double* tp = tape_;
-  SWC_CK(cudaMemcpyAsync(tp + TP_RHOIN * ng, rho_, ng * 8, cudaMemcpyDeviceToDevice, stream_));
+  constexpr bool mixed = !std::is_same<T, double>::value;
+  auto put = [&](int q, const void* src, bool is_double) -> int {
+    if (mixed && is_double) {
+      narrow_kernel<<<(unsigned)((ng / 4 + 255) / 256), 256, 0, stream_>>>((const double*)src, (float*)(tp + q * ng),
+                                                                           (long long)ng);
+      SWC_CK(cudaGetLastError());
+    } else {
+      SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src, ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+    }
+    return SWC_OK;
+  };
+  SWC_TRY(put(TP_RHOIN, rho_, true));
   const bool relax = !(n > p_.divv_switch || p_.load == 1);
   SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old and v_sol
   const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
                             amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
                             vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
   for (int q = 0; q < kTape; ++q)
-    if (src[q]) SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src[q], ng * 8, cudaMemcpyDeviceToDevice, stream_));
+    if (src[q]) SWC_TRY(put(q, src[q], q == TP_QOLD || q == TP_QNEW || q == TP_RHONEW));
   ++fwd_steps_;
-  return adjoint_step(0, relax, n == 1);
+  return SWC_OK;
 }
 
 // k plain forward steps from the loaded state `from` (steps from+1 .. from+k).
@@ -302,7 +349,7 @@ int StepEngine<T>::reverse_binomial(int64_t l, int64_t n, size_t sl, size_t ff, 
 }
 
 template <typename T>
-int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double* dpsi0, double* drho0,
+int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0,
                                  swc_grad* out) {
   const int K = p_.adjoint_ckpt;
   if (K == 0) {
@@ -329,9 +376,9 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
   int64_t nsnap = 0;
   if (binomial) {
     // snapshot slots under the cap: engine arrays + adjoint work + tape + slots 0, 1 + s
-    const size_t slot_bytes = 6 * ng * sizeof(double);
-    const size_t used = engine_bytes_ + (size_t)kAdj * ng * 8 + pgrad_doubles() * 8 + (size_t)kTape * ng * 8 +
-                        ckpt_.size() * slot_bytes;
+    const size_t slot_bytes = ckpt_slot_bytes();
+    const size_t used = engine_bytes_ + (size_t)kAdj * ng * sizeof(T) + pgrad_doubles() * 8 +
+                        (size_t)kTape * ng * sizeof(T) + ckpt_.size() * slot_bytes + (stage_ ? ng * 8 : 0);
     double cap = p_.adjoint_cap_gb * 1e9;
     if (cap <= 0) {
       size_t fr = 0, tot = 0;
@@ -349,19 +396,19 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
   }
   fwd_steps_ = 0;
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
-  SWC_CK(cudaMemsetAsync(adj_, 0, (size_t)kAdj * ng * sizeof(double), stream_));
+  SWC_CK(cudaMemsetAsync(adj_, 0, (size_t)kAdj * ng * sizeof(T), stream_));
   SWC_CK(cudaMemsetAsync(pgrad_, 0, pgrad_doubles() * sizeof(double), stream_));
   // cotangent of the final state: psi(T) = DCT-III^3 psiq(T), rho(T)
   if (dpsi) {
-    SWC_CK(cudaMemcpyAsync(AJ(AJ_PSI), dpsi, ng * 8, cudaMemcpyHostToDevice, stream_));
-    using LP = LdPlain<double, double>;
-    using SP = StPlain<double, double>;
-    const AxisWeights wh{{0, 0, 0}, 0.5};
+    SWC_TRY(host_to_field(dpsi, AJ(AJ_PSI)));
+    using LP = LdPlain<T, T>;
+    using SP = StPlain<T, T>;
+    const AxisWeights<T> wh{{0, 0, 0}, (T)0.5};
     SWC_TRY((pass<K_C2, 2>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
     SWC_TRY((pass<K_C2, 1>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
-    SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_PSI)}, StW{g_, AJ(AJ_Q), wh, 0})));
+    SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_PSI)}, StW<T>{g_, AJ(AJ_Q), wh, 0})));
   }
-  if (drho) SWC_CK(cudaMemcpyAsync(AJ(AJ_R), drho, ng * 8, cudaMemcpyHostToDevice, stream_));
+  if (drho) SWC_TRY(host_to_field(drho, AJ(AJ_R)));
   if (binomial) {
     SWC_TRY(reverse_binomial(0, Tn, 0, 2, nsnap));
   } else {
@@ -370,18 +417,7 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
     for (int64_t sg = nseg - 1; sg >= 0; --sg) {
       const int64_t s0 = sg * K, s1 = std::min<int64_t>(s0 + K, Tn);
       SWC_TRY(restore_ckpt((size_t)sg));
-      for (int64_t n = s0 + 1; n <= s1; ++n) {
-        double* tp = tape_ + (size_t)(n - s0 - 1) * kTape * ng;
-        SWC_CK(cudaMemcpyAsync(tp + TP_RHOIN * ng, rho_, ng * 8, cudaMemcpyDeviceToDevice, stream_));
-        const bool relax = !(n > p_.divv_switch || p_.load == 1);
-        SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old
-        const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
-                                  amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
-                                  vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
-        for (int q = 0; q < kTape; ++q)
-          if (src[q]) SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src[q], ng * 8, cudaMemcpyDeviceToDevice, stream_));
-        ++fwd_steps_;
-      }
+      for (int64_t n = s0 + 1; n <= s1; ++n) SWC_TRY(record_tape(tape_ + (size_t)(n - s0 - 1) * kTape * ng, n));
       for (int64_t n = s1; n > s0; --n) {
         const bool relax = !(n > p_.divv_switch || p_.load == 1);
         SWC_TRY(adjoint_step((size_t)(n - s0 - 1), relax, n == 1));
@@ -391,19 +427,19 @@ int StepEngine<T>::backward_fp64(const double* dpsi, const double* drho, double*
   // swc_set_state: psiq0 = scale DCT-II^3 psi0 = psiq_old0  =>  psi0_bar = scale DCT-III^3 D0 (Q_bar + Qo_bar)
   const unsigned blocks = (unsigned)((g_.ng + 255) / 256);
   if (dpsi0) {
-    axpby_kernel<<<blocks, 256, 0, stream_>>>(g_.ng, 1.0, AJ(AJ_Q), 1.0, AJ(AJ_QO), AJ(AJ_PSI));
+    axpby_kernel<T><<<blocks, 256, 0, stream_>>>(g_.ng, (T)1.0, AJ(AJ_Q), (T)1.0, AJ(AJ_QO), AJ(AJ_PSI));
     SWC_CK(cudaGetLastError());
-    using LP = LdPlain<double, double>;
-    using SP = StPlain<double, double>;
-    const AxisWeights w2{{0, 0, 0}, 2.0};
-    SWC_TRY((pass<K_C3, 2>(LdW{g_, AJ(AJ_PSI), w2}, SP{AJ(AJ_PSI)})));
+    using LP = LdPlain<T, T>;
+    using SP = StPlain<T, T>;
+    const AxisWeights<T> w2{{0, 0, 0}, (T)2.0};
+    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, AJ(AJ_PSI), w2}, SP{AJ(AJ_PSI)})));
     SWC_TRY((pass<K_C3, 1>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
     SWC_TRY((pass<K_C3, 0>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
-    axpby_kernel<<<blocks, 256, 0, stream_>>>(g_.ng, scale_, AJ(AJ_PSI), 0.0, nullptr, AJ(AJ_PSI));
+    axpby_kernel<T><<<blocks, 256, 0, stream_>>>(g_.ng, (T)scale_, AJ(AJ_PSI), (T)0.0, nullptr, AJ(AJ_PSI));
     SWC_CK(cudaGetLastError());
-    SWC_CK(cudaMemcpyAsync(dpsi0, AJ(AJ_PSI), ng * 8, cudaMemcpyDeviceToHost, stream_));
+    SWC_TRY(field_to_host(AJ(AJ_PSI), dpsi0));
   }
-  if (drho0) SWC_CK(cudaMemcpyAsync(drho0, AJ(AJ_R), ng * 8, cudaMemcpyDeviceToHost, stream_));
+  if (drho0) SWC_TRY(field_to_host(AJ(AJ_R), drho0));
   pg_reduce_kernel<<<PG_COUNT, 256, 0, stream_>>>(pgrad_, blocks);
   SWC_CK(cudaGetLastError());
   double pg[PG_COUNT];

@@ -430,6 +430,14 @@ template <typename T> struct S6Args {
   T rho0_t, kp_t, zeta_t, ep_t, beta_t, gamma_t, off_t;  // the coefficients in T, converted on the host
 };
 
+// FP64 -> FP32 copy (integer-pipe rounding), four elements per thread (n a multiple of 4).
+static __global__ void __launch_bounds__(256) narrow_kernel(const double* src, float* dst, long long n) {
+  const long long i = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= n) return;
+  const double2 a = *reinterpret_cast<const double2*>(src + i), b = *reinterpret_cast<const double2*>(src + i + 2);
+  *reinterpret_cast<float4*>(dst + i) = make_float4(narrow_f64(a.x), narrow_f64(a.y), narrow_f64(b.x), narrow_f64(b.y));
+}
+
 // FP32 -> FP64 copy, four elements per thread (n a multiple of 4).
 static __global__ void __launch_bounds__(256) widen_kernel(const float* src, double* dst, long long n) {
   const long long i = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -440,14 +448,14 @@ static __global__ void __launch_bounds__(256) widen_kernel(const float* src, dou
 }
 
 // Mixed engine: the FP32 copies of the FP64 state, rhof = rho - off and psiqf = psiq,
-// and the FP32 f_rho from its FP64 form (or zero), after swc_set_state / swc_load.
+// and the FP32 f_rho from its FP64 form (or zero; frhot null: left as it is).
 static __global__ void __launch_bounds__(256) mixed_copies_kernel(long long n, const double* rho, const double* psiq,
                                                                   const double* frho, double off, float* rhof,
                                                                   float* psiqf, float* frhot) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     rhof[i] = narrow_f64(rho[i] - off);
     psiqf[i] = narrow_f64(psiq[i]);
-    frhot[i] = frho ? narrow_f64(frho[i]) : 0.0f;
+    if (frhot) frhot[i] = frho ? narrow_f64(frho[i]) : 0.0f;
   }
 }
 
@@ -856,19 +864,21 @@ template <typename T> class StepEngine : public EngineBase {
   int save(const char* path) override;
   int load(const char* path) override;
   int backward(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out) override {
-    if constexpr (std::is_same<T, double>::value) {
-      return backward_fp64(dpsi, drho, dpsi0, drho0, out);
-    } else {
-      set_error("swc_backward needs the FP64 engine (precision SWC_PREC_FP64)");
-      return SWC_ERR_BAD_PARAM;
-    }
+    return backward_impl(dpsi, drho, dpsi0, drho0, out);
   }
 
  private:
   // ---- adjoint support (checkpoints here; the adjoint itself in swc_adjoint_impl.cuh)
   int save_ckpt(size_t slot);
+  size_t ckpt_slot_bytes() const;
   int restore_ckpt(size_t slot);
-  int backward_fp64(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
+  // FP64 engine: the FP64 adjoint (swc_adjoint_impl.cuh, in swc_step_fp64.cu); mixed
+  // engine: the same adjoint in FP32 on the mixed trajectory (swc_step_mixed_adj.cu)
+  int backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
+  int record_tape(T* tp, int64_t n);
+  int host_to_field(const double* src, T* dst);
+  int field_to_host(const T* src, double* dst);
+  int stage_alloc();
   int adjoint_step(size_t slot, bool relax, bool first);
   int adjoint_alloc(size_t tape_steps);
   int tape_and_adjoint(int64_t n);                        // step n from the loaded state n-1
@@ -877,9 +887,9 @@ template <typename T> class StepEngine : public EngineBase {
   int64_t fwd_steps_ = 0;          // forward steps rerun by the current swc_backward
   size_t engine_bytes_ = 0;        // device bytes of the engine's own arrays
   std::vector<double*> ckpt_;      // state at steps 0, K, 2K, ... (6 arrays each)
-  double* tape_ = nullptr;         // forward intermediates of one segment
+  T* tape_ = nullptr;              // forward intermediates of one segment
   size_t tape_steps_ = 0;
-  double* adj_ = nullptr;          // adjoint work arrays
+  T* adj_ = nullptr;               // adjoint work arrays
   double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
   int* status_ = nullptr;          // set by a transform pass whose bounded wait ran out
   double* stage_ = nullptr;        // FP64 staging of FP32 fields for swc_get_field
@@ -929,7 +939,7 @@ template <typename T> class StepEngine : public EngineBase {
   // state kept where the state is written: rhof = rho - rho_off_, psiqf = psiq
   T *inv_c2f_ = nullptr, *frhot_ = nullptr, *rhof_ = nullptr, *psiqf_ = nullptr;
   double rho_off_ = 0;  // (rho_0 + rho_s)/2 in the mixed engine, 0 in the FP64 engine
-  int refresh_copies(bool have_frho);
+  int refresh_copies(int frho_mode);
   int diag_blocks_ = 0;
   std::map<int, cudaGraphExec_t> graphs_;
   std::map<int, int64_t> graph_kernels_;  // kernel nodes per captured variant
@@ -953,7 +963,8 @@ template <typename T> void StepEngine<T>::release() {
   if (adj_) cudaFree(adj_);
   if (pgrad_) cudaFree(pgrad_);
   if (stage_) cudaFree(stage_);
-  tape_ = adj_ = pgrad_ = stage_ = nullptr;
+  tape_ = adj_ = nullptr;
+  pgrad_ = stage_ = nullptr;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
   for (void* a : allocs_) cudaFree(a);
@@ -1208,15 +1219,16 @@ struct StScaleD {
   __device__ __forceinline__ void operator()(int, int, int, long long idx, double v) const { p[idx] = s * v; }
 };
 
-// Mixed engine: rebuild the FP32 copies of the FP64 state (and f_rho from its FP64
-// form after swc_load, zero after swc_set_state). No-op for the FP64 engine.
-template <typename T> int StepEngine<T>::refresh_copies(bool have_frho) {
+// Mixed engine: rebuild the FP32 copies of the FP64 state, and f_rho: 0 zero (after
+// swc_set_state), 1 from its FP64 form (after swc_load), 2 kept (checkpoint restore).
+// No-op for the FP64 engine.
+template <typename T> int StepEngine<T>::refresh_copies(int frho_mode) {
   if constexpr (!std::is_same<T, double>::value) {
-    mixed_copies_kernel<<<1024, 256, 0, stream_>>>(g_.ng, rho_, psiq_, have_frho ? frho_ : nullptr, rho_off_, rhof_,
-                                                  psiqf_, frhot_);
+    mixed_copies_kernel<<<1024, 256, 0, stream_>>>(g_.ng, rho_, psiq_, frho_mode == 1 ? frho_ : nullptr, rho_off_,
+                                                  rhof_, psiqf_, frho_mode == 2 ? nullptr : frhot_);
     SWC_CK(cudaGetLastError());
   }
-  (void)have_frho;
+  (void)frho_mode;
   return SWC_OK;
 }
 
@@ -1241,7 +1253,7 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   SWC_TRY((pass<K_C3, 1>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
   SWC_TRY((pass<K_C3, 0>(LdPlain<T, T>{psi_}, StPlain<T, T>{psi_})));
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, nt, cudaMemcpyDeviceToDevice, stream_));  // REF:1010
-  SWC_TRY(refresh_copies(false));
+  SWC_TRY(refresh_copies(0));
   if (p_.adjoint_ckpt != 0) SWC_TRY(save_ckpt(0));
   adj_valid_ = p_.adjoint_ckpt != 0;
   SWC_CK(cudaStreamSynchronize(stream_));
@@ -1253,34 +1265,47 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   return SWC_OK;
 }
 
-// Checkpoint slot: psiq, psiq_old, Nl_old, rho, f_rho, psi (raw copies, ng*8 bytes each).
+// Checkpoint slot: psiq, psiq_old, rho (FP64), Nl_old, f_rho, psi (the engine's
+// precision: FP64, or FP32 in the mixed engine), packed: ckpt_slot_bytes() each.
+template <typename T> size_t StepEngine<T>::ckpt_slot_bytes() const {
+  return (size_t)g_.ng * (3 * sizeof(double) + 3 * sizeof(T));
+}
+
 template <typename T> int StepEngine<T>::save_ckpt(size_t slot) {
   const size_t ng = (size_t)g_.ng;
   while (ckpt_.size() <= slot) {
     double* c = nullptr;
-    if (cudaMalloc(&c, 6 * ng * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&c, ckpt_slot_bytes()) != cudaSuccess) {
       cudaGetLastError();
-      set_error("cudaMalloc for an adjoint checkpoint failed (%zu MB)", (6 * ng * 8) >> 20);
+      set_error("cudaMalloc for an adjoint checkpoint failed (%zu MB)", ckpt_slot_bytes() >> 20);
       return SWC_ERR_OOM;
     }
     ckpt_.push_back(c);
   }
-  double* c = ckpt_[slot];
-  const void* src[6] = {psiq_, psiq_old_, nlq_, rho_, frho_, psi_};
-  const size_t sz[6] = {8, 8, sizeof(T), 8, 8, sizeof(T)};
-  for (int q = 0; q < 6; ++q)
-    SWC_CK(cudaMemcpyAsync(c + q * ng, src[q], ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
+  char* c = reinterpret_cast<char*>(ckpt_[slot]);
+  constexpr bool mixed = !std::is_same<T, double>::value;
+  const void* src[6] = {psiq_, psiq_old_, rho_, nlq_, mixed ? (const void*)frhot_ : (const void*)frho_, psi_};
+  const size_t sz[6] = {8, 8, 8, sizeof(T), sizeof(T), sizeof(T)};
+  size_t off = 0;
+  for (int q = 0; q < 6; ++q) {
+    SWC_CK(cudaMemcpyAsync(c + off, src[q], ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
+    off += ng * sz[q];
+  }
   return SWC_OK;
 }
 
 template <typename T> int StepEngine<T>::restore_ckpt(size_t slot) {
   const size_t ng = (size_t)g_.ng;
-  const double* c = ckpt_[slot];
-  void* dst[6] = {psiq_, psiq_old_, nlq_, rho_, frho_, psi_};
-  const size_t sz[6] = {8, 8, sizeof(T), 8, 8, sizeof(T)};
-  for (int q = 0; q < 6; ++q)
-    SWC_CK(cudaMemcpyAsync(dst[q], c + q * ng, ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
-  return SWC_OK;
+  const char* c = reinterpret_cast<const char*>(ckpt_[slot]);
+  constexpr bool mixed = !std::is_same<T, double>::value;
+  void* dst[6] = {psiq_, psiq_old_, rho_, nlq_, mixed ? (void*)frhot_ : (void*)frho_, psi_};
+  const size_t sz[6] = {8, 8, 8, sizeof(T), sizeof(T), sizeof(T)};
+  size_t off = 0;
+  for (int q = 0; q < 6; ++q) {
+    SWC_CK(cudaMemcpyAsync(dst[q], c + off, ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
+    off += ng * sz[q];
+  }
+  return refresh_copies(2);  // the mixed engine's FP32 copies of rho and psiq (f_rho restored above)
 }
 
 template <typename T> int StepEngine<T>::step(int nsteps) {
@@ -1405,6 +1430,19 @@ template <typename T> int StepEngine<T>::field_src(int field, const void** src, 
   return SWC_OK;
 }
 
+// The FP64 staging buffer of the mixed engine's host transfers (allocated on first use).
+template <typename T> int StepEngine<T>::stage_alloc() {
+  if (stage_) return SWC_OK;
+  const size_t n = (size_t)g_.ng;
+  if (cudaMalloc(&stage_, n * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    stage_ = nullptr;
+    set_error("cudaMalloc of the %zu MB field staging buffer failed", (n * 8) >> 20);
+    return SWC_ERR_OOM;
+  }
+  return SWC_OK;
+}
+
 template <typename T> int StepEngine<T>::get_field(int field, double* dst) {
   const void* src;
   bool is_d;
@@ -1418,14 +1456,7 @@ template <typename T> int StepEngine<T>::get_field(int field, double* dst) {
   } else {
     // FP32 field: widened to FP64 on the device (staging buffer allocated on first use),
     // then one device-to-host copy straight into the caller's buffer
-    if (!stage_) {
-      if (cudaMalloc(&stage_, n * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        stage_ = nullptr;
-        set_error("cudaMalloc of the %zu MB field staging buffer failed", (n * 8) >> 20);
-        return SWC_ERR_OOM;
-      }
-    }
+    SWC_TRY(stage_alloc());
     widen_kernel<<<(unsigned)((n / 4 + 255) / 256), 256, 0, stream_>>>(reinterpret_cast<const float*>(src), stage_,
                                                                        (long long)n);
     SWC_CK(cudaGetLastError());
@@ -1537,7 +1568,7 @@ template <typename T> int StepEngine<T>::load(const char* path) {
     return SWC_ERR_IO;
   }
   SWC_CK(cudaMemcpyAsync(psi_old_, psi_, n * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
-  SWC_TRY(refresh_copies(true));
+  SWC_TRY(refresh_copies(1));
   SWC_CK(cudaStreamSynchronize(stream_));
   adj_valid_ = false;  // the checkpoints no longer describe this trajectory
   nloop_ = h.nloop;

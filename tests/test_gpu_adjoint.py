@@ -133,3 +133,27 @@ def test_binomial_cap_too_small_is_rejected(lib):
         e.step(3)
         with pytest.raises(SwcError):
             e.backward(dpsi=np.ones((16, 16, 16)))
+
+
+def test_fp32_adjoint_of_the_mixed_engine(lib):
+    """The mixed engine's FP32 adjoint (same kernels, T = float, on the mixed trajectory)
+    agrees with the FP64 adjoint of the FP64 engine to FP32 accuracy, and its binomial
+    schedule returns its fixed-interval gradients."""
+    shape, ds, nsteps = (32, 32, 32), 3, 10
+    rng = np.random.default_rng(5)
+    wp, wr = rng.standard_normal(shape), rng.standard_normal(shape)
+    g = {}
+    for prec, ckpt in ((abi.SWC_PREC_FP64, 5), (abi.SWC_PREC_MIXED, 5), (abi.SWC_PREC_MIXED, -1)):
+        p = abi.default_params(*shape, rho_0=0.8, divv_switch=ds, adjoint_ckpt=ckpt, ref_ranks=2, precision=prec)
+        psi0, rho0 = ic.undulated_interface(p, sigma=1e-2)
+        with Engine(p) as e:
+            e.set_state(psi0, rho0)
+            e.step(nsteps)
+            g[(prec, ckpt)] = e.backward(dpsi=wp, drho=wr, want_psi0=True, want_rho0=True)
+    ref, f32, f32b = g[(abi.SWC_PREC_FP64, 5)], g[(abi.SWC_PREC_MIXED, 5)], g[(abi.SWC_PREC_MIXED, -1)]
+    for key in ("psi0", "rho0"):
+        assert np.linalg.norm(f32[key] - ref[key]) <= 1e-4 * np.linalg.norm(ref[key]), key
+        assert np.array_equal(f32b[key], f32[key]), key
+    for name in COEFFS:
+        assert abs(f32[name] - ref[name]) <= 1e-3 * abs(ref[name]) + 1e-6, (name, f32[name], ref[name])
+        assert f32b[name] == f32[name], name
