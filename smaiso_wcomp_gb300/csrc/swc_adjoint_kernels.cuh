@@ -37,6 +37,16 @@ template <typename T> struct LdW {
   __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
     return p[idx] * aw.at(g, i, j, k);
   }
+  // vector forms for the FP32 two-line pass (z: k .. k+3; x/y: k, k+1)
+  __device__ __forceinline__ float4 quad(int i, int j, int k, long long idx) const {
+    const float4 v = ld4v(p, idx);
+    return make_float4(v.x * (float)aw.at(g, i, j, k), v.y * (float)aw.at(g, i, j, k + 1),
+                       v.z * (float)aw.at(g, i, j, k + 2), v.w * (float)aw.at(g, i, j, k + 3));
+  }
+  __device__ __forceinline__ float2 pair(int i, int j, int k, long long idx) const {
+    const float2 v = ld2v(p, idx);
+    return make_float2(v.x * (float)aw.at(g, i, j, k), v.y * (float)aw.at(g, i, j, k + 1));
+  }
 };
 
 // store v * weight (output side of DCT-III^T / DST-III^T); acc: += instead of =
@@ -49,12 +59,25 @@ template <typename T> struct StW {
     const T y = v * aw.at(g, i, j, k);
     p[idx] = acc ? p[idx] + y : y;
   }
+  __device__ __forceinline__ void pair(int i, int j, int k, long long idx, float2 v) const {
+    float2 y = make_float2(v.x * (float)aw.at(g, i, j, k), v.y * (float)aw.at(g, i, j, k + 1));
+    if (acc) {
+      const float2 o = ld2v(p, idx);
+      y.x += o.x;
+      y.y += o.y;
+    }
+    st2v(p, idx, y);
+  }
 };
 
 // accumulate (+=) a real-space result
 template <typename T> struct StAcc {
   T* p;
   __device__ __forceinline__ void operator()(int, int, int, long long idx, T v) const { p[idx] += v; }
+  __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const {
+    const float2 o = ld2v(p, idx);
+    st2v(p, idx, make_float2(o.x + v.x, o.y + v.y));
+  }
 };
 
 // Transpose of the shifted spectral derivative (REF:1190-1219): the forward wrote
@@ -74,6 +97,22 @@ template <typename T> struct StAdjGrad {
     if (c >= n - 1) return;
     target[idx + shift] += -fac * vs[c] * (v * aw.at(g, i, j, k));
   }
+  // x/y passes of the FP32 two-line pass: elements (k, k+1); an even shift keeps the
+  // shifted pair 8-byte aligned (one vector read-modify-write), shift 1 does not
+  __device__ __forceinline__ void pair(int i, int j, int k, long long idx, float2 v) const {
+    if (shift & 1) {
+      (*this)(i, j, k, idx, v.x);
+      (*this)(i, j, k + 1, idx + 1, v.y);
+      return;
+    }
+    const int n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    const int c0 = axis == 0 ? i : (axis == 1 ? j : k), c1 = axis == 2 ? k + 1 : c0;
+    const float a = (c0 < n - 1) ? -(float)fac * (float)vs[c0] * (v.x * (float)aw.at(g, i, j, k)) : 0.f;
+    const float b = (c1 < n - 1) ? -(float)fac * (float)vs[c1] * (v.y * (float)aw.at(g, i, j, k + 1)) : 0.f;
+    if (c0 >= n - 1 && c1 >= n - 1) return;
+    const float2 o = ld2v(target, idx + shift);
+    st2v(target, idx + shift, make_float2(o.x + a, o.y + b));
+  }
 };
 
 // Last pass of Delta_s(bar lapR) (normal phase, transpose of REF:1319-1342):
@@ -84,6 +123,11 @@ template <typename T> struct StAdjLap {
   __device__ __forceinline__ void operator()(int, int, int, long long idx, T y) const {
     brho[idx] += L[idx] * y;
     bL[idx] += rho[idx] * y;
+  }
+  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 y) const {
+    const float4 l = ld4v(L, idx), r = ld4v(rho, idx), a = ld4v(brho, idx), b = ld4v(bL, idx);
+    st4v(brho, idx, make_float4(a.x + l.x * y.x, a.y + l.y * y.y, a.z + l.z * y.z, a.w + l.w * y.w));
+    st4v(bL, idx, make_float4(b.x + r.x * y.x, b.y + r.y * y.y, b.z + r.z * y.z, b.w + r.w * y.w));
   }
 };
 
@@ -102,6 +146,29 @@ template <typename T> struct StAdjAmp {
     bgx[idx] += a * s;
     bgy[idx] += b * s;
     bgz[idx] += c * s;
+  }
+  // z pass of the FP32 two-line pass: four consecutive elements with vector accesses
+  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 y) const {
+    const float4 P = ld4v(psi, idx), X = ld4v(gx, idx), Y = ld4v(gy, idx), Z = ld4v(gz, idx);
+    float4 bp = ld4v(bpsi, idx), bx = ld4v(bgx, idx), by = ld4v(bgy, idx), bz = ld4v(bgz, idx);
+    const float q = (float)q02;
+    auto one = [&](float p, float a, float b, float c, float yy, float& op, float& ox, float& oy, float& oz) {
+      const float A = sqrtf(q * (p * p) + (a * a) + (b * b) + (c * c));
+      if (!(A > 0.f)) return;
+      const float s2 = yy / A;
+      op += q * p * s2;
+      ox += a * s2;
+      oy += b * s2;
+      oz += c * s2;
+    };
+    one(P.x, X.x, Y.x, Z.x, y.x, bp.x, bx.x, by.x, bz.x);
+    one(P.y, X.y, Y.y, Z.y, y.y, bp.y, bx.y, by.y, bz.y);
+    one(P.z, X.z, Y.z, Z.z, y.z, bp.z, bx.z, by.z, bz.z);
+    one(P.w, X.w, Y.w, Z.w, y.w, bp.w, bx.w, by.w, bz.w);
+    st4v(bpsi, idx, bp);
+    st4v(bgx, idx, bx);
+    st4v(bgy, idx, by);
+    st4v(bgz, idx, bz);
   }
 };
 
@@ -167,15 +234,27 @@ __global__ void __launch_bounds__(256) adj_cn_kernel(Grid g, const T* qx, const 
     const T C1 = T(2.0) - s.dt * s.rho_m * aLin, C2 = T(1.5) - s.dt * s.rho_m * aLin;
     const T h = s.dtd2 * s.scale;
     const T bq = bQ[idx];
-    T bnl = T(3.0) * h / C2 * bq + bNlo[idx];
-    if (first) bnl += -h / C2 * bq;  // REF:2170-2172: Nl_old = Nl at nLoop == 1
-    bNlq[idx] = bnl;
-    bNlo[idx] = first ? T(0.0) : -h / C2 * bq;
-    const T bqo_next = bQo[idx];
-    bQo[idx] = -T(0.5) / C2 * bq;
-    bQ[idx] = C1 / C2 * bq + bqo_next;
-    // dC1/dalpha = dC2/dalpha = dt rho_m sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
-    da = bq * s.dt * s.rho_m * sq * sq * (Qold[idx] - Qnew[idx]) / C2;
+    if constexpr (sizeof(T) == 8) {  // the FP64 adjoint keeps its divisions
+      T bnl = T(3.0) * h / C2 * bq + bNlo[idx];
+      if (first) bnl += -h / C2 * bq;  // REF:2170-2172: Nl_old = Nl at nLoop == 1
+      bNlq[idx] = bnl;
+      bNlo[idx] = first ? T(0.0) : -h / C2 * bq;
+      const T bqo_next = bQo[idx];
+      bQo[idx] = -T(0.5) / C2 * bq;
+      bQ[idx] = C1 / C2 * bq + bqo_next;
+      // dC1/dalpha = dC2/dalpha = dt rho_m sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
+      da = bq * s.dt * s.rho_m * sq * sq * (Qold[idx] - Qnew[idx]) / C2;
+    } else {  // FP32: one reciprocal
+      const T r = T(1.0) / C2, hb = h * r * bq;
+      T bnl = T(3.0) * hb + bNlo[idx];
+      if (first) bnl -= hb;
+      bNlq[idx] = bnl;
+      bNlo[idx] = first ? T(0.0) : -hb;
+      const T bqo_next = bQo[idx];
+      bQo[idx] = -T(0.5) * r * bq;
+      bQ[idx] = C1 * r * bq + bqo_next;
+      da = bq * s.dt * s.rho_m * sq * sq * (Qold[idx] - Qnew[idx]) * r;
+    }
   }
   block_accum(da, pgrad, PG_ALPHA);
 }
