@@ -61,7 +61,7 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   const T* tp = tape_ + slot * (size_t)kTape * ng;
   auto TP = [&](int q) { return tp + (size_t)q * ng; };
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
-  const unsigned blocks = (unsigned)((g_.ng + 255) / 256);
+  const unsigned blocks = pt4_blocks(g_);
   const AdjScalars<T> sc{(T)p_.ep, (T)p_.alpha, (T)p_.beta, (T)p_.gamma, (T)p_.zeta, (T)kp_, (T)p_.rho_0,
                          (T)(p_.q0 * p_.q0), (T)p_.dt, (T)(p_.dt / 2), (T)rho_m_, (T)scale_, (T)p_.nu,
                          (T)(p_.lambda + 2 * p_.nu)};
@@ -76,7 +76,7 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   SWC_CK(cudaGetLastError());
   // (2) grad.f subtracted in spectral space, then Nl-hat = DCT-II^3 Nl -> Nl_bar = DCT-III^3 D0 Nlq_bar
   adj_dq_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], AJ(AJ_NL), AJ(AJ_FX), AJ(AJ_FY),
-                                             AJ(AJ_FZ));
+                                             AJ(AJ_FZ), sine_w(0, 2.0), sine_w(1, 2.0), sine_w(2, 2.0));
   SWC_CK(cudaGetLastError());
   SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, AJ(AJ_NL), w2}, SP{AJ(AJ_NL)})));
   SWC_TRY((pass<K_C3, 1>(LP{AJ(AJ_NL)}, SP{AJ(AJ_NL)})));
@@ -94,20 +94,21 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   }
   // (4) divv = DCT-III^3 divv-hat -> divv-hat_bar = D0^-1 DCT-II^3 divv_bar;
   //     v_a = inverse mixed of v-hat_a -> v-hat_bar = W^-1 forward-mixed(v_bar)
+  //     (the output weights D0^-1, W^-1 are applied where adj_stokes1_kernel reads them)
   SWC_TRY((pass<K_C2, 2>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
   SWC_TRY((pass<K_C2, 1>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
-  SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_DIVV)}, StW<T>{g_, adj_ + AJ_DIVV * ng, wh, 0})));
+  SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_DIVV)}, SP{AJ(AJ_DIVV)})));
   {
     T* bv[3] = {adj_ + AJ_VX * ng, adj_ + AJ_VY * ng, adj_ + AJ_VZ * ng};
     SWC_TRY((pass<K_C2, 2>(LP{bv[0]}, SP{bv[0]})));
     SWC_TRY((pass<K_C2, 1>(LP{bv[0]}, SP{bv[0]})));
-    SWC_TRY((pass<K_S2, 0>(LP{bv[0]}, StW<T>{g_, bv[0], sine_w(0, 0.5), 0})));
+    SWC_TRY((pass<K_S2, 0>(LP{bv[0]}, SP{bv[0]})));
     SWC_TRY((pass<K_C2, 2>(LP{bv[1]}, SP{bv[1]})));
     SWC_TRY((pass<K_S2, 1>(LP{bv[1]}, SP{bv[1]})));
-    SWC_TRY((pass<K_C2, 0>(LP{bv[1]}, StW<T>{g_, bv[1], sine_w(1, 0.5), 0})));
+    SWC_TRY((pass<K_C2, 0>(LP{bv[1]}, SP{bv[1]})));
     SWC_TRY((pass<K_S2, 2>(LP{bv[2]}, SP{bv[2]})));
     SWC_TRY((pass<K_C2, 1>(LP{bv[2]}, SP{bv[2]})));
-    SWC_TRY((pass<K_C2, 0>(LP{bv[2]}, StW<T>{g_, bv[2], sine_w(2, 0.5), 0})));
+    SWC_TRY((pass<K_C2, 0>(LP{bv[2]}, SP{bv[2]})));
   }
   // (5) Stokes solve + divergence (REF:1468-2078)
   {
@@ -117,20 +118,21 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
                     adj_ + AJ_FGPY * ng, adj_ + AJ_FGPZ * ng, vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2],
                     gq_[0], gq_[1], gq_[2], gs_[0], gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu),
                     (T)(1.0 / (p_.lambda + 2 * p_.nu)), (T)p_.nu, (T)(p_.lambda + 2 * p_.nu), p_.nx / p_.ref_ranks,
-                    pgrad_};
+                    sine_w(0, 0.5), sine_w(1, 0.5), sine_w(2, 0.5), wh, pgrad_};
     adj_stokes1_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
     AdjStokes2Args<T> b{AJ(AJ_DOTX), AJ(AJ_DOTY), AJ(AJ_DOTZ), AJ(AJ_SDX), AJ(AJ_SDY), AJ(AJ_SDZ), AJ(AJ_FGPX),
                      AJ(AJ_FGPY), AJ(AJ_FGPZ), adj_ + AJ_SX * ng, adj_ + AJ_SY * ng, adj_ + AJ_SZ * ng,
                      adj_ + AJ_FG * ng, adj_ + AJ_E * ng, vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2],
-                     gq_[0], gq_[1], gq_[2]};
+                     gq_[0], gq_[1], gq_[2], sine_w(0, 2.0), sine_w(1, 2.0), sine_w(2, 2.0), w2};
     adj_stokes2_kernel<T><<<blocks, 256, 0, stream_>>>(g_, b);
     SWC_CK(cudaGetLastError());
   }
   // (6) forward transforms of S7 (REF:1427-1457) transposed: DCT-II^T = DCT-III D0,
-  //     DST-II^T = DST-III DL, applied in place to the spectral cotangents
+  //     DST-II^T = DST-III DL, applied in place to the spectral cotangents (their
+  //     producers, adj_stokes2_kernel and adj_dq_kernel, stored them times D0 / DL)
   auto cos_t = [&](T* b) -> int {
-    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, b, w2}, SP{b})));
+    SWC_TRY((pass<K_C3, 2>(LP{b}, SP{b})));
     SWC_TRY((pass<K_C3, 1>(LP{b}, SP{b})));
     SWC_TRY((pass<K_C3, 0>(LP{b}, SP{b})));
     return SWC_OK;
@@ -141,13 +143,13 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
     T* bx = adj_ + (c == 0 ? AJ_SX : AJ_FX) * ng;
     T* by = adj_ + (c == 0 ? AJ_SY : AJ_FY) * ng;
     T* bz = adj_ + (c == 0 ? AJ_SZ : AJ_FZ) * ng;
-    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, bx, sine_w(0, 2.0)}, SP{bx})));
+    SWC_TRY((pass<K_C3, 2>(LP{bx}, SP{bx})));
     SWC_TRY((pass<K_C3, 1>(LP{bx}, SP{bx})));
     SWC_TRY((pass<K_S3, 0>(LP{bx}, SP{bx})));
-    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, by, sine_w(1, 2.0)}, SP{by})));
+    SWC_TRY((pass<K_C3, 2>(LP{by}, SP{by})));
     SWC_TRY((pass<K_S3, 1>(LP{by}, SP{by})));
     SWC_TRY((pass<K_C3, 0>(LP{by}, SP{by})));
-    SWC_TRY((pass<K_S3, 2>(LdW<T>{g_, bz, sine_w(2, 2.0)}, SP{bz})));
+    SWC_TRY((pass<K_S3, 2>(LP{bz}, SP{bz})));
     SWC_TRY((pass<K_C3, 1>(LP{bz}, SP{bz})));
     SWC_TRY((pass<K_C3, 0>(LP{bz}, SP{bz})));
   }
@@ -174,9 +176,10 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
     // lapR_raw = DCT-III^3 (-q^2 alpha (q0^2 - q^2) psiq)
     SWC_TRY((pass<K_C2, 2>(LP{blap}, SP{blap})));
     SWC_TRY((pass<K_C2, 1>(LP{blap}, SP{blap})));
-    SWC_TRY((pass<K_C2, 0>(LP{blap}, StW<T>{g_, blap, wh, 0})));
-    adj_acc_spec_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], 1, p_.alpha, p_.q0 * p_.q0,
-                                                     blap, TP(TP_QOLD), AJ(AJ_Q), pgrad_);
+    SWC_TRY((pass<K_C2, 0>(LP{blap}, SP{blap})));
+    adj_acc_spec_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], 1, (T)p_.alpha,
+                                                     (T)(p_.q0 * p_.q0), wh, blap, TP(TP_QOLD), AJ(AJ_Q),
+                                                     pgrad_);
     SWC_CK(cudaGetLastError());
   }
   // (9) dfDlapPsi = DCT-III^3 (alpha (q0^2 - q^2) psiq)  (REF:1293-1308)
@@ -184,9 +187,9 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
     T* bl = adj_ + AJ_L * ng;
     SWC_TRY((pass<K_C2, 2>(LP{bl}, SP{bl})));
     SWC_TRY((pass<K_C2, 1>(LP{bl}, SP{bl})));
-    SWC_TRY((pass<K_C2, 0>(LP{bl}, StW<T>{g_, bl, wh, 0})));
-    adj_acc_spec_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], 0, p_.alpha, p_.q0 * p_.q0, bl,
-                                                     TP(TP_QOLD), AJ(AJ_Q), pgrad_);
+    SWC_TRY((pass<K_C2, 0>(LP{bl}, SP{bl})));
+    adj_acc_spec_kernel<T><<<blocks, 256, 0, stream_>>>(g_, vq_[0], vq_[1], vq_[2], 0, (T)p_.alpha,
+                                                     (T)(p_.q0 * p_.q0), wh, bl, TP(TP_QOLD), AJ(AJ_Q), pgrad_);
     SWC_CK(cudaGetLastError());
   }
   // (10) amplitude filter A = F(A_raw) (symmetric) and A_raw = |psi, grad psi| (REF:1254-1289)
@@ -196,44 +199,49 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
     SWC_TRY((pass<K_C2, 1>(LP{bA}, SP{bA})));
     SWC_TRY((pass<K_FILT, 0>(LP{bA}, SP{bA}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
     SWC_TRY((pass<K_C3, 1>(LP{bA}, SP{bA})));
-    SWC_TRY((pass<K_C3, 2>(LP{bA}, StAdjAmp<T>{TP(TP_PSI), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ), adj_ + AJ_PSI * ng,
-                                            adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng, adj_ + AJ_GPZ * ng,
-                                            (T)(p_.q0 * p_.q0)})));
+    SWC_TRY((pass<K_C3, 2>(LP{bA}, SP{bA})));
+    adj_amp_kernel<T><<<blocks, 256, 0, stream_>>>(g_, bA, TP(TP_PSI), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ),
+                                                (T)(p_.q0 * p_.q0), AJ(AJ_PSI), AJ(AJ_GPX), AJ(AJ_GPY),
+                                                AJ(AJ_GPZ));
+    SWC_CK(cudaGetLastError());
   }
   // (11) gradients (REF:1166-1250): grad_a = inverse-mixed(-fac Vs shift X); transpose =
-  //      forward-mixed, output weights, then the shifted scatter into X_bar
-  SWC_CK(cudaMemsetAsync(adj_ + AJ_RQ * ng, 0, ng * sizeof(T), stream_));
-  const long long sx = 1LL << (g_.ly + g_.lz), sy = g_.nz;
+  //      forward-mixed, then the output weights and the shifted gather into X_bar
+  //      (adj_grad_kernel, both gradient families in one pass)
   for (int which = 0; which < 2; ++which) {
-    T* target = which == 0 ? adj_ + AJ_Q * ng : adj_ + AJ_RQ * ng;
-    const T fac = which == 0 ? (T)1.0 : (T)scale_;
     T* bgx = adj_ + (which == 0 ? AJ_GPX : AJ_GRX) * ng;
     T* bgy = adj_ + (which == 0 ? AJ_GPY : AJ_GRY) * ng;
     T* bgz = adj_ + (which == 0 ? AJ_GPZ : AJ_GRZ) * ng;
     SWC_TRY((pass<K_C2, 2>(LP{bgx}, SP{bgx})));
     SWC_TRY((pass<K_C2, 1>(LP{bgx}, SP{bgx})));
-    SWC_TRY((pass<K_S2, 0>(LP{bgx}, StAdjGrad<T>{g_, target, vs_[0], fac, 0, sx, sine_w(0, 0.5)})));
+    SWC_TRY((pass<K_S2, 0>(LP{bgx}, SP{bgx})));
     SWC_TRY((pass<K_C2, 2>(LP{bgy}, SP{bgy})));
     SWC_TRY((pass<K_S2, 1>(LP{bgy}, SP{bgy})));
-    SWC_TRY((pass<K_C2, 0>(LP{bgy}, StAdjGrad<T>{g_, target, vs_[1], fac, 1, sy, sine_w(1, 0.5)})));
+    SWC_TRY((pass<K_C2, 0>(LP{bgy}, SP{bgy})));
     SWC_TRY((pass<K_S2, 2>(LP{bgz}, SP{bgz})));
     SWC_TRY((pass<K_C2, 1>(LP{bgz}, SP{bgz})));
-    SWC_TRY((pass<K_C2, 0>(LP{bgz}, StAdjGrad<T>{g_, target, vs_[2], fac, 2, 1, sine_w(2, 0.5)})));
+    SWC_TRY((pass<K_C2, 0>(LP{bgz}, SP{bgz})));
+  }
+  {
+    AdjGradArgs<T> a{AJ(AJ_GPX), AJ(AJ_GPY), AJ(AJ_GPZ), AJ(AJ_GRX), AJ(AJ_GRY), AJ(AJ_GRZ), AJ(AJ_Q), AJ(AJ_RQ),
+                     vs_[0], vs_[1], vs_[2], (T)scale_, sine_w(0, 0.5), sine_w(1, 0.5), sine_w(2, 0.5), w2};
+    adj_grad_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
+    SWC_CK(cudaGetLastError());
   }
   // (12) rho-hat = DCT-II^3 rho (REF:1104-1106): rho_bar += DCT-III^3 D0 rhoq_bar
-  {
-    T* rq = adj_ + AJ_RQ * ng;
-    SWC_TRY((pass<K_C3, 2>(LdW<T>{g_, rq, w2}, SP{rq})));
-    SWC_TRY((pass<K_C3, 1>(LP{rq}, SP{rq})));
-    SWC_TRY((pass<K_C3, 0>(LP{rq}, StAcc<T>{adj_ + AJ_R * ng})));
-  }
-  // (13) the step's psi = DCT-III^3 psiq: psiq_bar += D0^-1 DCT-II^3 psi_bar
-  {
-    T* bp = adj_ + AJ_PSI * ng;
-    SWC_TRY((pass<K_C2, 2>(LP{bp}, SP{bp})));
-    SWC_TRY((pass<K_C2, 1>(LP{bp}, SP{bp})));
-    SWC_TRY((pass<K_C2, 0>(LP{bp}, StW<T>{g_, adj_ + AJ_Q * ng, wh, 1})));
-  }
+  //      (D0 applied by adj_grad_kernel)
+  T* rq = adj_ + AJ_RQ * ng;
+  SWC_TRY((pass<K_C3, 2>(LP{rq}, SP{rq})));
+  SWC_TRY((pass<K_C3, 1>(LP{rq}, SP{rq})));
+  SWC_TRY((pass<K_C3, 0>(LP{rq}, SP{rq})));
+  // (13) the step's psi = DCT-III^3 psiq: psiq_bar += D0^-1 DCT-II^3 psi_bar; then both
+  //      accumulations (adj_fold_kernel)
+  T* bp = adj_ + AJ_PSI * ng;
+  SWC_TRY((pass<K_C2, 2>(LP{bp}, SP{bp})));
+  SWC_TRY((pass<K_C2, 1>(LP{bp}, SP{bp})));
+  SWC_TRY((pass<K_C2, 0>(LP{bp}, SP{bp})));
+  adj_fold_kernel<T><<<blocks, 256, 0, stream_>>>(g_, bp, wh, rq, AJ(AJ_Q), AJ(AJ_R));
+  SWC_CK(cudaGetLastError());
   return SWC_OK;
 }
 

@@ -70,51 +70,6 @@ template <typename T> struct StW {
   }
 };
 
-// accumulate (+=) a real-space result
-template <typename T> struct StAcc {
-  T* p;
-  __device__ __forceinline__ void operator()(int, int, int, long long idx, T v) const { p[idx] += v; }
-  __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const {
-    const float2 o = ld2v(p, idx);
-    st2v(p, idx, make_float2(o.x + v.x, o.y + v.y));
-  }
-};
-
-// Transpose of the shifted spectral derivative (REF:1190-1219): the forward wrote
-// out[c] = -fac Vs[c] in[c+1]; here in_bar[c+1] += -fac Vs[c] y[c] (output weight
-// of the transposed inverse transform applied first).
-template <typename T> struct StAdjGrad {
-  Grid g;
-  T* target;
-  const T* vs;
-  T fac;
-  int axis;
-  long long shift;
-  AxisWeights<T> aw;
-  __device__ __forceinline__ void operator()(int i, int j, int k, long long idx, T v) const {
-    const int c = axis == 0 ? i : (axis == 1 ? j : k);
-    const int n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
-    if (c >= n - 1) return;
-    target[idx + shift] += -fac * vs[c] * (v * aw.at(g, i, j, k));
-  }
-  // x/y passes of the FP32 two-line pass: elements (k, k+1); an even shift keeps the
-  // shifted pair 8-byte aligned (one vector read-modify-write), shift 1 does not
-  __device__ __forceinline__ void pair(int i, int j, int k, long long idx, float2 v) const {
-    if (shift & 1) {
-      (*this)(i, j, k, idx, v.x);
-      (*this)(i, j, k + 1, idx + 1, v.y);
-      return;
-    }
-    const int n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
-    const int c0 = axis == 0 ? i : (axis == 1 ? j : k), c1 = axis == 2 ? k + 1 : c0;
-    const float a = (c0 < n - 1) ? -(float)fac * (float)vs[c0] * (v.x * (float)aw.at(g, i, j, k)) : 0.f;
-    const float b = (c1 < n - 1) ? -(float)fac * (float)vs[c1] * (v.y * (float)aw.at(g, i, j, k + 1)) : 0.f;
-    if (c0 >= n - 1 && c1 >= n - 1) return;
-    const float2 o = ld2v(target, idx + shift);
-    st2v(target, idx + shift, make_float2(o.x + a, o.y + b));
-  }
-};
-
 // Last pass of Delta_s(bar lapR) (normal phase, transpose of REF:1319-1342):
 // rho_bar += L * y, L_bar += rho * y (Delta_s is symmetric).
 template <typename T> struct StAdjLap {
@@ -131,69 +86,51 @@ template <typename T> struct StAdjLap {
   }
 };
 
-// Last pass of F(bar A) (F symmetric, REF:1271-1288), then the transpose of
-// A_raw = sqrt(q0^2 psi^2 + |grad psi|^2) (REF:1262-1266).
-template <typename T> struct StAdjAmp {
-  const T *psi, *gx, *gy, *gz;
-  T *bpsi, *bgx, *bgy, *bgz;
-  T q02;
-  __device__ __forceinline__ void operator()(int, int, int, long long idx, T y) const {
-    const T p = psi[idx], a = gx[idx], b = gy[idx], c = gz[idx];
-    const T A = sqrt(q02 * (p * p) + (a * a) + (b * b) + (c * c));
-    if (!(A > 0)) return;  // the square root is not differentiable at 0: no contribution
-    const T s = y / A;
-    bpsi[idx] += q02 * p * s;
-    bgx[idx] += a * s;
-    bgy[idx] += b * s;
-    bgz[idx] += c * s;
-  }
-  // z pass of the FP32 two-line pass: four consecutive elements with vector accesses
-  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 y) const {
-    const float4 P = ld4v(psi, idx), X = ld4v(gx, idx), Y = ld4v(gy, idx), Z = ld4v(gz, idx);
-    float4 bp = ld4v(bpsi, idx), bx = ld4v(bgx, idx), by = ld4v(bgy, idx), bz = ld4v(bgz, idx);
-    const float q = (float)q02;
-    auto one = [&](float p, float a, float b, float c, float yy, float& op, float& ox, float& oy, float& oz) {
-      const float A = sqrtf(q * (p * p) + (a * a) + (b * b) + (c * c));
-      if (!(A > 0.f)) return;
-      const float s2 = yy / A;
-      op += q * p * s2;
-      ox += a * s2;
-      oy += b * s2;
-      oz += c * s2;
-    };
-    one(P.x, X.x, Y.x, Z.x, y.x, bp.x, bx.x, by.x, bz.x);
-    one(P.y, X.y, Y.y, Z.y, y.y, bp.y, bx.y, by.y, bz.y);
-    one(P.z, X.z, Y.z, Z.z, y.z, bp.z, bx.z, by.z, bz.z);
-    one(P.w, X.w, Y.w, Z.w, y.w, bp.w, bx.w, by.w, bz.w);
-    st4v(bpsi, idx, bp);
-    st4v(bgx, idx, bx);
-    st4v(bgy, idx, by);
-    st4v(bgz, idx, bz);
-  }
-};
-
 // parameter-gradient slots
 enum { PG_ALPHA = 0, PG_BETA = 1, PG_GAMMA = 2, PG_NU = 3, PG_RHO0 = 4, PG_KP = 5, PG_COUNT = 8 };
 
-// Block sum of v (in its own precision: the FP32 adjoint sums a block in FP32) added in
-// FP64 to this block's own cell of parameter slot `slot` (all threads of the block must
-// call). The cells sit after the PG_COUNT totals, gridDim.x per slot, and
-// are summed in a fixed order by pg_reduce_kernel, so the parameter gradients do not
-// depend on the order in which blocks finish (no atomics).
-template <typename V> __device__ __forceinline__ void block_accum(V v, double* pgrad, int slot) {
-  __shared__ V shv[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+// The pointwise adjoint kernels take four consecutive points of one z line per thread
+// (every extent is a power of two >= 4) and move them with vector accesses (V4).
+struct Pt4 {
+  long long idx;  // the first of the four points
+  int i, j, k;    // its coordinates; the others are (i, j, k + 1 .. k + 3)
+};
+__device__ __forceinline__ bool pt4(const Grid& g, Pt4& p) {
+  p.idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (p.idx >= g.ng) return false;
+  decompose(g, p.idx, p.i, p.j, p.k);
+  return true;
+}
+static inline unsigned pt4_blocks(const Grid& g) { return (unsigned)((g.ng / 4 + 255) / 256); }
+
+// Parameter-gradient cells: ceil(n^3 / 256) per slot after the PG_COUNT totals (the
+// cells of blocks a kernel does not launch stay zero).
+__device__ __forceinline__ size_t pg_cells(const Grid& g) { return (size_t)((g.ng + 255) / 256); }
+
+// Block sums of v[0 .. NS) (in their own precision: the FP32 adjoint sums a block in
+// FP32) added in FP64 to this block's own cell of the parameter slots slot[0 .. NS).
+// Every thread of the block calls it, once per kernel. pg_reduce_kernel sums the cells
+// in a fixed order, so the parameter gradients do not depend on the order in which
+// blocks finish (no atomics).
+template <typename V, int NS>
+__device__ __forceinline__ void block_accum(const V (&v)[NS], const int (&slot)[NS], const Grid& g,
+                                            double* pgrad) {
+  __shared__ V shv[NS][32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 0; s < NS; ++s) {
+    V t = v[s];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) shv[s][w] = t;
+  }
   __syncthreads();
-  if (lane == 0) shv[w] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  if ((int)threadIdx.x < NS) {
+    const int s = threadIdx.x;
     V t = 0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += shv[q];
-    pgrad[PG_COUNT + (size_t)slot * gridDim.x + blockIdx.x] += (double)t;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += shv[s][q];
+    pgrad[PG_COUNT + (size_t)slot[s] * pg_cells(g) + blockIdx.x] += (double)t;
   }
 }
-
 
 // pgrad[s] = sum over the nblk cells of slot s, in a fixed order (one block per slot,
 // 256 threads).
@@ -221,63 +158,99 @@ template <typename T> struct AdjScalars {
 template <typename T>
 __global__ void __launch_bounds__(256) adj_cn_kernel(Grid g, const T* qx, const T* qy, const T* qz,
                                                      AdjScalars<T> s, int first, const T* Qold, const T* Qnew,
-                                                     T* bQ, T* bQo, T* bNlo, T* bNlq,
-                                                     double* pgrad) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  T da = 0;
-  if (idx < g.ng) {
-    int i, j, k;
-    decompose(g, idx, i, j, k);
-    const T mq2 = qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k];
-    const T sq = s.q02 - mq2;
-    const T aLin = s.ep - s.alpha * (sq * sq);
-    const T C1 = T(2.0) - s.dt * s.rho_m * aLin, C2 = T(1.5) - s.dt * s.rho_m * aLin;
+                                                     T* bQ, T* bQo, T* bNlo, T* bNlq, double* pgrad) {
+  Pt4 p;
+  T da[1] = {T(0.0)};
+  if (pt4(g, p)) {
+    const long long x = p.idx;
+    V4<T> bq, nlo, qo, q0, q1, nl;
+    bq.load(bQ, x);
+    nlo.load(bNlo, x);
+    qo.load(bQo, x);
+    q0.load(Qold, x);
+    q1.load(Qnew, x);
+    const T qxy = qx[p.i] * qx[p.i] + qy[p.j] * qy[p.j];
     const T h = s.dtd2 * s.scale;
-    const T bq = bQ[idx];
-    if constexpr (sizeof(T) == 8) {  // the FP64 adjoint keeps its divisions
-      T bnl = T(3.0) * h / C2 * bq + bNlo[idx];
-      if (first) bnl += -h / C2 * bq;  // REF:2170-2172: Nl_old = Nl at nLoop == 1
-      bNlq[idx] = bnl;
-      bNlo[idx] = first ? T(0.0) : -h / C2 * bq;
-      const T bqo_next = bQo[idx];
-      bQo[idx] = -T(0.5) / C2 * bq;
-      bQ[idx] = C1 / C2 * bq + bqo_next;
-      // dC1/dalpha = dC2/dalpha = dt rho_m sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
-      da = bq * s.dt * s.rho_m * sq * sq * (Qold[idx] - Qnew[idx]) / C2;
-    } else {  // FP32: one reciprocal
-      const T r = T(1.0) / C2, hb = h * r * bq;
-      T bnl = T(3.0) * hb + bNlo[idx];
-      if (first) bnl -= hb;
-      bNlq[idx] = bnl;
-      bNlo[idx] = first ? T(0.0) : -hb;
-      const T bqo_next = bQo[idx];
-      bQo[idx] = -T(0.5) * r * bq;
-      bQ[idx] = C1 * r * bq + bqo_next;
-      da = bq * s.dt * s.rho_m * sq * sq * (Qold[idx] - Qnew[idx]) * r;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const T kz = qz[p.k + e];
+      const T sq = s.q02 - (qxy + kz * kz);
+      const T aLin = s.ep - s.alpha * (sq * sq);
+      const T C1 = T(2.0) - s.dt * s.rho_m * aLin, C2 = T(1.5) - s.dt * s.rho_m * aLin;
+      const T b = bq.v[e];
+      if constexpr (sizeof(T) == 8) {  // the FP64 adjoint keeps its divisions
+        T bnl = T(3.0) * h / C2 * b + nlo.v[e];
+        if (first) bnl += -h / C2 * b;  // REF:2170-2172: Nl_old = Nl at nLoop == 1
+        nl.v[e] = bnl;
+        nlo.v[e] = first ? T(0.0) : -h / C2 * b;
+        bq.v[e] = C1 / C2 * b + qo.v[e];
+        qo.v[e] = -T(0.5) / C2 * b;
+        // dC1/dalpha = dC2/dalpha = dt rho_m sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
+        da[0] += b * s.dt * s.rho_m * sq * sq * (q0.v[e] - q1.v[e]) / C2;
+      } else {  // FP32: one reciprocal
+        const T r = T(1.0) / C2, hb = h * r * b;
+        T bnl = T(3.0) * hb + nlo.v[e];
+        if (first) bnl -= hb;
+        nl.v[e] = bnl;
+        nlo.v[e] = first ? T(0.0) : -hb;
+        bq.v[e] = C1 * r * b + qo.v[e];
+        qo.v[e] = -T(0.5) * r * b;
+        da[0] += b * s.dt * s.rho_m * sq * sq * (q0.v[e] - q1.v[e]) * r;
+      }
     }
+    nl.store(bNlq, x);
+    nlo.store(bNlo, x);
+    bq.store(bQ, x);
+    qo.store(bQo, x);
   }
-  block_accum(da, pgrad, PG_ALPHA);
+  const int slots[1] = {PG_ALPHA};
+  block_accum(da, slots, g, pgrad);
 }
 
 // Transpose of dq = q . f-hat shifted (REF:2076-2078, subtracted from Nl-hat): f-hat_a
-// at c receives -Vq_a[c+1] bar(Nlq) at c+1.
+// at c receives -Vq_a[c+1] bar(Nlq) at c+1. Each output is stored times the input
+// weights (wx, wy, wz) of the transposed transform it feeds.
 template <typename T>
 __global__ void __launch_bounds__(256) adj_dq_kernel(Grid g, const T* qx, const T* qy, const T* qz,
-                                                     const T* bNlq, T* bfx, T* bfy, T* bfz) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.ng) return;
-  int i, j, k;
-  decompose(g, idx, i, j, k);
-  const long long sx = 1LL << (g.ly + g.lz), sy = g.nz;
-  bfx[idx] = (i + 1 < g.nx) ? -qx[i + 1] * bNlq[idx + sx] : T(0.0);
-  bfy[idx] = (j + 1 < g.ny) ? -qy[j + 1] * bNlq[idx + sy] : T(0.0);
-  bfz[idx] = (k + 1 < g.nz) ? -qz[k + 1] * bNlq[idx + 1] : T(0.0);
+                                                     const T* bNlq, T* bfx, T* bfy, T* bfz, AxisWeights<T> wx,
+                                                     AxisWeights<T> wy, AxisWeights<T> wz) {
+  Pt4 p;
+  if (!pt4(g, p)) return;
+  const int i = p.i, j = p.j, k = p.k;
+  const long long x = p.idx, sx = 1LL << (g.ly + g.lz), sy = g.nz;
+  V4<T> f = V4<T>::zero();
+  if (i + 1 < g.nx) {
+    V4<T> n;
+    n.load(bNlq, x + sx);
+    const T q = -qx[i + 1];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) f.v[e] = q * n.v[e] * wx.at(g, i, j, k + e);
+  }
+  f.store(bfx, x);
+  f = V4<T>::zero();
+  if (j + 1 < g.ny) {
+    V4<T> n;
+    n.load(bNlq, x + sy);
+    const T q = -qy[j + 1];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) f.v[e] = q * n.v[e] * wy.at(g, i, j, k + e);
+  }
+  f.store(bfy, x);
+  {
+    V4<T> n;
+    n.load(bNlq, x);
+    const T sh[4] = {n.v[1], n.v[2], n.v[3], (k + 4 < g.nz) ? bNlq[x + 4] : T(0.0)};
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      f.v[e] = (k + e + 1 < g.nz) ? -qz[k + e + 1] * sh[e] * wz.at(g, i, j, k + e) : T(0.0);
+  }
+  f.store(bfz, x);
 }
 
 // Transpose of the density update (REF:2121-2139) and of the real-space Nl
 // (REF:2153-2160, grad.f handled by adj_dq_kernel):
-//   S_rho = -v.grad rho - rho_in divv;  rho' = rho_in + dt (T(1.5) S_rho - T(0.5) F);  F' = S_rho
-//   Nl = -mu + c' (rho' - rho0 - kp A) psi - v.grad psi,  c' = kp zeta/(A + T(0.001))
+//   S_rho = -v.grad rho - rho_in divv;  rho' = rho_in + dt (1.5 S_rho - 0.5 F);  F' = S_rho
+//   Nl = -mu + c' (rho' - rho0 - kp A) psi - v.grad psi,  c' = kp zeta/(A + 0.001)
 // rho_in: the density the forward step used (the relax reset rho0 + kp A, REF:1371,
 // when relax is set). Outputs initialise the real-space cotangent buffers.
 template <typename T> struct AdjNlArgs {
@@ -289,38 +262,79 @@ template <typename T> struct AdjNlArgs {
 };
 template <typename T>
 __global__ void __launch_bounds__(256) adj_nl_kernel(Grid g, AdjNlArgs<T> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  T dkp = 0, drho0 = 0;
-  if (idx < g.ng) {
-    const T b = a.bNl[idx], psi = a.psi[idx], A = a.A[idx];
-    const T rin = a.relax ? a.s.rho0 + a.s.kp * A : a.rho_in[idx];
-    const T rn = a.rho_new[idx];
-    const T den = A + T(0.001);
-    const T cp = a.s.kp * a.s.zeta / den;
-    const T t2 = rn - a.s.rho0 - a.s.kp * A;
-    const T brp = a.bR[idx] + cp * psi * b;  // bar rho'
-    a.bmu[idx] = -b;
-    a.bA[idx] = psi * b * (-a.s.kp * a.s.zeta * t2 / (den * den) - cp * a.s.kp);
-    a.bpsi[idx] = cp * t2 * b;
-    const T vx = a.vx[idx], vy = a.vy[idx], vz = a.vz[idx];
-    const T bS = a.bF[idx] + T(1.5) * a.s.dt * brp;  // bar S_rho
-    a.bgpx[idx] = -vx * b;
-    a.bgpy[idx] = -vy * b;
-    a.bgpz[idx] = -vz * b;
-    a.bvx[idx] = -a.gpx[idx] * b - a.grx[idx] * bS;
-    a.bvy[idx] = -a.gpy[idx] * b - a.gry[idx] * bS;
-    a.bvz[idx] = -a.gpz[idx] * b - a.grz[idx] * bS;
-    a.bgrx[idx] = -vx * bS;
-    a.bgry[idx] = -vy * bS;
-    a.bgrz[idx] = -vz * bS;
-    a.bdivv[idx] = -rin * bS;
-    a.bR[idx] = brp - a.divv[idx] * bS;  // bar rho_in (relax: folded into A later)
-    a.bF[idx] = -T(0.5) * a.s.dt * brp;
-    dkp = b * psi * (a.s.zeta * t2 / den - cp * A);
-    drho0 = -b * psi * cp;
+  Pt4 p;
+  T acc[2] = {T(0.0), T(0.0)};  // kp, rho0
+  if (pt4(g, p)) {
+    const long long x = p.idx;
+    const AdjScalars<T>& s = a.s;
+    V4<T> b, brp, rin, o;
+    {
+      V4<T> psi, A, rn, bR, oA, op;
+      b.load(a.bNl, x);
+      psi.load(a.psi, x);
+      A.load(a.A, x);
+      rn.load(a.rho_new, x);
+      bR.load(a.bR, x);
+      if (a.relax) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) rin.v[e] = s.rho0 + s.kp * A.v[e];
+      } else {
+        rin.load(a.rho_in, x);
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const T den = A.v[e] + T(0.001);
+        const T cp = s.kp * s.zeta / den;
+        const T t2 = rn.v[e] - s.rho0 - s.kp * A.v[e];
+        const T pb = psi.v[e] * b.v[e];
+        brp.v[e] = bR.v[e] + cp * psi.v[e] * b.v[e];  // bar rho'
+        o.v[e] = -b.v[e];
+        oA.v[e] = pb * (-s.kp * s.zeta * t2 / (den * den) - cp * s.kp);
+        op.v[e] = cp * t2 * b.v[e];
+        acc[0] += pb * (s.zeta * t2 / den - cp * A.v[e]);
+        acc[1] += -b.v[e] * psi.v[e] * cp;
+      }
+      o.store(a.bmu, x);
+      oA.store(a.bA, x);
+      op.store(a.bpsi, x);
+    }
+    V4<T> bS;  // bar S_rho
+    {
+      V4<T> bF, dv;
+      bF.load(a.bF, x);
+      dv.load(a.divv, x);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        bS.v[e] = bF.v[e] + T(1.5) * s.dt * brp.v[e];
+        o.v[e] = -rin.v[e] * bS.v[e];
+        bF.v[e] = -T(0.5) * s.dt * brp.v[e];
+        brp.v[e] = brp.v[e] - dv.v[e] * bS.v[e];  // bar rho_in (relax: folded into A later)
+      }
+      o.store(a.bdivv, x);
+      bF.store(a.bF, x);
+      brp.store(a.bR, x);
+    }
+    auto component = [&](const T* v_, const T* gp_, const T* gr_, T* bgp, T* bv, T* bgr) {
+      V4<T> v, gp, gr, ov, og;
+      v.load(v_, x);
+      gp.load(gp_, x);
+      gr.load(gr_, x);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        o.v[e] = -v.v[e] * b.v[e];
+        ov.v[e] = -gp.v[e] * b.v[e] - gr.v[e] * bS.v[e];
+        og.v[e] = -v.v[e] * bS.v[e];
+      }
+      o.store(bgp, x);
+      ov.store(bv, x);
+      og.store(bgr, x);
+    };
+    component(a.vx, a.gpx, a.grx, a.bgpx, a.bvx, a.bgrx);
+    component(a.vy, a.gpy, a.gry, a.bgpy, a.bvy, a.bgry);
+    component(a.vz, a.gpz, a.grz, a.bgpz, a.bvz, a.bgrz);
   }
-  block_accum(dkp, a.pgrad, PG_KP);
-  block_accum(drho0, a.pgrad, PG_RHO0);
+  const int slots[2] = {PG_KP, PG_RHO0};
+  block_accum(acc, slots, g, a.pgrad);
 }
 
 // Transpose of the Stokes solve, part 1 (REF:1581-1974 and the divergence REF:2076):
@@ -330,67 +344,102 @@ __global__ void __launch_bounds__(256) adj_nl_kernel(Grid g, AdjNlArgs<T> a) {
 //   bfgp_a(o)     =  (CM1/(lam+2nu)) Vs bar virr   (the f-grad'(o + e_a) term)
 // with bar vsol = bar v-hat_a, bar virr = bar v-hat_a + Vq_a[o_a+1] bar divv-hat(o + e_a);
 // zero elsewhere. nu_bar += bar vsol (-vsol/nu) + bar virr (-2 virr/(lam + 2nu)).
+// bar v-hat_a and bar divv-hat arrive without the output weights of the transposed
+// transforms that made them (wv[a], wdq), which are applied here.
 template <typename T> struct AdjStokesArgs {
   const T *bvx, *bvy, *bvz, *bdq, *vsx_, *vsy_, *vsz_, *vix, *viy, *viz;
   T *bdotx, *bdoty, *bdotz, *bsx, *bsy, *bsz, *bgx, *bgy, *bgz;
   const T *vqx, *vqy, *vqz, *vsx, *vsy, *vsz, *gqx, *gqy, *gqz, *gsx, *gsy, *gsz;
   T scale, inv_nu, inv_lam2nu, nu, lam2nu;
   int block;
+  AxisWeights<T> wvx, wvy, wvz, wdq;
   double* pgrad;
 };
 template <typename T>
 __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs<T> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  T dnu = 0;
-  if (idx < g.ng) {
-    int i, j, k;
-    decompose(g, idx, i, j, k);
-    const long long sx = 1LL << (g.ly + g.lz), sy = g.nz;
-    const T qxi = a.vqx[i], qyj = a.vqy[j], qzk = a.vqz[k];
-    T d = 0, sd = 0, fp = 0;
+  Pt4 p;
+  T dnu[1] = {T(0.0)};
+  if (pt4(g, p)) {
+    const int i = p.i, j = p.j, k = p.k;
+    const long long x = p.idx, sx = 1LL << (g.ly + g.lz), sy = g.nz;
+    const T qxi = a.vqx[i], qyj = a.vqy[j];
+    V4<T> d = V4<T>::zero(), sd = V4<T>::zero(), fp = V4<T>::zero();
     if (i < g.nx - 1) {
-      const T s_ = a.vsx[i];
-      const T inv = T(1.0) / (s_ * s_ + qyj * qyj + qzk * qzk);
-      const T CM1 = a.scale * inv, CM2 = s_ * inv, G = a.gsx[i] * a.gqy[j] * a.gqz[k];
-      const T bvs = a.bvx[idx];
-      const T bvi = bvs + a.vqx[i + 1] * a.bdq[idx + sx];
-      d = -(CM1 * a.inv_nu) * CM2 * bvs + (CM1 * a.inv_lam2nu) * CM2 * G * bvi;
-      sd = (CM1 * a.inv_nu) * bvs;
-      fp = (CM1 * a.inv_lam2nu) * s_ * bvi;
-      dnu += bvs * (-a.vsx_[idx] / a.nu) + bvi * (-T(2.0) * a.vix[idx] / a.lam2nu);
-    }
-    a.bdotx[idx] = d; a.bsx[idx] = sd; a.bgx[idx] = fp;
-    T dy = 0, sdy = 0, fpy = 0, dz = 0, sdz = 0, fpz = 0;
-    if (j < g.ny - 1 && k < g.nz - 1) {
-      {
-        const T s_ = a.vsy[j];
-        const T inv = T(1.0) / (qxi * qxi + s_ * s_ + qzk * qzk);
-        const T CM1 = a.scale * inv, CM2 = s_ * inv, G = a.gqx[i] * a.gsy[j] * a.gqz[k];
-        const T bvs = a.bvy[idx];
-        const T bvi = bvs + a.vqy[j + 1] * a.bdq[idx + sy];
-        dy = -(CM1 * a.inv_nu) * CM2 * bvs + (CM1 * a.inv_lam2nu) * CM2 * G * bvi;
-        sdy = (CM1 * a.inv_nu) * bvs;
-        fpy = (CM1 * a.inv_lam2nu) * s_ * bvi;
-        dnu += bvs * (-a.vsy_[idx] / a.nu) + bvi * (-T(2.0) * a.viy[idx] / a.lam2nu);
-      }
-      {
-        const T s_ = a.vsz[k];
-        const T inv = T(1.0) / (qxi * qxi + qyj * qyj + s_ * s_);
-        const T CM1 = a.scale * inv, CM2 = s_ * inv;
-        const bool q1 = (k == 0) && (j > 0) && (i % a.block != 0);  // REF:1932
-        const T G = q1 ? (a.gqx[i] * a.gsy[j] * a.gqz[k]) : (a.gqx[i] * a.gqy[j] * a.gsz[k]);
-        const T bvs = a.bvz[idx];
-        const T bvi = bvs + a.vqz[k + 1] * a.bdq[idx + 1];
-        dz = -(CM1 * a.inv_nu) * CM2 * bvs + (CM1 * a.inv_lam2nu) * CM2 * G * bvi;
-        sdz = (CM1 * a.inv_nu) * bvs;
-        fpz = (CM1 * a.inv_lam2nu) * s_ * bvi;
-        dnu += bvs * (-a.vsz_[idx] / a.nu) + bvi * (-T(2.0) * a.viz[idx] / a.lam2nu);
+      V4<T> bv, dq, vs, vi;
+      bv.load(a.bvx, x);
+      dq.load(a.bdq, x + sx);
+      vs.load(a.vsx_, x);
+      vi.load(a.vix, x);
+      const T s_ = a.vsx[i], q1 = a.vqx[i + 1], gxy = a.gsx[i] * a.gqy[j];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const T qzk = a.vqz[k + e];
+        const T inv = T(1.0) / (s_ * s_ + qyj * qyj + qzk * qzk);
+        const T CM1 = a.scale * inv, CM2 = s_ * inv, G = gxy * a.gqz[k + e];
+        const T bvs = bv.v[e] * a.wvx.at(g, i, j, k + e);
+        const T bvi = bvs + q1 * (dq.v[e] * a.wdq.at(g, i + 1, j, k + e));
+        d.v[e] = -(CM1 * a.inv_nu) * CM2 * bvs + (CM1 * a.inv_lam2nu) * CM2 * G * bvi;
+        sd.v[e] = (CM1 * a.inv_nu) * bvs;
+        fp.v[e] = (CM1 * a.inv_lam2nu) * s_ * bvi;
+        dnu[0] += bvs * (-vs.v[e] * a.inv_nu) + bvi * (-T(2.0) * vi.v[e] * a.inv_lam2nu);
       }
     }
-    a.bdoty[idx] = dy; a.bsy[idx] = sdy; a.bgy[idx] = fpy;
-    a.bdotz[idx] = dz; a.bsz[idx] = sdz; a.bgz[idx] = fpz;
+    d.store(a.bdotx, x);
+    sd.store(a.bsx, x);
+    fp.store(a.bgx, x);
+    V4<T> dy = V4<T>::zero(), sdy = V4<T>::zero(), fpy = V4<T>::zero();
+    V4<T> dz = V4<T>::zero(), sdz = V4<T>::zero(), fpz = V4<T>::zero();
+    if (j < g.ny - 1) {
+      V4<T> bvy, dqy, vsy, viy, bvz, dqz, vsz, viz;
+      bvy.load(a.bvy, x);
+      dqy.load(a.bdq, x + sy);
+      vsy.load(a.vsy_, x);
+      viy.load(a.viy, x);
+      bvz.load(a.bvz, x);
+      dqz.load(a.bdq, x);
+      vsz.load(a.vsz_, x);
+      viz.load(a.viz, x);
+      const T dq4 = (k + 4 < g.nz) ? a.bdq[x + 4] : T(0.0);
+      const T dzs[4] = {dqz.v[1], dqz.v[2], dqz.v[3], dq4};  // bar divv-hat at k + e + 1
+      const T sy_ = a.vsy[j], qy1 = a.vqy[j + 1];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (k + e >= g.nz - 1) continue;
+        const T qzk = a.vqz[k + e];
+        {
+          const T inv = T(1.0) / (qxi * qxi + sy_ * sy_ + qzk * qzk);
+          const T CM1 = a.scale * inv, CM2 = sy_ * inv, G = a.gqx[i] * a.gsy[j] * a.gqz[k + e];
+          const T bvs = bvy.v[e] * a.wvy.at(g, i, j, k + e);
+          const T bvi = bvs + qy1 * (dqy.v[e] * a.wdq.at(g, i, j + 1, k + e));
+          dy.v[e] = -(CM1 * a.inv_nu) * CM2 * bvs + (CM1 * a.inv_lam2nu) * CM2 * G * bvi;
+          sdy.v[e] = (CM1 * a.inv_nu) * bvs;
+          fpy.v[e] = (CM1 * a.inv_lam2nu) * sy_ * bvi;
+          dnu[0] += bvs * (-vsy.v[e] * a.inv_nu) + bvi * (-T(2.0) * viy.v[e] * a.inv_lam2nu);
+        }
+        {
+          const T s_ = a.vsz[k + e];
+          const T inv = T(1.0) / (qxi * qxi + qyj * qyj + s_ * s_);
+          const T CM1 = a.scale * inv, CM2 = s_ * inv;
+          const bool q1 = (k + e == 0) && (j > 0) && (i % a.block != 0);  // REF:1932
+          const T G = q1 ? (a.gqx[i] * a.gsy[j] * a.gqz[k + e]) : (a.gqx[i] * a.gqy[j] * a.gsz[k + e]);
+          const T bvs = bvz.v[e] * a.wvz.at(g, i, j, k + e);
+          const T bvi = bvs + a.vqz[k + e + 1] * (dzs[e] * a.wdq.at(g, i, j, k + e + 1));
+          dz.v[e] = -(CM1 * a.inv_nu) * CM2 * bvs + (CM1 * a.inv_lam2nu) * CM2 * G * bvi;
+          sdz.v[e] = (CM1 * a.inv_nu) * bvs;
+          fpz.v[e] = (CM1 * a.inv_lam2nu) * s_ * bvi;
+          dnu[0] += bvs * (-vsz.v[e] * a.inv_nu) + bvi * (-T(2.0) * viz.v[e] * a.inv_lam2nu);
+        }
+      }
+    }
+    dy.store(a.bdoty, x);
+    sdy.store(a.bsy, x);
+    fpy.store(a.bgy, x);
+    dz.store(a.bdotz, x);
+    sdz.store(a.bsz, x);
+    fpz.store(a.bgz, x);
   }
-  block_accum(dnu, a.pgrad, PG_NU);
+  const int slots[1] = {PG_NU};
+  block_accum(dnu, slots, g, a.pgrad);
 }
 
 // Transpose of the Stokes solve, part 2: gather at each input mode p the terms of
@@ -400,49 +449,131 @@ __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs<
 //   S_z(p): dot_z(p) w Vs_z[p_z]; dot_x(p_x-1, p_y, p_z+1) w Vq_z[p_z+1]; dot_y(p_x, p_y-1, p_z+1) w Vq_z[p_z+1]
 //   fgrad'(p) = sum_a bfgp_a(p - e_a)
 // bar dot and bfgp are zero outside each component's computed modes, so only the
-// array bounds are tested. Then f-grad-hat_bar = fgrad'_bar, E-hat_bar = G fgrad'_bar (REF:1486).
+// array bounds are tested. Then f-grad-hat_bar = fgrad'_bar, E-hat_bar = G fgrad'_bar
+// (REF:1486). Each output is stored times the input weights of the transposed
+// transform it feeds (ws[a] for S_a, w2 for f-grad-hat and E-hat).
 template <typename T> struct AdjStokes2Args {
   const T *bdotx, *bdoty, *bdotz, *bsx, *bsy, *bsz, *bgx, *bgy, *bgz;
   T *bSx, *bSy, *bSz, *bfg, *bE;
   const T *vqx, *vqy, *vqz, *vsx, *vsy, *vsz, *gqx, *gqy, *gqz;
+  AxisWeights<T> wsx, wsy, wsz, w2;
 };
 template <typename T>
 __global__ void __launch_bounds__(256) adj_stokes2_kernel(Grid g, AdjStokes2Args<T> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.ng) return;
-  int i, j, k;
-  decompose(g, idx, i, j, k);
-  const long long sx = 1LL << (g.ly + g.lz), sy = g.nz;
-  T Sx = a.bsx[idx] + a.vsx[i] * a.bdotx[idx];
+  Pt4 p;
+  if (!pt4(g, p)) return;
+  const int i = p.i, j = p.j, k = p.k;
+  const long long x = p.idx, sx = 1LL << (g.ly + g.lz), sy = g.nz;
+  // values at (., ., k - 1 .. k + 2) of a line starting at x: {v[x-1], q0, q1, q2}
+  auto back1 = [&](const T* f, long long at, T (&o)[4]) {
+    V4<T> q;
+    q.load(f, at);
+    o[0] = (k >= 1) ? f[at - 1] : T(0.0);
+    o[1] = q.v[0];
+    o[2] = q.v[1];
+    o[3] = q.v[2];
+  };
+  // values at (., ., k + 1 .. k + 4) of a line starting at x: {q1, q2, q3, v[x+4]}
+  auto fwd1 = [&](const T* f, long long at, T (&o)[4]) {
+    V4<T> q;
+    q.load(f, at);
+    o[0] = q.v[1];
+    o[1] = q.v[2];
+    o[2] = q.v[3];
+    o[3] = (k + 4 < g.nz) ? f[at + 4] : T(0.0);
+  };
+  V4<T> S, t;
+  T sh[4];
+  // S_x
+  S.load(a.bsx, x);
+  t.load(a.bdotx, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) S.v[e] = S.v[e] + a.vsx[i] * t.v[e];
   if (i + 1 < g.nx) {
-    if (j >= 1) Sx += a.vqx[i + 1] * a.bdoty[idx + sx - sy];
-    if (k >= 1) Sx += a.vqx[i + 1] * a.bdotz[idx + sx - 1];
+    const T q = a.vqx[i + 1];
+    if (j >= 1) {
+      t.load(a.bdoty, x + sx - sy);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) S.v[e] += q * t.v[e];
+    }
+    back1(a.bdotz, x + sx, sh);
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (k + e >= 1) S.v[e] += q * sh[e];
   }
-  T Sy = a.bsy[idx] + a.vsy[j] * a.bdoty[idx];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) S.v[e] = S.v[e] * a.wsx.at(g, i, j, k + e);
+  S.store(a.bSx, x);
+  // S_y
+  S.load(a.bsy, x);
+  t.load(a.bdoty, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) S.v[e] = S.v[e] + a.vsy[j] * t.v[e];
   if (j + 1 < g.ny) {
-    if (i >= 1) Sy += a.vqy[j + 1] * a.bdotx[idx - sx + sy];
-    if (k >= 1) Sy += a.vqy[j + 1] * a.bdotz[idx + sy - 1];
+    const T q = a.vqy[j + 1];
+    if (i >= 1) {
+      t.load(a.bdotx, x - sx + sy);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) S.v[e] += q * t.v[e];
+    }
+    back1(a.bdotz, x + sy, sh);
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (k + e >= 1) S.v[e] += q * sh[e];
   }
-  T Sz = a.bsz[idx] + a.vsz[k] * a.bdotz[idx];
-  if (k + 1 < g.nz) {
-    if (i >= 1) Sz += a.vqz[k + 1] * a.bdotx[idx - sx + 1];
-    if (j >= 1) Sz += a.vqz[k + 1] * a.bdoty[idx - sy + 1];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) S.v[e] = S.v[e] * a.wsy.at(g, i, j, k + e);
+  S.store(a.bSy, x);
+  // S_z
+  S.load(a.bsz, x);
+  t.load(a.bdotz, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) S.v[e] = S.v[e] + a.vsz[k + e] * t.v[e];
+  {
+    T sx4[4] = {T(0.0), T(0.0), T(0.0), T(0.0)}, sy4[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
+    if (i >= 1) fwd1(a.bdotx, x - sx, sx4);
+    if (j >= 1) fwd1(a.bdoty, x - sy, sy4);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if (k + e + 1 >= g.nz) continue;
+      if (i >= 1) S.v[e] += a.vqz[k + e + 1] * sx4[e];
+      if (j >= 1) S.v[e] += a.vqz[k + e + 1] * sy4[e];
+    }
   }
-  a.bSx[idx] = Sx;
-  a.bSy[idx] = Sy;
-  a.bSz[idx] = Sz;
-  T fg = 0;
-  if (i >= 1) fg += a.bgx[idx - sx];
-  if (j >= 1) fg += a.bgy[idx - sy];
-  if (k >= 1) fg += a.bgz[idx - 1];
-  a.bfg[idx] = fg;
-  a.bE[idx] = fg * (a.gqx[i] * a.gqy[j] * a.gqz[k]);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) S.v[e] = S.v[e] * a.wsz.at(g, i, j, k + e);
+  S.store(a.bSz, x);
+  // f-grad' and E
+  V4<T> fg = V4<T>::zero();
+  if (i >= 1) {
+    t.load(a.bgx, x - sx);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) fg.v[e] += t.v[e];
+  }
+  if (j >= 1) {
+    t.load(a.bgy, x - sy);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) fg.v[e] += t.v[e];
+  }
+  back1(a.bgz, x, sh);
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (k + e >= 1) fg.v[e] += sh[e];
+  const T gxy = a.gqx[i] * a.gqy[j];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const T w = a.w2.at(g, i, j, k + e);
+    t.v[e] = fg.v[e] * (gxy * a.gqz[k + e]) * w;
+    fg.v[e] = fg.v[e] * w;
+  }
+  fg.store(a.bfg, x);
+  t.store(a.bE, x);
 }
 
 // Transpose of S6 (REF:1385-1425) and of the relax reset (REF:1371-1374):
 //   E = L^2/2, t = rho0 + kp A, fgrad = zeta/2 (rho^2 - t^2), mu1 = lapR + rho L,
 //   S_a = mu1 gpsi_a + E grho_a, mu = lapR + rho P5, P5 = L - ep psi - beta psi^3 + gamma psi^5,
-//   Erho = rho E, c = kp zeta (rho - t)/(A + T(0.001)), f_a = c gpsi_a;
+//   Erho = rho E, c = kp zeta (rho - t)/(A + 0.001), f_a = c gpsi_a;
 //   relax: rho = rho0 + kp A and lapR = rho lapR_raw.
 // bR enters holding bar rho_in from adj_nl_kernel and leaves holding the cotangent
 // of the step's incoming density (zero in the relax phase, whose rho is reset).
@@ -456,82 +587,264 @@ template <typename T> struct AdjS6Args {
 };
 template <typename T>
 __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  T dbeta = 0, dgamma = 0, drho0 = 0, dkp = 0;
-  if (idx < g.ng) {
-    const T A = a.A[idx], L = a.L[idx], psi = a.psi[idx];
-    const T rho = a.relax ? a.s.rho0 + a.s.kp * A : a.rho_in[idx];
-    const T lraw = a.lapR[idx];
-    const T lapR = a.relax ? rho * lraw : lraw;
-    const T gpx = a.gpx[idx], gpy = a.gpy[idx], gpz = a.gpz[idx];
-    const T grx = a.grx[idx], gry = a.gry[idx], grz = a.grz[idx];
-    const T E = T(0.5) * (L * L), t = a.s.rho0 + a.s.kp * A, den = A + T(0.001);
-    const T mu1 = lapR + rho * L;
-    const T c = a.s.kp * a.s.zeta * (rho - t) / den;
-    const T p2 = psi * psi;
-    const T P5 = L - a.s.ep * psi - a.s.beta * (p2 * psi) + a.s.gamma * (p2 * p2 * psi);
-    const T bSx = a.bSx[idx], bSy = a.bSy[idx], bSz = a.bSz[idx];
-    const T bfx = a.bfx[idx], bfy = a.bfy[idx], bfz = a.bfz[idx];
-    const T bmu = a.bmu[idx], bfg = a.bfgrad[idx], bEr = a.bE[idx];
-    const T bmu1 = bSx * gpx + bSy * gpy + bSz * gpz;
-    a.bgpx[idx] += mu1 * bSx + c * bfx;
-    a.bgpy[idx] += mu1 * bSy + c * bfy;
-    a.bgpz[idx] += mu1 * bSz + c * bfz;
-    const T bEn = bSx * grx + bSy * gry + bSz * grz + rho * bEr;
-    a.bgrx[idx] += E * bSx;
-    a.bgry[idx] += E * bSy;
-    a.bgrz[idx] += E * bSz;
-    const T bc = bfx * gpx + bfy * gpy + bfz * gpz;
-    const T blap = bmu1 + bmu;
-    T brho = L * bmu1 + P5 * bmu + E * bEr + a.s.zeta * rho * bfg + (a.s.kp * a.s.zeta / den) * bc;
-    a.bL[idx] = rho * bmu1 + rho * bmu + L * bEn;
-    a.bpsi[idx] += rho * (-a.s.ep - T(3.0) * a.s.beta * p2 + T(5.0) * a.s.gamma * (p2 * p2)) * bmu;
-    const T bt = -a.s.zeta * t * bfg - (a.s.kp * a.s.zeta / den) * bc;
-    T bA = a.s.kp * bt + bc * (-a.s.kp * a.s.zeta * (rho - t) / (den * den));
-    dkp = bt * A + bc * a.s.zeta * (rho - t) / den;
-    drho0 = bt;
-    dbeta = bmu * rho * (-(p2 * psi));
-    dgamma = bmu * rho * (p2 * p2 * psi);
+  Pt4 p;
+  T acc[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};  // beta, gamma, rho0, kp
+  if (pt4(g, p)) {
+    const long long x = p.idx;
+    const AdjScalars<T>& s = a.s;
+    V4<T> A, L, rho, lraw;
+    A.load(a.A, x);
+    L.load(a.L, x);
+    lraw.load(a.lapR, x);
     if (a.relax) {
-      brho += lraw * blap;
-      a.blapR[idx] = rho * blap;
-      const T bri = brho + a.bR[idx];  // every use of the reset density
-      bA += a.s.kp * bri;
-      dkp += A * bri;
-      drho0 += bri;
-      a.bR[idx] = T(0.0);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) rho.v[e] = s.rho0 + s.kp * A.v[e];
     } else {
-      a.blapR[idx] = blap;
-      a.bR[idx] += brho;
+      rho.load(a.rho_in, x);
     }
-    a.bA[idx] += bA;
+    // bmu1 = bS . gpsi, bc = bf . gpsi, bEn = bS . grho + rho bEr, EbE = E bEr
+    V4<T> bSx, bSy, bSz, bmu1, bc, bEn, EbE;
+    bSx.load(a.bSx, x);
+    bSy.load(a.bSy, x);
+    bSz.load(a.bSz, x);
+    {
+      V4<T> bfx, bfy, bfz, gx, gy, gz, mu1, c;
+      bfx.load(a.bfx, x);
+      bfy.load(a.bfy, x);
+      bfz.load(a.bfz, x);
+      gx.load(a.gpx, x);
+      gy.load(a.gpy, x);
+      gz.load(a.gpz, x);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const T t = s.rho0 + s.kp * A.v[e], den = A.v[e] + T(0.001);
+        const T lapR = a.relax ? rho.v[e] * lraw.v[e] : lraw.v[e];
+        mu1.v[e] = lapR + rho.v[e] * L.v[e];
+        c.v[e] = s.kp * s.zeta * (rho.v[e] - t) / den;
+        bmu1.v[e] = bSx.v[e] * gx.v[e] + bSy.v[e] * gy.v[e] + bSz.v[e] * gz.v[e];
+        bc.v[e] = bfx.v[e] * gx.v[e] + bfy.v[e] * gy.v[e] + bfz.v[e] * gz.v[e];
+      }
+      auto upd = [&](T* bg, const V4<T>& bS, const V4<T>& bf) {
+        V4<T> o;
+        o.load(bg, x);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) o.v[e] += mu1.v[e] * bS.v[e] + c.v[e] * bf.v[e];
+        o.store(bg, x);
+      };
+      upd(a.bgpx, bSx, bfx);
+      upd(a.bgpy, bSy, bfy);
+      upd(a.bgpz, bSz, bfz);
+    }
+    {
+      V4<T> bEr, gx, gy, gz, E;
+      bEr.load(a.bE, x);
+      gx.load(a.grx, x);
+      gy.load(a.gry, x);
+      gz.load(a.grz, x);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        E.v[e] = T(0.5) * (L.v[e] * L.v[e]);
+        bEn.v[e] = bSx.v[e] * gx.v[e] + bSy.v[e] * gy.v[e] + bSz.v[e] * gz.v[e] + rho.v[e] * bEr.v[e];
+        EbE.v[e] = E.v[e] * bEr.v[e];
+      }
+      auto upd = [&](T* bg, const V4<T>& bS) {
+        V4<T> o;
+        o.load(bg, x);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) o.v[e] += E.v[e] * bS.v[e];
+        o.store(bg, x);
+      };
+      upd(a.bgrx, bSx);
+      upd(a.bgry, bSy);
+      upd(a.bgrz, bSz);
+    }
+    {
+      V4<T> psi, bmu, bfg, oA, op, oR, ol, oL;
+      psi.load(a.psi, x);
+      bmu.load(a.bmu, x);
+      bfg.load(a.bfgrad, x);
+      oA.load(a.bA, x);
+      op.load(a.bpsi, x);
+      oR.load(a.bR, x);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const T Ae = A.v[e], Le = L.v[e], pe = psi.v[e], re = rho.v[e], bm = bmu.v[e], bf = bfg.v[e];
+        const T t = s.rho0 + s.kp * Ae, den = Ae + T(0.001);
+        const T p2 = pe * pe;
+        const T P5 = Le - s.ep * pe - s.beta * (p2 * pe) + s.gamma * (p2 * p2 * pe);
+        const T blap = bmu1.v[e] + bm;
+        T brho = Le * bmu1.v[e] + P5 * bm + EbE.v[e] + s.zeta * re * bf + (s.kp * s.zeta / den) * bc.v[e];
+        oL.v[e] = re * bmu1.v[e] + re * bm + Le * bEn.v[e];
+        op.v[e] += re * (-s.ep - T(3.0) * s.beta * p2 + T(5.0) * s.gamma * (p2 * p2)) * bm;
+        const T bt = -s.zeta * t * bf - (s.kp * s.zeta / den) * bc.v[e];
+        T bA = s.kp * bt + bc.v[e] * (-s.kp * s.zeta * (re - t) / (den * den));
+        T dkp = bt * Ae + bc.v[e] * s.zeta * (re - t) / den, drho0 = bt;
+        acc[0] += bm * re * (-(p2 * pe));
+        acc[1] += bm * re * (p2 * p2 * pe);
+        if (a.relax) {
+          brho += lraw.v[e] * blap;
+          ol.v[e] = re * blap;
+          const T bri = brho + oR.v[e];  // every use of the reset density
+          bA += s.kp * bri;
+          dkp += Ae * bri;
+          drho0 += bri;
+          oR.v[e] = T(0.0);
+        } else {
+          ol.v[e] = blap;
+          oR.v[e] += brho;
+        }
+        acc[2] += drho0;
+        acc[3] += dkp;
+        oA.v[e] += bA;
+      }
+      oL.store(a.bL, x);
+      op.store(a.bpsi, x);
+      ol.store(a.blapR, x);
+      oR.store(a.bR, x);
+      oA.store(a.bA, x);
+    }
   }
-  block_accum(dbeta, a.pgrad, PG_BETA);
-  block_accum(dgamma, a.pgrad, PG_GAMMA);
-  block_accum(drho0, a.pgrad, PG_RHO0);
-  block_accum(dkp, a.pgrad, PG_KP);
+  const int slots[4] = {PG_BETA, PG_GAMMA, PG_RHO0, PG_KP};
+  block_accum(acc, slots, g, a.pgrad);
 }
 
 // bQ += Lambda(q) Y for the spectral multipliers of the forward (REF:1302 for
 // dfDlapPsi, REF:1356 for the relax-phase Laplacian), and alpha_bar += Y dLambda/dalpha Q.
 //   mode 0: Lambda = alpha (q0^2 - q^2);   mode 1: Lambda = -q^2 alpha (q0^2 - q^2)
+// Y arrives without the output weights wy of the transposed transform that made it.
 template <typename T>
-__global__ void __launch_bounds__(256) adj_acc_spec_kernel(Grid g, const T* qx, const T* qy,
-                                                           const T* qz, int mode, T alpha, T q02,
-                                                           const T* Y, const T* Q, T* bQ,
-                                                           double* pgrad) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  T da = 0;
-  if (idx < g.ng) {
-    int i, j, k;
-    decompose(g, idx, i, j, k);
-    const T mq2 = qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k];
-    const T dl = mode == 0 ? (q02 - mq2) : -mq2 * (q02 - mq2);  // dLambda/dalpha
-    const T y = Y[idx];
-    bQ[idx] += alpha * dl * y;
-    da = y * dl * Q[idx];
+__global__ void __launch_bounds__(256) adj_acc_spec_kernel(Grid g, const T* qx, const T* qy, const T* qz,
+                                                           int mode, T alpha, T q02, AxisWeights<T> wy,
+                                                           const T* Y, const T* Q, T* bQ, double* pgrad) {
+  Pt4 p;
+  T da[1] = {T(0.0)};
+  if (pt4(g, p)) {
+    const long long x = p.idx;
+    V4<T> y, q, b;
+    y.load(Y, x);
+    q.load(Q, x);
+    b.load(bQ, x);
+    const T qxy = qx[p.i] * qx[p.i] + qy[p.j] * qy[p.j];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const T kz = qz[p.k + e];
+      const T mq2 = qxy + kz * kz;
+      const T dl = mode == 0 ? (q02 - mq2) : -mq2 * (q02 - mq2);  // dLambda/dalpha
+      const T ye = y.v[e] * wy.at(g, p.i, p.j, p.k + e);
+      b.v[e] += alpha * dl * ye;
+      da[0] += ye * dl * q.v[e];
+    }
+    b.store(bQ, x);
   }
-  block_accum(da, pgrad, PG_ALPHA);
+  const int slots[1] = {PG_ALPHA};
+  block_accum(da, slots, g, pgrad);
+}
+
+// Transpose of A_raw = sqrt(q0^2 psi^2 + |grad psi|^2) (REF:1262-1266), applied to
+// y = F(bar A) (the amplitude filter F of REF:1271-1288 is symmetric).
+template <typename T>
+__global__ void __launch_bounds__(256) adj_amp_kernel(Grid g, const T* y, const T* psi, const T* gx, const T* gy,
+                                                      const T* gz, T q02, T* bpsi, T* bgx, T* bgy, T* bgz) {
+  Pt4 p;
+  if (!pt4(g, p)) return;
+  const long long x = p.idx;
+  V4<T> Y, P, X, G, Z, bp, bx, by, bz;
+  Y.load(y, x);
+  P.load(psi, x);
+  X.load(gx, x);
+  G.load(gy, x);
+  Z.load(gz, x);
+  bp.load(bpsi, x);
+  bx.load(bgx, x);
+  by.load(bgy, x);
+  bz.load(bgz, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const T pe = P.v[e], ae = X.v[e], be = G.v[e], ce = Z.v[e];
+    const T A = sqrt(q02 * (pe * pe) + (ae * ae) + (be * be) + (ce * ce));
+    if (!(A > T(0.0))) continue;  // the square root is not differentiable at 0: no contribution
+    const T sc = Y.v[e] / A;
+    bp.v[e] += q02 * pe * sc;
+    bx.v[e] += ae * sc;
+    by.v[e] += be * sc;
+    bz.v[e] += ce * sc;
+  }
+  bp.store(bpsi, x);
+  bx.store(bgx, x);
+  by.store(bgy, x);
+  bz.store(bgz, x);
+}
+
+// Transpose of the shifted spectral derivatives of the gradients (REF:1166-1250): the
+// forward wrote grad_a-hat[c] = -fac Vs_a[c] X-hat[c+1] (c < n_a - 1), so with g_a the
+// transposed inverse transform of grad_a-bar (without its output weights w[a]),
+//   X-bar[c'] += -fac Vs_a[c'-1] w[a](c'-1) g_a[c'-1]   (c' >= 1).
+// Both families at once: psi-hat (fac 1, added to bQ) and rho-hat (fac = scale,
+// written to bRq times the input weights w2 of the transposed transform it feeds).
+template <typename T> struct AdjGradArgs {
+  const T *gpx, *gpy, *gpz, *grx, *gry, *grz;
+  T *bQ, *bRq;
+  const T *vsx, *vsy, *vsz;
+  T scale;
+  AxisWeights<T> wx, wy, wz, w2;
+};
+template <typename T>
+__global__ void __launch_bounds__(256) adj_grad_kernel(Grid g, AdjGradArgs<T> a) {
+  Pt4 p;
+  if (!pt4(g, p)) return;
+  const int i = p.i, j = p.j, k = p.k;
+  const long long x = p.idx, sx = 1LL << (g.ly + g.lz), sy = g.nz;
+  auto gather = [&](const T* fx, const T* fy, const T* fz, T fac, V4<T>& acc) {
+    V4<T> t;
+    if (i >= 1) {
+      t.load(fx, x - sx);
+      const T c = -fac * a.vsx[i - 1];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc.v[e] += c * (t.v[e] * a.wx.at(g, i - 1, j, k + e));
+    }
+    if (j >= 1) {
+      t.load(fy, x - sy);
+      const T c = -fac * a.vsy[j - 1];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc.v[e] += c * (t.v[e] * a.wy.at(g, i, j - 1, k + e));
+    }
+    t.load(fz, x);
+    const T sh[4] = {(k >= 1) ? fz[x - 1] : T(0.0), t.v[0], t.v[1], t.v[2]};
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (k + e >= 1) acc.v[e] += (-fac * a.vsz[k + e - 1]) * (sh[e] * a.wz.at(g, i, j, k + e - 1));
+  };
+  V4<T> q, r = V4<T>::zero();
+  q.load(a.bQ, x);
+  gather(a.gpx, a.gpy, a.gpz, T(1.0), q);
+  q.store(a.bQ, x);
+  gather(a.grx, a.gry, a.grz, a.scale, r);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) r.v[e] = r.v[e] * a.w2.at(g, i, j, k + e);
+  r.store(a.bRq, x);
+}
+
+// End of the adjoint step, the transposes of psi = DCT-III^3 psiq and of
+// rho-hat = DCT-II^3 rho (REF:1104-1106): bQ += wq ypsi, bR += yrho (ypsi without the
+// output weights wq of its transposed transform).
+template <typename T>
+__global__ void __launch_bounds__(256) adj_fold_kernel(Grid g, const T* ypsi, AxisWeights<T> wq, const T* yrho,
+                                                       T* bQ, T* bR) {
+  Pt4 p;
+  if (!pt4(g, p)) return;
+  const long long x = p.idx;
+  V4<T> yp, yr, q, r;
+  yp.load(ypsi, x);
+  yr.load(yrho, x);
+  q.load(bQ, x);
+  r.load(bR, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    q.v[e] = q.v[e] + yp.v[e] * wq.at(g, p.i, p.j, p.k + e);
+    r.v[e] += yr.v[e];
+  }
+  q.store(bQ, x);
+  r.store(bR, x);
 }
 
 // out = a * x (+ b * y): small helper for the final dL/dpsi0 = scale C2^T (bQ + bQo).
