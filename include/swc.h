@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define SWC_ABI_VERSION 2
+#define SWC_ABI_VERSION 3
 
 /* ---- status codes ---------------------------------------------------------- */
 enum {
@@ -128,6 +128,11 @@ typedef struct swc_params {
                             the device's free memory at the call less 1 GB. */
   int adjoint_snapshots; /* adjoint_ckpt = -1: at most this many snapshots (<= 0: as
                             many as fit under the cap) */
+  int diag_interval;  /* when the diagnostics of :2202-2262 run: 0 = at the last step of
+                         every swc_step call; K > 0 = at the steps with nLoop % K == 0
+                         (the reference's cadence is K = 50, :2202), so a loop of
+                         swc_step(ctx, 1) calls pays for them every K steps only. The
+                         non-finite check and the energy-density field come with them. */
 } swc_params;
 
 /* Gradients returned by swc_backward: dL/d(coefficient) of the coefficients the
@@ -143,7 +148,8 @@ typedef struct swc_grad {
   int64_t snapshots;      /* state snapshot slots used (binomial mode; 0 otherwise) */
 } swc_grad;
 
-/* Diagnostics of the last step of a swc_step call (smaiso-wcomp.cpp:2202-2262). */
+/* Diagnostics of the last diagnostic step (smaiso-wcomp.cpp:2202-2262; see
+ * swc_params.diag_interval): by default the last step of the last swc_step call. */
 typedef struct swc_diag {
   double l1;          /* sum|psi-psi_old| / (dt sum|psi|)        (:2246) */
   double mass;        /* sum rho * dx^3                          (:2252) */
@@ -152,7 +158,7 @@ typedef struct swc_diag {
   double sum_abs_psi;
   double sum_rho;
   double sum_energy;
-  int64_t step;       /* nLoop after the call */
+  int64_t step;       /* nLoop of the step they describe */
   int64_t nonfinite;  /* count of non-finite psi/rho values */
 } swc_diag;
 
@@ -205,6 +211,19 @@ int swc_diagnostics(swc_ctx* ctx, swc_diag* out);
  * host memory gets a direct DMA copy; the mixed engine widens FP32 fields on the
  * device into a staging buffer it allocates on the first such call. */
 int swc_get_field(swc_ctx* ctx, int field, double* dst);
+
+/* Asynchronous swc_get_field for a field read after every step (the loop's output,
+ * REF:2273-2446, taken more often than the reference's every 500 steps): the field is
+ * snapshotted in FP64 on the context's stream (widened from FP32 by the mixed engine)
+ * and copied to dst on a second stream, so the copy overlaps the swc_step calls that
+ * follow. dst must stay valid until the copy completes, and must be pinned host memory
+ * for the copy to run asynchronously. Two snapshot buffers (2 * nx*ny*nz doubles,
+ * allocated on the first call) alternate: a call first waits for the copy issued two
+ * calls before it, so when it returns the destination of the call before last holds
+ * its field; swc_get_field_wait completes every pending copy. Errors of a copy are
+ * returned by the call that waits for it. */
+int swc_get_field_async(swc_ctx* ctx, int field, double* dst);
+int swc_get_field_wait(swc_ctx* ctx);
 
 /* Device pointer of a field in the context's own precision (8-byte elements for
  * FP64 fields, 4-byte for FP32 work fields of the mixed path); *elem_bytes tells

@@ -38,7 +38,8 @@ FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 EXPORTS = [
     "swc_abi_version", "swc_strerror", "swc_last_error", "swc_default_params", "swc_derive",
     "swc_create", "swc_destroy", "swc_set_state", "swc_step", "swc_diagnostics",
-    "swc_get_field", "swc_field_device_ptr", "swc_get_step", "swc_last_step_ms",
+    "swc_get_field", "swc_get_field_async", "swc_get_field_wait", "swc_field_device_ptr", "swc_get_step",
+    "swc_last_step_ms",
     "swc_last_step_launches", "swc_device_fma_peak", "swc_diagnostics_noalloc",
     "swc_backward", "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
     "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host", "swc_r2r_plan_set_wait_test",
@@ -54,7 +55,7 @@ class SwcParams(ctypes.Structure):
         ("rho_0", ctypes.c_double), ("divv_switch", ctypes.c_int), ("load", ctypes.c_int),
         ("ref_ranks", ctypes.c_int), ("precision", ctypes.c_int), ("device", ctypes.c_int),
         ("watchdog_s", ctypes.c_double), ("adjoint_ckpt", ctypes.c_int), ("adjoint_cap_gb", ctypes.c_double),
-        ("adjoint_snapshots", ctypes.c_int),
+        ("adjoint_snapshots", ctypes.c_int), ("diag_interval", ctypes.c_int),
     ]
 
 
@@ -95,7 +96,8 @@ def default_params(nx, ny=None, nz=None, **overrides):
     p = SwcParams(nx=nx, ny=ny, nz=nz, nw=8, dt=0.001, alpha=1.0, beta=2.0, gamma=1.0,
                   ep=-0.001, q0=1.0, nu=1.0, lambda_=1.0, zeta=1.0, rho_0=0.01,
                   divv_switch=50, load=0, ref_ranks=2, precision=SWC_PREC_FP64, device=0,
-                  watchdog_s=0.0, adjoint_ckpt=0, adjoint_cap_gb=0.0, adjoint_snapshots=0)
+                  watchdog_s=0.0, adjoint_ckpt=0, adjoint_cap_gb=0.0, adjoint_snapshots=0,
+                  diag_interval=0)
     for k, v in overrides.items():
         setattr(p, "lambda_" if k == "lambda" else k, v)
     return p
@@ -140,6 +142,8 @@ def load_library(path=None):
         "swc_step": (ctypes.c_int, [vp, ctypes.c_int]),
         "swc_diagnostics": (ctypes.c_int, [vp, P(SwcDiag)]),
         "swc_get_field": (ctypes.c_int, [vp, ctypes.c_int, dp]),
+        "swc_get_field_async": (ctypes.c_int, [vp, ctypes.c_int, dp]),
+        "swc_get_field_wait": (ctypes.c_int, [vp]),
         "swc_field_device_ptr": (ctypes.c_int, [vp, ctypes.c_int, P(vp), P(ctypes.c_int)]),
         "swc_get_step": (ctypes.c_int, [vp, P(ctypes.c_int64)]),
         "swc_last_step_ms": (ctypes.c_int, [vp, dp]),

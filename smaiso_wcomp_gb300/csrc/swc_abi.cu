@@ -106,6 +106,10 @@ int validate_params(const swc_params* p) {
     set_error("ref_ranks=%d must be >= 1 and divide nx=%d", p->ref_ranks, p->nx);
     return SWC_ERR_BAD_PARAM;
   }
+  if (p->diag_interval < 0) {
+    set_error("diag_interval must be >= 0");
+    return SWC_ERR_BAD_PARAM;
+  }
   if (p->adjoint_ckpt < -1) {
     set_error("adjoint_ckpt must be -1 (binomial), 0 or K > 0");
     return SWC_ERR_BAD_PARAM;
@@ -186,6 +190,7 @@ int swc_default_params(swc_params* p, int nx, int ny, int nz) {
   p->adjoint_ckpt = 0;
   p->adjoint_cap_gb = 0.0;
   p->adjoint_snapshots = 0;
+  p->diag_interval = 0;
   return SWC_OK;
 }
 
@@ -252,6 +257,17 @@ int swc_get_field(swc_ctx* ctx, int field, double* dst) {
   SWC_NEED_CTX(ctx);
   if (!dst) { set_error("dst is NULL"); return SWC_ERR_BAD_PARAM; }
   SWC_GUARD(ctx->eng->get_field(field, dst));
+}
+
+int swc_get_field_async(swc_ctx* ctx, int field, double* dst) {
+  SWC_NEED_CTX(ctx);
+  if (!dst) { set_error("dst is NULL"); return SWC_ERR_BAD_PARAM; }
+  SWC_GUARD(ctx->eng->get_field_async(field, dst));
+}
+
+int swc_get_field_wait(swc_ctx* ctx) {
+  SWC_NEED_CTX(ctx);
+  SWC_GUARD(ctx->eng->get_field_wait());
 }
 
 int swc_field_device_ptr(swc_ctx* ctx, int field, void** dev_ptr, int* elem_bytes) {

@@ -296,7 +296,7 @@ template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n) {
   };
   SWC_TRY(put(TP_RHOIN, rho_, true));
   const bool relax = !(n > p_.divv_switch || p_.load == 1);
-  SWC_TRY(run_graph(relax, n == 1, true));  // the diagnostic variant keeps psi_old and v_sol
+  SWC_TRY(run_graph(relax, n == 1, true, true));  // the diagnostic variant keeps psi_old and v_sol
   const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
                             amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
                             vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
@@ -310,7 +310,7 @@ template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n) {
 template <typename T> int StepEngine<T>::advance(int64_t from, int64_t k) {
   for (int64_t n = from + 1; n <= from + k; ++n) {
     const bool relax = !(n > p_.divv_switch || p_.load == 1);
-    SWC_TRY(run_graph(relax, n == 1, false));
+    SWC_TRY(run_graph(relax, n == 1, false, false));
   }
   fwd_steps_ += k;
   return SWC_OK;
@@ -453,6 +453,7 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
   double pg[PG_COUNT];
   SWC_CK(cudaMemcpyAsync(pg, pgrad_, sizeof(pg), cudaMemcpyDeviceToHost, stream_));
   SWC_TRY(restore_ckpt(last_slot));
+  diag_step_ = -1;  // the recompute overwrote the energy density
   SWC_CK(cudaStreamSynchronize(stream_));
   // chain rule through Amp(beta, gamma) and kp = (1 - rho_0)/Amp (REF:250-253); rho_s = 1, rho_m = 1/2
   const double disc = std::sqrt(9 * p_.beta * p_.beta + 40 * p_.ep * p_.gamma);

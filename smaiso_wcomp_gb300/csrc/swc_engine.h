@@ -19,6 +19,8 @@ class EngineBase {
   virtual int step(int nsteps) = 0;
   virtual int diagnostics(swc_diag* out) = 0;
   virtual int get_field(int field, double* dst) = 0;
+  virtual int get_field_async(int field, double* dst) = 0;
+  virtual int get_field_wait() = 0;
   virtual int field_ptr(int field, void** ptr, int* elem_bytes) = 0;
   virtual int get_step(int64_t* n) = 0;
   virtual int last_ms(double* ms) = 0;

@@ -817,14 +817,17 @@ template <typename T> __global__ void __launch_bounds__(kDiagThreads) diag_kerne
   }
 }
 
-// Deterministic final sum of the per-block partials (one block, fixed order).
-static __global__ void __launch_bounds__(32) diag_final_kernel(const double* partial, int nblocks, double* out) {
-  const int q = threadIdx.x;
-  if (q < 5) {
-    double t = 0;
-    for (int b = 0; b < nblocks; ++b) t += partial[5 * b + q];
-    out[q] = t;
-  }
+// Deterministic final sum of the per-block partials (one block of 5 warps): warp q sums
+// column q lane-strided, then by a fixed shuffle tree, so the result depends only on
+// the partials and nblocks.
+constexpr int kDiagFinalThreads = 160;
+static __global__ void __launch_bounds__(kDiagFinalThreads) diag_final_kernel(const double* partial, int nblocks,
+                                                                            double* out) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double t = 0;
+  for (int b = lane; b < nblocks; b += 32) t += partial[5 * b + q];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[q] = t;
 }
 
 // ---------------------------------------------------------------------------------
@@ -848,6 +851,8 @@ template <typename T> class StepEngine : public EngineBase {
     return SWC_OK;
   }
   int get_field(int field, double* dst) override;
+  int get_field_async(int field, double* dst) override;
+  int get_field_wait() override;
   int field_ptr(int field, void** ptr, int* elem_bytes) override;
   int get_step(int64_t* n) override {
     *n = nloop_;
@@ -893,6 +898,13 @@ template <typename T> class StepEngine : public EngineBase {
   double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
   int* status_ = nullptr;          // set by a transform pass whose bounded wait ran out
   double* stage_ = nullptr;        // FP64 staging of FP32 fields for swc_get_field
+  // swc_get_field_async: two FP64 snapshots of the field, each copied to the host on
+  // copy_stream_ while the next steps run on stream_
+  cudaStream_t copy_stream_ = nullptr;
+  double* astage_[2] = {nullptr, nullptr};
+  cudaEvent_t aready_[2] = {nullptr, nullptr}, adone_[2] = {nullptr, nullptr};
+  bool apending_[2] = {false, false};
+  int anext_ = 0;
   size_t pgrad_doubles() const { return 8 * (1 + (size_t)((g_.ng + 255) / 256)); }
   bool adj_valid_ = false;         // checkpoints describe the run since swc_set_state
   // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
@@ -912,7 +924,11 @@ template <typename T> class StepEngine : public EngineBase {
   int enqueue_part_c(bool relax, bool first, bool diag);  // S11-S14 (swc_step_part_c.cuh)
   int inverse_velocity(int ax, T* in, T* out);             // (swc_step_part_c.cuh)
   int transform_vsol();                                    // (swc_step_part_c.cuh)
-  int run_graph(bool relax, bool first, bool diag);
+  // diag: the diagnostic variant (S15 reductions, psi_old <- psi rotation, energy field);
+  // vsol: the Stokes kernel also writes v_sol (the last step of a swc_step call)
+  int run_graph(bool relax, bool first, bool diag, bool vsol);
+  bool cap_vsol_ = false;  // vsol flag of the variant being captured
+  int64_t diag_step_ = -1;  // nLoop of the last step that ran the diagnostics
   void release();
   int field_src(int field, const void** src, bool* is_double);
 
@@ -956,7 +972,18 @@ template <typename T> class StepEngine : public EngineBase {
 template <typename T> void StepEngine<T>::release() {
   // queued graphs may still run (e.g. after a watchdog timeout): drain before freeing
   if (stream_) cudaStreamSynchronize(stream_);
+  if (copy_stream_) cudaStreamSynchronize(copy_stream_);
   cudaGetLastError();
+  for (int b = 0; b < 2; ++b) {
+    if (astage_[b]) cudaFree(astage_[b]);
+    if (aready_[b]) cudaEventDestroy(aready_[b]);
+    if (adone_[b]) cudaEventDestroy(adone_[b]);
+    astage_[b] = nullptr;
+    aready_[b] = adone_[b] = nullptr;
+    apending_[b] = false;
+  }
+  if (copy_stream_) cudaStreamDestroy(copy_stream_);
+  copy_stream_ = nullptr;
   for (double* c : ckpt_) cudaFree(c);
   ckpt_.clear();
   if (tape_) cudaFree(tape_);
@@ -1180,13 +1207,15 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
   return SWC_OK;
 }
 
-template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag) {
-  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0);
+template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag, bool vsol) {
+  vsol = vsol || diag;
+  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0) | (vsol ? 8 : 0);
   auto it = graphs_.find(key);
   if (it == graphs_.end()) {
     cudaGraph_t graph = nullptr;
     SWC_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     launches_ = 0;
+    cap_vsol_ = vsol;
     int rc = enqueue_step(relax, first, diag);
     cudaError_t e = cudaStreamEndCapture(stream_, &graph);
     if (rc) {
@@ -1262,6 +1291,7 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   have_vsol_ = false;
   vsol_pending_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
+  diag_step_ = -1;
   return SWC_OK;
 }
 
@@ -1321,10 +1351,15 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   SWC_CK(cudaSetDevice(p_.device));
   SWC_CK(cudaEventRecord(ev0_, stream_));
   last_launches_ = 0;
+  int64_t diag_at = -1;  // the call's last diagnostic step
   for (int s = 0; s < nsteps; ++s) {
     const int64_t n = nloop_ + 1;  // nLoop after the increment at REF:1085
     const bool relax = !(n > p_.divv_switch || p_.load == 1);
-    SWC_TRY(run_graph(relax, n == 1, s == nsteps - 1));
+    const bool last = s == nsteps - 1;
+    // diagnostics: the call's last step, or every diag_interval steps (REF:2202: 50)
+    const bool diag = p_.diag_interval > 0 ? (n % p_.diag_interval == 0) : last;
+    SWC_TRY(run_graph(relax, n == 1, diag, last));
+    if (diag) diag_at = n;
     nloop_ = n;
     if (p_.adjoint_ckpt > 0 && n % p_.adjoint_ckpt == 0) SWC_TRY(save_ckpt((size_t)(n / p_.adjoint_ckpt)));
   }
@@ -1354,7 +1389,7 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   last_ms_ = ms;
   double sums[5];
   int tma_status = 0;
-  SWC_CK(cudaMemcpyAsync(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost, stream_));
+  if (diag_at >= 0) SWC_CK(cudaMemcpyAsync(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost, stream_));
   SWC_CK(cudaMemcpyAsync(&tma_status, status_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
   SWC_CK(cudaStreamSynchronize(stream_));
   if (tma_status) {
@@ -1363,6 +1398,10 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
     set_error("a tile copy of a transform pass did not complete in time (step %lld)", (long long)nloop_);
     return SWC_ERR_CUDA;
   }
+  have_vsol_ = true;
+  vsol_pending_ = true;
+  if (diag_at < 0) return SWC_OK;  // no diagnostic step in this call
+  diag_step_ = diag_at;
   // REF:2244-2258
   diag_.sum_abs_dpsi = sums[0];
   diag_.sum_abs_psi = sums[1];
@@ -1371,12 +1410,10 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   diag_.l1 = sums[0] / (p_.dt * sums[1]);
   diag_.mass = sums[2] * dx_ * dx_ * dx_;
   diag_.energy = sums[3] * dx_ * dx_ * dx_;
-  diag_.step = nloop_;
+  diag_.step = diag_at;
   diag_.nonfinite = (int64_t)sums[4];
-  have_vsol_ = true;
-  vsol_pending_ = true;
   if (diag_.nonfinite) {
-    set_error("non-finite psi/rho after step %lld (%lld values)", (long long)nloop_, (long long)diag_.nonfinite);
+    set_error("non-finite psi/rho after step %lld (%lld values)", (long long)diag_at, (long long)diag_.nonfinite);
     return SWC_ERR_NONFINITE;
   }
   return SWC_OK;
@@ -1401,7 +1438,14 @@ template <typename T> int StepEngine<T>::field_src(int field, const void** src, 
     case SWC_F_VSOLX: *src = vsolr_[0]; break;
     case SWC_F_VSOLY: *src = vsolr_[1]; break;
     case SWC_F_VSOLZ: *src = vsolr_[2]; break;
-    case SWC_F_ENERGY: *src = energy_; break;
+    case SWC_F_ENERGY:
+      if (diag_step_ != nloop_) {
+        set_error("the energy density is written at diagnostic steps only (last: step %lld, now %lld)",
+                  (long long)diag_step_, (long long)nloop_);
+        return SWC_ERR_STATE;
+      }
+      *src = energy_;
+      break;
     case SWC_F_PSIQ: *src = psiq_; *is_double = true; break;
     case SWC_F_PSIQ_OLD: *src = psiq_old_; *is_double = true; break;
     case SWC_F_NLQ: *src = nlq_; break;
@@ -1462,6 +1506,59 @@ template <typename T> int StepEngine<T>::get_field(int field, double* dst) {
     SWC_CK(cudaGetLastError());
     SWC_CK(cudaMemcpyAsync(dst, stage_, n * sizeof(double), cudaMemcpyDeviceToHost, stream_));
     SWC_CK(cudaStreamSynchronize(stream_));
+  }
+  return SWC_OK;
+}
+
+// Asynchronous read: the field is snapshotted in FP64 on stream_ (widened from FP32 in
+// the mixed engine), and the snapshot is copied to dst on copy_stream_, so the copy
+// overlaps the steps that follow. Two snapshot buffers alternate; a call first waits
+// for the copy issued two calls before it (the buffer it reuses), so when it returns
+// the destination of the call before last is complete. get_field_wait() completes all.
+template <typename T> int StepEngine<T>::get_field_async(int field, double* dst) {
+  const void* src;
+  bool is_d;
+  SWC_TRY(field_src(field, &src, &is_d));
+  SWC_CK(cudaSetDevice(p_.device));
+  const size_t n = (size_t)g_.ng;
+  const int b = anext_;
+  if (apending_[b]) {
+    apending_[b] = false;
+    SWC_CK(cudaEventSynchronize(adone_[b]));
+  }
+  if (!copy_stream_) SWC_CK(cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking));
+  if (!astage_[b]) {
+    if (cudaMalloc(&astage_[b], n * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      astage_[b] = nullptr;
+      set_error("cudaMalloc of the field snapshot failed (%zu MB)", (n * sizeof(double)) >> 20);
+      return SWC_ERR_OOM;
+    }
+    SWC_CK(cudaEventCreateWithFlags(&aready_[b], cudaEventDisableTiming));
+    SWC_CK(cudaEventCreateWithFlags(&adone_[b], cudaEventDisableTiming));
+  }
+  if (is_d || std::is_same<T, double>::value) {
+    SWC_CK(cudaMemcpyAsync(astage_[b], src, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
+  } else {
+    widen_kernel<<<(unsigned)((n / 4 + 255) / 256), 256, 0, stream_>>>(reinterpret_cast<const float*>(src),
+                                                                       astage_[b], (long long)n);
+    SWC_CK(cudaGetLastError());
+  }
+  SWC_CK(cudaEventRecord(aready_[b], stream_));
+  SWC_CK(cudaStreamWaitEvent(copy_stream_, aready_[b], 0));
+  SWC_CK(cudaMemcpyAsync(dst, astage_[b], n * sizeof(double), cudaMemcpyDeviceToHost, copy_stream_));
+  SWC_CK(cudaEventRecord(adone_[b], copy_stream_));
+  apending_[b] = true;
+  anext_ = b ^ 1;
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::get_field_wait() {
+  SWC_CK(cudaSetDevice(p_.device));
+  for (int b = 0; b < 2; ++b) {
+    if (!apending_[b]) continue;
+    apending_[b] = false;
+    SWC_CK(cudaEventSynchronize(adone_[b]));
   }
   return SWC_OK;
 }
@@ -1576,6 +1673,7 @@ template <typename T> int StepEngine<T>::load(const char* path) {
   have_vsol_ = false;
   vsol_pending_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
+  diag_step_ = -1;
   diag_.step = nloop_;
   return SWC_OK;
 }

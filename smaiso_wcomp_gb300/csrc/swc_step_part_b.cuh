@@ -44,7 +44,7 @@ template <typename T> int StepEngine<T>::enqueue_part_b(bool relax, bool first, 
     StokesArgs<T> a{S_[0], S_[1], S_[2], fgrad_, ener_, vsol_[0], vsol_[1], vsol_[2], virr_[0], virr_[1],
                     virr_[2], vq_[0], vq_[1], vq_[2], vs_[0], vs_[1], vs_[2], gq_[0], gq_[1], gq_[2], gs_[0],
                     gs_[1], gs_[2], (T)scale_, (T)(1.0 / p_.nu), (T)(1.0 / (p_.lambda + 2 * p_.nu)),
-                    p_.nx / p_.ref_ranks, v_[0], v_[1], v_[2], diag ? 1 : 0};
+                    p_.nx / p_.ref_ranks, v_[0], v_[1], v_[2], cap_vsol_ ? 1 : 0};
     stokes_kernel<T><<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
     ++launches_;

@@ -68,7 +68,7 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
                   (T)p_.rho_0, (T)kp_, (T)rho_off_};
     diag_kernel<T><<<diag_blocks_, kDiagThreads, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
-    diag_final_kernel<<<1, 32, 0, stream_>>>(partial_, diag_blocks_, dsum_);
+    diag_final_kernel<<<1, kDiagFinalThreads, 0, stream_>>>(partial_, diag_blocks_, dsum_);
     SWC_CK(cudaGetLastError());
     launches_ += 2;
   }

@@ -74,6 +74,16 @@ class Engine:
                f"swc_get_field({name})")
         return out
 
+    def field_async(self, name, out):
+        """swc_get_field_async: queue the read of `name` into `out` (pinned for overlap);
+        `out` is complete after field_wait() or after the next-but-one field_async."""
+        _check(self.lib, self.lib.swc_get_field_async(self._h, abi.FIELD_ID[name], abi.as_dptr(out)),
+               f"swc_get_field_async({name})")
+        return out
+
+    def field_wait(self):
+        _check(self.lib, self.lib.swc_get_field_wait(self._h), "swc_get_field_wait")
+
     def device_ptr(self, name):
         ptr = ctypes.c_void_p()
         eb = ctypes.c_int()

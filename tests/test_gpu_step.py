@@ -114,6 +114,41 @@ def test_checkpoint_continuation_is_bitwise(lib, tmp_path, prec):
             assert np.array_equal(e2.field(f), v), f
 
 
+def _pinned(shape):
+    import torch
+    return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+
+@pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
+def test_field_async_matches_sync_read(lib, prec):
+    """swc_get_field_async after every step returns that step's field: distinct host
+    buffers (pinned and pageable) and then two alternating pinned buffers, checked
+    after swc_get_field_wait."""
+    p = abi.default_params(32, 16, 16, rho_0=0.8, divv_switch=2, precision=prec)
+    psi, rho = ic.undulated_interface(p)
+    with Engine(p) as e:
+        e.set_state(psi, rho)
+        bufs = [_pinned(e.shape) if s % 2 == 0 else np.empty(e.shape) for s in range(6)]
+        refs = []
+        for s in range(6):
+            e.step(1)
+            e.field_async("psi" if s != 3 else "rho", bufs[s])
+            refs.append(e.field("psi" if s != 3 else "rho"))
+        e.field_wait()
+        for s in range(6):
+            assert np.array_equal(bufs[s], refs[s]), s
+        alt = [_pinned(e.shape), _pinned(e.shape)]
+        refs = []
+        for s in range(5):
+            e.step(1)
+            refs.append(e.field("psi"))
+            e.field_async("psi", alt[s & 1])
+        e.field_wait()
+        assert np.array_equal(alt[0], refs[4])
+        assert np.array_equal(alt[1], refs[3])
+        assert not np.array_equal(refs[3], refs[4])
+
+
 def test_nonfinite_detected(lib):
     p = abi.default_params(8)
     psi = np.zeros((8, 8, 8))
@@ -183,3 +218,33 @@ def test_dislocations_512x512x256_mixed_vs_fp64(lib):
     vn = np.sqrt(sum(np.linalg.norm(b[c]) ** 2 for c in ("vx", "vy", "vz")))
     dv = np.sqrt(sum(np.linalg.norm(a[c] - b[c]) ** 2 for c in ("vx", "vy", "vz")))
     assert dv <= 1e-3 * vn
+
+
+@pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
+def test_diag_interval_cadence(lib, prec):
+    """diag_interval = 3: diagnostics at nLoop % 3 == 0 only, equal to those of a run that
+    ends its swc_step call on the same step; every field of the current step is still
+    readable (v_sol included), the energy density only at diagnostic steps."""
+    p = abi.default_params(16, 16, 32, rho_0=0.8, divv_switch=2, precision=prec)
+    psi, rho = ic.undulated_interface(p)
+    q = abi.default_params(16, 16, 32, rho_0=0.8, divv_switch=2, precision=prec, diag_interval=3)
+    with Engine(p) as a, Engine(q) as b:
+        a.set_state(psi, rho)
+        b.set_state(psi, rho)
+        a.step(6)
+        for _ in range(6):
+            b.step(1)
+        da, db = a.diagnostics(), b.diagnostics()
+        assert db["step"] == 6 and da == db
+        assert np.array_equal(a.field("energy"), b.field("energy"))
+        a.step(1)
+        b.step(1)
+        assert b.diagnostics() == db  # step 7 ran no diagnostics
+        for f in ("psi", "rho", "vx", "vsolx", "vsolz", "divv", "psiq"):
+            assert np.array_equal(a.field(f), b.field(f)), f
+        with pytest.raises(SwcError) as ex:
+            b.field("energy")
+        assert ex.value.status == abi.SWC_ERR_STATE
+        a.step(2)
+        b.step(2)
+        assert b.diagnostics()["step"] == 9 and a.diagnostics() == b.diagnostics()

@@ -49,7 +49,8 @@ def test_derived_match_c(lib):
 def test_bad_params_rejected_before_device(lib):
     import ctypes
     h = ctypes.c_void_p()
-    for bad in (dict(nz=12), dict(ref_ranks=3), dict(dt=0.0), dict(nu=-1.0), dict(precision=7)):
+    for bad in (dict(nz=12), dict(ref_ranks=3), dict(dt=0.0), dict(nu=-1.0), dict(precision=7),
+                dict(diag_interval=-1), dict(adjoint_ckpt=-2)):
         p = abi.default_params(16)
         for k, v in bad.items():
             setattr(p, k, v)
