@@ -56,6 +56,10 @@ def parse():
                     default="undulated",
                     help="dislocations: the 512x512x256 layer-dislocation configuration, reported as "
                          "its own JSON line (mixed and FP64 steps/s, mixed-vs-FP64 errors)")
+    ap.add_argument("--adjoint-steps", type=int, default=None,
+                    help="adjoint workloads: steps instead of the configuration's (short profiling runs)")
+    ap.add_argument("--divv-switch", type=int, default=None,
+                    help="adjoint workloads: relax-phase length instead of the reference's 50")
     ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
                     help="profiling mode: run only this engine's warm-up + timed steps and print its timing")
     return ap.parse_args()
@@ -254,7 +258,7 @@ def gradient_forward_ratio(steps, ckpt=20, n=128):
 CAL_COEFFS = ("alpha", "beta", "gamma", "nu", "rho_0")
 
 
-def calibration_adjoint(which):
+def calibration_adjoint(which, steps=None, divv_switch=None):
     """The calibration-adjoint configurations: adjoint128 -- FP64 forward + FP64 adjoint,
     128^3, 400 steps, checkpoints every 20 steps; adjoint256 -- mixed forward + FP32
     adjoint, 256^3, 2000 steps, binomial checkpoint/recompute under a 40 GB device-memory
@@ -263,17 +267,21 @@ def calibration_adjoint(which):
     scaled by 1 + U(-0.1, 0.1) (seeded); loss L = ||psi(T) - psi_target||^2 (the
     interface free-energy term of the configuration is left out: lambda = 0). Reports the
     gradient/forward wall-time ratio, the gradient and, for adjoint128, its error against
-    central finite differences of the FP64 forward (h = 1e-6 relative)."""
+    central finite differences of the FP64 forward (h = 1e-6 relative). steps and
+    divv_switch override the configuration's step count and relax-phase length (short
+    profiling runs)."""
     from smaiso_wcomp_gb300 import abi, ic
     from smaiso_wcomp_gb300.engine import Engine
-    n, steps = (128, 400) if which == "adjoint128" else (256, 2000)
+    n, nsteps = (128, 400) if which == "adjoint128" else (256, 2000)
+    steps = steps or nsteps
+    dv = {} if divv_switch is None else {"divv_switch": divv_switch}
     prec = abi.SWC_PREC_MIXED if which == "adjoint256" else abi.SWC_PREC_FP64
     mode = dict(adjoint_ckpt=20) if which == "adjoint128" else dict(adjoint_ckpt=-1, adjoint_cap_gb=40.0)
     mode["precision"] = prec
-    base = abi.default_params(n, rho_0=0.8)
+    base = abi.default_params(n, rho_0=0.8, **dv)
     psi0, rho0 = ic.undulated_interface(base)
     u = ic.uniform01(1004, np.arange(len(CAL_COEFFS), dtype=np.uint64))
-    tgt = abi.default_params(n, rho_0=0.8, precision=prec)
+    tgt = abi.default_params(n, rho_0=0.8, precision=prec, **dv)
     for c, x in zip(CAL_COEFFS, u):
         setattr(tgt, c, getattr(tgt, c) * (1.0 + 0.2 * (x - 0.5)))
     with Engine(tgt) as e:
@@ -288,7 +296,7 @@ def calibration_adjoint(which):
             d = e.field("psi") - psi_t
             return float(np.sum(d * d))
 
-    p = abi.default_params(n, rho_0=0.8, **mode)
+    p = abi.default_params(n, rho_0=0.8, **mode, **dv)
     with Engine(p) as e:
         e.set_state(psi0, rho0)     # warm-up: graphs, adjoint buffers
         e.step(2)
@@ -300,7 +308,8 @@ def calibration_adjoint(which):
         t1 = time.perf_counter()
         g = e.backward(dpsi=2.0 * (psi_T - psi_t), want_psi0=True)
         t2 = time.perf_counter()
-    res = {"workload": f"calibration adjoint {n}^3, {steps} steps, "
+    res = {"workload": f"calibration adjoint {n}^3, {steps} steps"
+                       + ("" if divv_switch is None else f" (relax phase {divv_switch} steps)") + ", "
                        + ("mixed forward + FP32 adjoint, " if prec == abi.SWC_PREC_MIXED else
                           "FP64 forward + FP64 adjoint, ")
                        + ("checkpoints every 20 steps" if which == "adjoint128" else
@@ -314,7 +323,7 @@ def calibration_adjoint(which):
         # central differences with h = 1e-3 (relative): at h = 1e-6 the FP64 roundoff of
         # L over 400 steps (~1e-13 |L|) divided by 2h dominates for the small gradients
         def at(c, x):
-            q = abi.default_params(n, rho_0=0.8)
+            q = abi.default_params(n, rho_0=0.8, **dv)
             setattr(q, c, x)
             return forward(q)
         fd, fd4 = {}, {}
@@ -327,7 +336,7 @@ def calibration_adjoint(which):
         res["fd4_h1e-3"] = fd4
         res["rel_err_vs_fd4"] = {c: abs(g[c] - fd4[c]) / max(abs(fd4[c]), 1e-300) for c in CAL_COEFFS}
         d = ic.gaussian_noise((n, n, n), 77, 1.0)
-        with Engine(abi.default_params(n, rho_0=0.8)) as e:
+        with Engine(abi.default_params(n, rho_0=0.8, **dv)) as e:
             def fpsi(x):
                 e.set_state(psi0 + x * d, rho0)
                 e.step(steps)
@@ -454,7 +463,7 @@ def main():
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
     if args.workload in ("adjoint128", "adjoint256", "adjoint256_fp64"):
-        print(json.dumps(calibration_adjoint(args.workload)), flush=True)
+        print(json.dumps(calibration_adjoint(args.workload, args.adjoint_steps, args.divv_switch)), flush=True)
         return
     if args.workload == "dislocations":
         print(json.dumps(dislocation_run(args.steps, args.warmup, args.accuracy_steps or 50, local)), flush=True)
