@@ -357,6 +357,53 @@ template <int N> __device__ __forceinline__ void pair_pre(PC* buf, const float2*
   __syncthreads();
 }
 
+// K_DERIV between the two FFTs, in registers: the DCT-II post-processing of the slot
+// pair (k, M-k) yields Y_k, Y_{N-k}, Y_{M-k}, Y_{M+k}; the DST-III input is the shifted,
+// reversed X_r = w_{N-1-r} = mul(N-1-r) Y_{N-r} (X_0 = w_{N-1} = 0), and its
+// pre-processing of the same slot pair reads X_k, X_{N-k}, X_{M-k}, X_{M+k} -- exactly
+// those four Y times their multipliers. Each slot is read and written by one thread
+// only, so no barrier separates the two steps (one after, before the inverse FFT).
+template <int N, int AX, class MUL>
+__device__ __forceinline__ void pair_deriv(const Grid& g, int lineA, PC* buf, const float2* post,
+                                           const float2* pre, int lp, int tj, const MUL& mul) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, NP = (M / 2) / TPL;
+  auto m = [&](int pos) -> float2 {  // the multiplier at position pos of both lines
+    int i, j, k;
+    long long idx;
+    line_coords(g, AX, lineA, pos, i, j, k, idx);
+    return mul_ab<AX>(mul, i, j, k);
+  };
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const PC zk = buf[k * PP + lp];
+    const PC zm = buf[((M - k) & (M - 1)) * PP + lp];
+    const PC u0 = pcomb(post[2 * k], zk, post[2 * k + 1], zm);
+    const int km = M - k;
+    const PC u1 = pcomb(post[2 * km], zm, post[2 * km + 1], zk);
+    // Y_k = u0.re, Y_{N-k} = -u0.im, Y_{M-k} = u1.re, Y_{M+k} = -u1.im (k = 0: Y_M = u1.re)
+    const float2 xk = (k > 0) ? mul2(m(N - 1 - k), neg2(u0.im)) : f2(0.f);
+    const float2 xnk = (k > 0) ? mul2(m(k - 1), u0.re) : f2(0.f);
+    const float2 xmk = (k > 0) ? mul2(m(M - 1 + k), neg2(u1.im)) : mul2(m(M - 1), u1.re);
+    const float2 xmpk = mul2(m(M - 1 - k), u1.re);
+    PC z0, z1;
+    pair_pre_one(pre, M, k, xk, xnk, xmk, xmpk, z0, z1);
+    buf[k * PP + lp] = pswap(z0);
+    if (k > 0) buf[(M - k) * PP + lp] = pswap(z1);
+  }
+  if (tj == 0) {
+    const int k = M / 2;
+    const PC z = buf[k * PP + lp];
+    const PC u = pcomb(post[M], z, post[M + 1], z);
+    // Y_{M/2} = u.re, Y_{N-M/2} = -u.im: X_{M/2} = mul(N-1-M/2) Y_{N-M/2}, X_{N-M/2} = mul(M/2-1) Y_{M/2}
+    const float2 xk = mul2(m(N - 1 - k), neg2(u.im)), xnk = mul2(m(k - 1), u.re);
+    const PC U = pmake(xk, neg2(xnk));
+    buf[k * PP + lp] = pswap(pcomb(pre[2 * k], U, pre[2 * k + 1], U));
+  }
+  __syncthreads();
+}
+
 // x/y forward kinds: post-processing with the outputs of both lines stored straight
 // to global memory.
 template <int N, int KIND, int AX, class ST>
@@ -483,29 +530,13 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
       pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
       return;
     }
-    constexpr bool rows = !xy && !inv_out;  // z forward kinds: the z store reads position rows
-    pair_post<N, (KIND == K_DERIV ? K_C2 : KIND), AX, MulOp, rows>(g, lineA, buf, spost, lp, tj, mul);
     if constexpr (KIND == K_DERIV) {
-      // w_i = mul(i) u_{i+1} (w_{N-1} = 0), stored reversed as the DST-III input
-      constexpr int PER = N / TPL;
-      float2 w[PER];
-#pragma unroll
-      for (int b = 0; b < PER; ++b) {
-        const int i = tj + b * TPL;
-        w[b] = f2(0.f);
-        if (i < N - 1) {
-          int ii, jj, kk;
-          long long idx;
-          line_coords(g, AX, lineA, i, ii, jj, kk, idx);
-          w[b] = mul2(mul_ab<AX>(mul, ii, jj, kk), rb2[rpi<PP>(i + 1, lp)]);
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int b = 0; b < PER; ++b) rb2[rpi<PP>(N - 1 - (tj + b * TPL), lp)] = w[b];
-      __syncthreads();
+      pair_deriv<N, AX>(g, lineA, buf, spost, spre, lp, tj, mul);
+    } else {
+      constexpr bool rows = !xy && !inv_out;  // z forward kinds: the z store reads position rows
+      pair_post<N, KIND, AX, MulOp, rows>(g, lineA, buf, spost, lp, tj, mul);
+      if constexpr (inv_out) pair_pre<N>(buf, spre, lp, tj);
     }
-    if constexpr (inv_out) pair_pre<N>(buf, spre, lp, tj);
   }
 
   // ---------------- inverse FFT ----------------

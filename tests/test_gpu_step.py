@@ -86,6 +86,25 @@ def test_mixed_step_accuracy(lib, oracle_mod, shape, nsteps):
         assert abs(e.diagnostics()["mass"] - o.diagnostics()["mass"]) <= 1e-7 * abs(o.diagnostics()["mass"])
 
 
+@pytest.mark.parametrize("shape", [(64, 64, 64), (256, 32, 32), (32, 256, 32), (32, 32, 256)])
+def test_mixed_gradients_one_step(lib, oracle_mod, shape):
+    """The FP32 derivative passes (DCT-II, shifted multiply, DST-III in one pass; lines
+    of 64 and 256 points, each axis) against the FP64 oracle after one step."""
+    p = abi.default_params(*shape, rho_0=0.8, divv_switch=10)
+    psi, rho = ic.undulated_interface(p)
+    o = oracle_mod.Oracle(p)
+    o.set_state(psi, rho)
+    o.step(1)
+    pm = abi.default_params(*shape, rho_0=0.8, divv_switch=10, precision=abi.SWC_PREC_MIXED)
+    with Engine(pm) as e:
+        e.set_state(psi, rho)
+        e.step(1)
+        for vec in (("gpsix", "gpsiy", "gpsiz"), ("grhox", "grhoy", "grhoz")):
+            scale = np.sqrt(sum(np.linalg.norm(o.field(c)) ** 2 for c in vec))
+            for c in vec:
+                assert np.linalg.norm(e.field(c) - o.field(c)) <= 1e-5 * scale, c
+
+
 def test_zero_state_fixed_point(lib):
     p = abi.default_params(16, rho_0=0.3, divv_switch=2)
     with Engine(p) as e:
