@@ -404,6 +404,48 @@ __device__ __forceinline__ void pair_deriv(const Grid& g, int lineA, PC* buf, co
   __syncthreads();
 }
 
+// K_FILT between the two FFTs, in registers: X_p = Y_p mul(p) at the four positions
+// k, N-k, M-k, M+k that the DCT-II post-processing of the slot pair (k, M-k) yields and
+// the DCT-III pre-processing of the same pair reads (one barrier, as pair_deriv).
+template <int N, int AX, class MUL>
+__device__ __forceinline__ void pair_filt(const Grid& g, int lineA, PC* buf, const float2* post,
+                                          const float2* pre, int lp, int tj, const MUL& mul) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, NP = (M / 2) / TPL;
+  auto m = [&](int pos) -> float2 {
+    int i, j, k;
+    long long idx;
+    line_coords(g, AX, lineA, pos, i, j, k, idx);
+    return mul_ab<AX>(mul, i, j, k);
+  };
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const PC zk = buf[k * PP + lp];
+    const PC zm = buf[((M - k) & (M - 1)) * PP + lp];
+    const PC u0 = pcomb(post[2 * k], zk, post[2 * k + 1], zm);
+    const int km = M - k;
+    const PC u1 = pcomb(post[2 * km], zm, post[2 * km + 1], zk);
+    const float2 xk = mul2(u0.re, m(k));
+    const float2 xnk = (k > 0) ? mul2(neg2(u0.im), m(N - k)) : f2(0.f);
+    const float2 xmk = mul2(u1.re, m(M - k));
+    const float2 xmpk = (k > 0) ? mul2(neg2(u1.im), m(M + k)) : xmk;
+    PC z0, z1;
+    pair_pre_one(pre, M, k, xk, xnk, xmk, xmpk, z0, z1);
+    buf[k * PP + lp] = pswap(z0);
+    if (k > 0) buf[(M - k) * PP + lp] = pswap(z1);
+  }
+  if (tj == 0) {
+    const int k = M / 2;
+    const PC z = buf[k * PP + lp];
+    const PC u = pcomb(post[M], z, post[M + 1], z);
+    const float2 xk = mul2(u.re, m(k)), xnk = mul2(neg2(u.im), m(N - k));
+    const PC U = pmake(xk, neg2(xnk));
+    buf[k * PP + lp] = pswap(pcomb(pre[2 * k], U, pre[2 * k + 1], U));
+  }
+  __syncthreads();
+}
+
 // x/y forward kinds: post-processing with the outputs of both lines stored straight
 // to global memory.
 template <int N, int KIND, int AX, class ST>
@@ -532,6 +574,8 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
     }
     if constexpr (KIND == K_DERIV) {
       pair_deriv<N, AX>(g, lineA, buf, spost, spre, lp, tj, mul);
+    } else if constexpr (KIND == K_FILT) {
+      pair_filt<N, AX>(g, lineA, buf, spost, spre, lp, tj, mul);
     } else {
       constexpr bool rows = !xy && !inv_out;  // z forward kinds: the z store reads position rows
       pair_post<N, KIND, AX, MulOp, rows>(g, lineA, buf, spost, lp, tj, mul);

@@ -89,7 +89,8 @@ def test_mixed_step_accuracy(lib, oracle_mod, shape, nsteps):
 @pytest.mark.parametrize("shape", [(64, 64, 64), (256, 32, 32), (32, 256, 32), (32, 32, 256)])
 def test_mixed_gradients_one_step(lib, oracle_mod, shape):
     """The FP32 derivative passes (DCT-II, shifted multiply, DST-III in one pass; lines
-    of 64 and 256 points, each axis) against the FP64 oracle after one step."""
+    of 64 and 256 points, each axis) and the filter pass of the amplitude (DCT-II,
+    Gaussian, DCT-III along x) against the FP64 oracle after one step."""
     p = abi.default_params(*shape, rho_0=0.8, divv_switch=10)
     psi, rho = ic.undulated_interface(p)
     o = oracle_mod.Oracle(p)
@@ -103,6 +104,7 @@ def test_mixed_gradients_one_step(lib, oracle_mod, shape):
             scale = np.sqrt(sum(np.linalg.norm(o.field(c)) ** 2 for c in vec))
             for c in vec:
                 assert np.linalg.norm(e.field(c) - o.field(c)) <= 1e-5 * scale, c
+        assert rel(e.field("amp"), o.field("amp")) <= 1e-5
 
 
 def test_zero_state_fixed_point(lib):
