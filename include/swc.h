@@ -204,7 +204,25 @@ int swc_set_state(swc_ctx* ctx, const double* psi, const double* rho);
  * NaN/Inf afterwards. */
 int swc_step(swc_ctx* ctx, int nsteps);
 
-/* Read the diagnostics of the last swc_step call. */
+/* Capture now the CUDA graphs of every step variant (relax / normal phase, first
+ * step, diagnostic step, v_sol written or not), which swc_step otherwise captures on
+ * first use, so that no later swc_step call pays for a capture (a loop timed or run
+ * under a latency budget). Runs no step. Needs swc_set_state first. */
+int swc_prepare(swc_ctx* ctx);
+
+/* swc_step without the wait: the nsteps graph launches are enqueued on the context's
+ * stream and the call returns, so the host can enqueue the next step (or a field
+ * read, swc_get_field_async) while the device runs. The steps' status -- a transform
+ * pass whose tile wait ran out, the diagnostics of the last diagnostic step enqueued
+ * (swc_params.diag_interval) and its non-finite check -- is collected by the next
+ * swc_sync or swc_step call. swc_get_field waits for the steps before reading. */
+int swc_step_async(swc_ctx* ctx, int nsteps);
+
+/* Wait for every step enqueued by swc_step_async and return their status
+ * (SWC_ERR_NONFINITE, SWC_ERR_CUDA, ...); the diagnostics become readable. */
+int swc_sync(swc_ctx* ctx);
+
+/* Read the diagnostics of the last diagnostic step that swc_step or swc_sync collected. */
 int swc_diagnostics(swc_ctx* ctx, swc_diag* out);
 
 /* Copy one field (SWC_F_*) to host memory as nx*ny*nz doubles. Pinned (page-locked)

@@ -37,7 +37,8 @@ FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 # Every symbol include/swc.h declares (checked by the CPU test suite).
 EXPORTS = [
     "swc_abi_version", "swc_strerror", "swc_last_error", "swc_default_params", "swc_derive",
-    "swc_create", "swc_destroy", "swc_set_state", "swc_step", "swc_diagnostics",
+    "swc_create", "swc_destroy", "swc_set_state", "swc_step", "swc_step_async", "swc_sync",
+    "swc_prepare", "swc_diagnostics",
     "swc_get_field", "swc_get_field_async", "swc_get_field_wait", "swc_field_device_ptr", "swc_get_step",
     "swc_last_step_ms",
     "swc_last_step_launches", "swc_device_fma_peak", "swc_diagnostics_noalloc",
@@ -142,6 +143,9 @@ def load_library(path=None):
         "swc_step": (ctypes.c_int, [vp, ctypes.c_int]),
         "swc_diagnostics": (ctypes.c_int, [vp, P(SwcDiag)]),
         "swc_get_field": (ctypes.c_int, [vp, ctypes.c_int, dp]),
+        "swc_step_async": (ctypes.c_int, [vp, ctypes.c_int]),
+        "swc_sync": (ctypes.c_int, [vp]),
+        "swc_prepare": (ctypes.c_int, [vp]),
         "swc_get_field_async": (ctypes.c_int, [vp, ctypes.c_int, dp]),
         "swc_get_field_wait": (ctypes.c_int, [vp]),
         "swc_field_device_ptr": (ctypes.c_int, [vp, ctypes.c_int, P(vp), P(ctypes.c_int)]),

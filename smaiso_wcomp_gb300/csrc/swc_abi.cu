@@ -247,6 +247,21 @@ int swc_step(swc_ctx* ctx, int nsteps) {
   SWC_GUARD(ctx->eng->step(nsteps));
 }
 
+int swc_prepare(swc_ctx* ctx) {
+  SWC_NEED_CTX(ctx);
+  SWC_GUARD(ctx->eng->prepare());
+}
+
+int swc_step_async(swc_ctx* ctx, int nsteps) {
+  SWC_NEED_CTX(ctx);
+  SWC_GUARD(ctx->eng->step_async(nsteps));
+}
+
+int swc_sync(swc_ctx* ctx) {
+  SWC_NEED_CTX(ctx);
+  SWC_GUARD(ctx->eng->sync());
+}
+
 int swc_diagnostics(swc_ctx* ctx, swc_diag* out) {
   SWC_NEED_CTX(ctx);
   if (!out) { set_error("out is NULL"); return SWC_ERR_BAD_PARAM; }

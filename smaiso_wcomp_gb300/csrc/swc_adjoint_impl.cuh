@@ -453,7 +453,8 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
   double pg[PG_COUNT];
   SWC_CK(cudaMemcpyAsync(pg, pgrad_, sizeof(pg), cudaMemcpyDeviceToHost, stream_));
   SWC_TRY(restore_ckpt(last_slot));
-  diag_step_ = -1;  // the recompute overwrote the energy density
+  diag_step_ = -1;  // the recompute overwrote the energy density and the sums
+  pending_diag_ = -1;
   SWC_CK(cudaStreamSynchronize(stream_));
   // chain rule through Amp(beta, gamma) and kp = (1 - rho_0)/Amp (REF:250-253); rho_s = 1, rho_m = 1/2
   const double disc = std::sqrt(9 * p_.beta * p_.beta + 40 * p_.ep * p_.gamma);

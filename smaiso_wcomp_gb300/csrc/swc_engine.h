@@ -17,6 +17,9 @@ class EngineBase {
   virtual ~EngineBase() {}
   virtual int set_state(const double* psi, const double* rho) = 0;
   virtual int step(int nsteps) = 0;
+  virtual int step_async(int nsteps) = 0;
+  virtual int prepare() = 0;
+  virtual int sync() = 0;
   virtual int diagnostics(swc_diag* out) = 0;
   virtual int get_field(int field, double* dst) = 0;
   virtual int get_field_async(int field, double* dst) = 0;

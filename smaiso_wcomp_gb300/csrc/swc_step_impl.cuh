@@ -846,6 +846,9 @@ template <typename T> class StepEngine : public EngineBase {
   int init();
   int set_state(const double* psi, const double* rho) override;
   int step(int nsteps) override;
+  int step_async(int nsteps) override;
+  int prepare() override;
+  int sync() override;
   int diagnostics(swc_diag* out) override {
     *out = diag_;
     return SWC_OK;
@@ -927,8 +930,13 @@ template <typename T> class StepEngine : public EngineBase {
   // diag: the diagnostic variant (S15 reductions, psi_old <- psi rotation, energy field);
   // vsol: the Stokes kernel also writes v_sol (the last step of a swc_step call)
   int run_graph(bool relax, bool first, bool diag, bool vsol);
+  int graph_of(bool relax, bool first, bool diag, bool vsol, cudaGraphExec_t* out, int* key);
   bool cap_vsol_ = false;  // vsol flag of the variant being captured
   int64_t diag_step_ = -1;  // nLoop of the last step that ran the diagnostics
+  int64_t pending_diag_ = -1;  // diagnostic step enqueued, its sums not yet read
+  int check_step(int nsteps);
+  int enqueue_steps(int nsteps);
+  int finish_steps();
   void release();
   int field_src(int field, const void** src, bool* is_double);
 
@@ -1207,7 +1215,9 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
   return SWC_OK;
 }
 
-template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag, bool vsol) {
+// The instantiated graph of one step variant, captured on first use.
+template <typename T>
+int StepEngine<T>::graph_of(bool relax, bool first, bool diag, bool vsol, cudaGraphExec_t* out, int* key_out) {
   vsol = vsol || diag;
   const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0) | (vsol ? 8 : 0);
   auto it = graphs_.find(key);
@@ -1236,8 +1246,33 @@ template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool 
     it = graphs_.emplace(key, exec).first;
     graph_kernels_[key] = launches_;
   }
-  SWC_CK(cudaGraphLaunch(it->second, stream_));
+  *out = it->second;
+  *key_out = key;
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag, bool vsol) {
+  cudaGraphExec_t exec;
+  int key;
+  SWC_TRY(graph_of(relax, first, diag, vsol, &exec, &key));
+  SWC_CK(cudaGraphLaunch(exec, stream_));
   last_launches_ += graph_kernels_[key];
+  return SWC_OK;
+}
+
+// swc_prepare: capture every variant swc_step can launch (relax or normal phase, the
+// first step, diagnostic step, v_sol written or not) without running any.
+template <typename T> int StepEngine<T>::prepare() {
+  if (!have_state_) {
+    set_error("swc_prepare before swc_set_state");
+    return SWC_ERR_STATE;
+  }
+  SWC_CK(cudaSetDevice(p_.device));
+  cudaGraphExec_t exec;
+  int key;
+  for (int relax = 0; relax < 2; ++relax)
+    for (int first = 0; first < 2; ++first)
+      for (int v = 0; v < 3; ++v) SWC_TRY(graph_of(relax, first, v == 2, v >= 1, &exec, &key));
   return SWC_OK;
 }
 
@@ -1292,6 +1327,7 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
   vsol_pending_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
   diag_step_ = -1;
+  pending_diag_ = -1;
   return SWC_OK;
 }
 
@@ -1338,7 +1374,7 @@ template <typename T> int StepEngine<T>::restore_ckpt(size_t slot) {
   return refresh_copies(2);  // the mixed engine's FP32 copies of rho and psiq (f_rho restored above)
 }
 
-template <typename T> int StepEngine<T>::step(int nsteps) {
+template <typename T> int StepEngine<T>::check_step(int nsteps) {
   if (nsteps < 0) {
     set_error("nsteps must be >= 0");
     return SWC_ERR_BAD_PARAM;
@@ -1347,11 +1383,14 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
     set_error("swc_step before swc_set_state");
     return SWC_ERR_STATE;
   }
-  if (nsteps == 0) return SWC_OK;
+  return SWC_OK;
+}
+
+// Enqueue nsteps graph launches on stream_ (host bookkeeping at enqueue time: the
+// stream orders every later read of the fields after them).
+template <typename T> int StepEngine<T>::enqueue_steps(int nsteps) {
   SWC_CK(cudaSetDevice(p_.device));
-  SWC_CK(cudaEventRecord(ev0_, stream_));
   last_launches_ = 0;
-  int64_t diag_at = -1;  // the call's last diagnostic step
   for (int s = 0; s < nsteps; ++s) {
     const int64_t n = nloop_ + 1;  // nLoop after the increment at REF:1085
     const bool relax = !(n > p_.divv_switch || p_.load == 1);
@@ -1359,10 +1398,55 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
     // diagnostics: the call's last step, or every diag_interval steps (REF:2202: 50)
     const bool diag = p_.diag_interval > 0 ? (n % p_.diag_interval == 0) : last;
     SWC_TRY(run_graph(relax, n == 1, diag, last));
-    if (diag) diag_at = n;
+    if (diag) pending_diag_ = diag_step_ = n;
     nloop_ = n;
     if (p_.adjoint_ckpt > 0 && n % p_.adjoint_ckpt == 0) SWC_TRY(save_ckpt((size_t)(n / p_.adjoint_ckpt)));
   }
+  have_vsol_ = true;
+  vsol_pending_ = true;
+  return SWC_OK;
+}
+
+// With the stream idle: the transform passes' wait status and the sums of the last
+// diagnostic step enqueued since the previous check.
+template <typename T> int StepEngine<T>::finish_steps() {
+  double sums[5];
+  int tma_status = 0;
+  const int64_t diag_at = pending_diag_;
+  if (diag_at >= 0) SWC_CK(cudaMemcpyAsync(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost, stream_));
+  SWC_CK(cudaMemcpyAsync(&tma_status, status_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  SWC_CK(cudaStreamSynchronize(stream_));
+  pending_diag_ = -1;
+  if (tma_status) {
+    SWC_CK(cudaMemsetAsync(status_, 0, sizeof(int), stream_));
+    SWC_CK(cudaStreamSynchronize(stream_));
+    set_error("a tile copy of a transform pass did not complete in time (step %lld)", (long long)nloop_);
+    return SWC_ERR_CUDA;
+  }
+  if (diag_at < 0) return SWC_OK;  // no diagnostic step since the last check
+  // REF:2244-2258
+  diag_.sum_abs_dpsi = sums[0];
+  diag_.sum_abs_psi = sums[1];
+  diag_.sum_rho = sums[2];
+  diag_.sum_energy = sums[3];
+  diag_.l1 = sums[0] / (p_.dt * sums[1]);
+  diag_.mass = sums[2] * dx_ * dx_ * dx_;
+  diag_.energy = sums[3] * dx_ * dx_ * dx_;
+  diag_.step = diag_at;
+  diag_.nonfinite = (int64_t)sums[4];
+  if (diag_.nonfinite) {
+    set_error("non-finite psi/rho after step %lld (%lld values)", (long long)diag_at, (long long)diag_.nonfinite);
+    return SWC_ERR_NONFINITE;
+  }
+  return SWC_OK;
+}
+
+template <typename T> int StepEngine<T>::step(int nsteps) {
+  SWC_TRY(check_step(nsteps));
+  if (nsteps == 0) return SWC_OK;
+  SWC_CK(cudaSetDevice(p_.device));
+  SWC_CK(cudaEventRecord(ev0_, stream_));
+  SWC_TRY(enqueue_steps(nsteps));
   SWC_CK(cudaEventRecord(ev1_, stream_));
   // host watchdog: poll the stream's last event, never spin on the device
   if (p_.watchdog_s > 0) {
@@ -1387,36 +1471,20 @@ template <typename T> int StepEngine<T>::step(int nsteps) {
   float ms = 0;
   SWC_CK(cudaEventElapsedTime(&ms, ev0_, ev1_));
   last_ms_ = ms;
-  double sums[5];
-  int tma_status = 0;
-  if (diag_at >= 0) SWC_CK(cudaMemcpyAsync(sums, dsum_, sizeof(sums), cudaMemcpyDeviceToHost, stream_));
-  SWC_CK(cudaMemcpyAsync(&tma_status, status_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
-  SWC_CK(cudaStreamSynchronize(stream_));
-  if (tma_status) {
-    SWC_CK(cudaMemsetAsync(status_, 0, sizeof(int), stream_));
-    SWC_CK(cudaStreamSynchronize(stream_));
-    set_error("a tile copy of a transform pass did not complete in time (step %lld)", (long long)nloop_);
-    return SWC_ERR_CUDA;
-  }
-  have_vsol_ = true;
-  vsol_pending_ = true;
-  if (diag_at < 0) return SWC_OK;  // no diagnostic step in this call
-  diag_step_ = diag_at;
-  // REF:2244-2258
-  diag_.sum_abs_dpsi = sums[0];
-  diag_.sum_abs_psi = sums[1];
-  diag_.sum_rho = sums[2];
-  diag_.sum_energy = sums[3];
-  diag_.l1 = sums[0] / (p_.dt * sums[1]);
-  diag_.mass = sums[2] * dx_ * dx_ * dx_;
-  diag_.energy = sums[3] * dx_ * dx_ * dx_;
-  diag_.step = diag_at;
-  diag_.nonfinite = (int64_t)sums[4];
-  if (diag_.nonfinite) {
-    set_error("non-finite psi/rho after step %lld (%lld values)", (long long)diag_at, (long long)diag_.nonfinite);
-    return SWC_ERR_NONFINITE;
-  }
-  return SWC_OK;
+  return finish_steps();
+}
+
+// swc_step_async: the steps are enqueued and the call returns; swc_sync (or the next
+// swc_step) waits for them and reports their status and diagnostics.
+template <typename T> int StepEngine<T>::step_async(int nsteps) {
+  SWC_TRY(check_step(nsteps));
+  if (nsteps == 0) return SWC_OK;
+  return enqueue_steps(nsteps);
+}
+
+template <typename T> int StepEngine<T>::sync() {
+  SWC_CK(cudaSetDevice(p_.device));
+  return finish_steps();
 }
 
 template <typename T> int StepEngine<T>::field_src(int field, const void** src, bool* is_double) {
@@ -1674,6 +1742,7 @@ template <typename T> int StepEngine<T>::load(const char* path) {
   vsol_pending_ = false;
   std::memset(&diag_, 0, sizeof(diag_));
   diag_step_ = -1;
+  pending_diag_ = -1;
   diag_.step = nloop_;
   return SWC_OK;
 }

@@ -62,6 +62,17 @@ class Engine:
             _check(self.lib, rc, "swc_step")
         return rc
 
+    def step_async(self, n=1):
+        """swc_step_async: enqueue n steps and return; sync() collects their status."""
+        _check(self.lib, self.lib.swc_step_async(self._h, int(n)), "swc_step_async")
+
+    def prepare(self):
+        """swc_prepare: capture every step variant's CUDA graph now."""
+        _check(self.lib, self.lib.swc_prepare(self._h), "swc_prepare")
+
+    def sync(self):
+        _check(self.lib, self.lib.swc_sync(self._h), "swc_sync")
+
     def diagnostics(self):
         d = abi.SwcDiag()
         _check(self.lib, self.lib.swc_diagnostics(self._h, ctypes.byref(d)), "swc_diagnostics")

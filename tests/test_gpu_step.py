@@ -170,6 +170,33 @@ def test_field_async_matches_sync_read(lib, prec):
         assert not np.array_equal(refs[3], refs[4])
 
 
+@pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
+def test_step_async_matches_step(lib, prec):
+    """swc_step_async + swc_sync give the fields and diagnostics of swc_step; a field
+    read after swc_step_async waits for the steps; swc_sync reports a non-finite state."""
+    p = abi.default_params(16, 32, 16, rho_0=0.8, divv_switch=3, precision=prec, diag_interval=4)
+    psi, rho = ic.undulated_interface(p)
+    with Engine(p) as a, Engine(p) as b:
+        a.set_state(psi, rho)
+        b.set_state(psi, rho)
+        b.prepare()
+        for _ in range(9):
+            a.step(1)
+            b.step_async(1)
+        assert np.array_equal(b.field("psi"), a.field("psi"))
+        b.sync()
+        assert b.diagnostics() == a.diagnostics() and b.diagnostics()["step"] == 8
+        for f in ("psi", "rho", "vx", "vsoly", "psiq"):
+            assert np.array_equal(a.field(f), b.field(f)), f
+        bad = psi.copy()
+        bad[3, 4, 5] = np.nan
+        b.set_state(bad, rho)
+        b.step_async(4)
+        with pytest.raises(SwcError) as ex:
+            b.sync()
+        assert ex.value.status == abi.SWC_ERR_NONFINITE
+
+
 def test_nonfinite_detected(lib):
     p = abi.default_params(8)
     psi = np.zeros((8, 8, 8))
