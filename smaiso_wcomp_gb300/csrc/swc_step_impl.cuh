@@ -412,6 +412,14 @@ struct LdNlUpdate {
 // Pointwise kernels
 // ---------------------------------------------------------------------------------
 
+// The mixed engine's CN/AB2 update (REF:2177-2190), four points per thread: psiq_old <-
+// psiq, psiq <- psiq + FP32 increment, Nl_old <- Nl, and the FP32 copy psiqf of the new
+// psiq that the inverse transform then reads.
+static __global__ void __launch_bounds__(256) nl_update_kernel(long long n, LdNlUpdate lu) {
+  const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (idx < n) (void)lu.quad(0, 0, 0, idx);
+}
+
 __device__ __forceinline__ void decompose(const Grid& g, long long idx, int& i, int& j, int& k) {
   k = (int)(idx & (g.nz - 1));
   j = (int)((idx >> g.lz) & (g.ny - 1));

@@ -56,8 +56,13 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
     SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
     SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
     SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
+    // the CN update as a full-occupancy pointwise kernel (it writes the FP32 copy psiqf of
+    // the new psiq), then a plain TMA-fed pass from that copy
     LdNlUpdate lu{nlw_, dq_, nlq_, psiq_, psiq_old_, inv_c2f_, psiqf_, (float)(p_.dt / 2 * scale_), first ? 1 : 0};
-    SWC_TRY((pass<K_C3, 2>(lu, SP{pout})));
+    nl_update_kernel<<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_.ng, lu);
+    SWC_CK(cudaGetLastError());
+    ++launches_;
+    SWC_TRY((pass<K_C3, 2>(LP{psiqf_}, SP{pout})));
   }
   SWC_TRY((pass<K_C3, 1>(LP{pout}, SP{pout})));
   SWC_TRY((pass<K_C3, 0>(LP{pout}, SP{pout})));
