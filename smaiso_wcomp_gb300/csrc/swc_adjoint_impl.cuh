@@ -23,6 +23,7 @@ enum {
   TP_RHOIN, TP_RHONEW, TP_VX, TP_VY, TP_VZ, TP_DIVV, TP_VSX, TP_VSY, TP_VSZ, TP_VIX, TP_VIY, TP_VIZ, kTape
 };
 static_assert(PG_COUNT == 8, "pgrad_doubles() assumes 8 parameter slots");
+static_assert(kTape <= 32, "tape_alias_ holds one pointer per tape field");
 
 // adjoint work arrays
 enum {
@@ -59,7 +60,7 @@ template <typename T>
 int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
   const size_t ng = (size_t)g_.ng;
   const T* tp = tape_ + slot * (size_t)kTape * ng;
-  auto TP = [&](int q) { return tp + (size_t)q * ng; };
+  auto TP = [&](int q) { return (tape_alias_on_ && tape_alias_[q]) ? tape_alias_[q] : tp + (size_t)q * ng; };
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
   const unsigned blocks = pt4_blocks(g_);
   const AdjScalars<T> sc{(T)p_.ep, (T)p_.alpha, (T)p_.beta, (T)p_.gamma, (T)p_.zeta, (T)kp_, (T)p_.rho_0,
@@ -274,14 +275,20 @@ template <typename T> int StepEngine<T>::field_to_host(const T* src, double* dst
 
 // Step n (1-based) from the loaded state n-1 with its tape (slot 0), then its adjoint.
 template <typename T> int StepEngine<T>::tape_and_adjoint(int64_t n) {
-  SWC_TRY(record_tape(tape_, n));
+  SWC_TRY(record_tape(tape_, n, true));
   const bool relax = !(n > p_.divv_switch || p_.load == 1);
-  return adjoint_step(0, relax, n == 1);
+  tape_alias_on_ = true;
+  const int rc = adjoint_step(0, relax, n == 1);
+  tape_alias_on_ = false;
+  return rc;
 }
 
 // Run step n (1-based) from the loaded state n-1 and copy the fields its adjoint reads
 // into the tape slot tp; the mixed engine's FP64 state fields are narrowed to FP32.
-template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n) {
+// alias: the adjoint of step n runs next, so the fields that hold their taped values
+// until then (every one but the incoming density, and the narrowed FP64 state) are
+// left where the step wrote them and read in place (tape_alias_).
+template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n, bool alias) {
   const size_t ng = (size_t)g_.ng;
   constexpr bool mixed = !std::is_same<T, double>::value;
   auto put = [&](int q, const void* src, bool is_double) -> int {
@@ -300,8 +307,13 @@ template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n) {
   const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
                             amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
                             vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
-  for (int q = 0; q < kTape; ++q)
-    if (src[q]) SWC_TRY(put(q, src[q], q == TP_QOLD || q == TP_QNEW || q == TP_RHONEW));
+  for (int q = 0; q < kTape; ++q) {
+    tape_alias_[q] = nullptr;
+    if (!src[q]) continue;
+    const bool is_double = q == TP_QOLD || q == TP_QNEW || q == TP_RHONEW;
+    if (alias && !(mixed && is_double)) tape_alias_[q] = static_cast<const T*>(src[q]);
+    else SWC_TRY(put(q, src[q], is_double));
+  }
   ++fwd_steps_;
   return SWC_OK;
 }

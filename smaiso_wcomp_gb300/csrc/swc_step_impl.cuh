@@ -891,7 +891,7 @@ template <typename T> class StepEngine : public EngineBase {
   // FP64 engine: the FP64 adjoint (swc_adjoint_impl.cuh, in swc_step_fp64.cu); mixed
   // engine: the same adjoint in FP32 on the mixed trajectory (swc_step_mixed_adj.cu)
   int backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
-  int record_tape(T* tp, int64_t n);
+  int record_tape(T* tp, int64_t n, bool alias = false);
   int host_to_field(const double* src, T* dst);
   int field_to_host(const T* src, double* dst);
   int stage_alloc();
@@ -904,6 +904,10 @@ template <typename T> class StepEngine : public EngineBase {
   size_t engine_bytes_ = 0;        // device bytes of the engine's own arrays
   std::vector<double*> ckpt_;      // state at steps 0, K, 2K, ... (6 arrays each)
   T* tape_ = nullptr;              // forward intermediates of one segment
+  // binomial schedule: the tape step's fields read in place (the adjoint step that
+  // consumes them runs next on the same stream) instead of copied into tape_
+  const T* tape_alias_[32] = {};
+  bool tape_alias_on_ = false;
   size_t tape_steps_ = 0;
   T* adj_ = nullptr;               // adjoint work arrays
   double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
