@@ -301,7 +301,8 @@ int swc_diagnostics_noalloc(const swc_params* p, const double* psi, const double
  * the arrays passed to swc_set_state (host, nx*ny*nz doubles, either may be NULL)
  * and the coefficient gradients in *grad. The FP64 engine differentiates in FP64, the
  * mixed engine in FP32 (on its own trajectory); the context's state is the state at
- * step T again when the call returns. */
+ * step T again when the call returns. Steps enqueued by swc_step_async are waited for
+ * and their status returned first (as swc_sync). */
 int swc_backward(swc_ctx* ctx, const double* dL_dpsi, const double* dL_drho, double* dL_dpsi0,
                  double* dL_drho0, swc_grad* grad);
 

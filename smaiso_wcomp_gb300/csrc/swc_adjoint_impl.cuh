@@ -382,6 +382,7 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
     return SWC_ERR_STATE;
   }
   SWC_CK(cudaSetDevice(p_.device));
+  SWC_TRY(finish_steps());  // steps enqueued by swc_step_async: their status first
   if (vsol_pending_) {  // the recompute below reuses the spectral v_sol buffers
     SWC_TRY(transform_vsol());
     vsol_pending_ = false;
