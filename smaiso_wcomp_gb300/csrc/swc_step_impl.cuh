@@ -348,10 +348,10 @@ template <typename T> struct StNlUpdate {
   }
 };
 
-// Mixed engine: the CN/AB2 update of psiq (REF:2170-2190) in increment form, fused into
-// the loader of the first pass of psi = DCT-III^3 psiq_new (REF:2194-2197). It reads the
-// Nl transform's output nl_hat, writes psiq_old, psiq, nlq and the FP32 copy psiqf, and
-// returns psiqf. The increment (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
+// Mixed engine: the CN/AB2 update of psiq (REF:2170-2190) in increment form, applied by
+// nl_update_kernel before the first pass of psi = DCT-III^3 psiq_new (REF:2194-2197),
+// which reads the FP32 copy psiqf. It reads the Nl transform's output nl_hat, writes
+// psiq_old, psiq, nlq and psiqf. The increment (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
 // a small correction built from FP32 data, is formed in FP32 with an FP32 1/C2 table;
 // FP64 holds the state: two FP64 adds per point (psiq - psiq_old, psiq + increment),
 // conversions on the integer pipes.
@@ -367,18 +367,6 @@ struct LdNlUpdate {
     const float inc = (0.5f * narrow_f64(pq - pqo) + srcs * (3.0f * nl - nlo)) * ic;
     pn = pq + widen_f32(inc);
     return narrow_f64(pn);
-  }
-  __device__ __forceinline__ float operator()(int, int, int, long long idx) const {
-    const float nl = nlw[idx] - dq[idx];
-    const float nlo = first ? nl : nlq[idx];
-    const double pq = psiq[idx];
-    double pn;
-    const float pf = point(nl, nlo, pq, psiq_old[idx], inv_c2[idx], pn);
-    psiq_old[idx] = pq;
-    psiq[idx] = pn;
-    nlq[idx] = nl;
-    psiqf[idx] = pf;
-    return pf;
   }
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {

@@ -49,7 +49,7 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
     SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
     SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
   } else {
-    // mixed engine: FP64-lean density update, the CN update fused into the psi transform
+    // mixed engine: FP64-lean density update fused into the Nl transform, then the CN update
     LdNlMixed ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
                  rho_, frhot_, rhof_, rho_off_, (float)p_.dt, (float)kp_, (float)p_.zeta, (float)p_.rho_0,
                  (float)rho_off_};
