@@ -1,16 +1,18 @@
-// swc_adjoint_impl.cuh -- the discrete adjoint of the FP64 time step and the
-// segmented recompute behind swc_backward (included by the FP64 engine only).
+// swc_adjoint_impl.cuh -- the discrete adjoint of the time step and the recompute
+// behind swc_backward (instantiated for the FP64 engine, T = double, and for the FP32
+// adjoint of the mixed engine, T = float).
 //
 // Trajectory, two schedules. K = adjoint_ckpt > 0: swc_step kept the state every K
 // steps (swc_set_state kept step 0); swc_backward walks the segments from the last,
 // restores the segment's first state, reruns its steps keeping a tape of the
 // intermediates each adjoint step reads, then applies the adjoint steps in reverse.
-// Device memory: (T/K + 2) checkpoints of 6 N^3 doubles + K tape slots of kTape N^3
-// doubles + the adjoint work arrays (kAdj N^3 doubles). adjoint_ckpt = -1: binomial
-// checkpointing (Griewank's schedule): only the initial state is kept by the forward;
-// with s snapshot slots and t the least integer with C(s + t, t) >= T, the reversal
-// rerun each forward step at most t times plus once for the tape, the tape holds one
-// step, and s is the largest count that fits under adjoint_cap_gb.
+// Device memory: (T/K + 2) checkpoints + K tape slots of kTape N^3 values + the adjoint
+// work arrays (kAdj N^3 values). adjoint_ckpt = -1: binomial checkpointing (Griewank's
+// optimal schedule, reverse_binomial): only the initial state is kept by the forward;
+// s snapshot slots (the largest count that fits under adjoint_cap_gb) and a one-step
+// tape whose fields are mostly read in place; with S = s + 1 and t the least integer
+// with C(S + t, t) >= T, the reversal advances t T - C(S + t, t - 1) steps plus one
+// taped rerun per step.
 #pragma once
 
 #include "swc_adjoint_kernels.cuh"
@@ -32,7 +34,11 @@ enum {
   AJ_FGPX, AJ_FGPY, AJ_FGPZ, AJ_SX, AJ_SY, AJ_SZ, AJ_FG, AJ_E, AJ_LAPR, AJ_L, AJ_RQ, kAdj
 };
 
-template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_steps) {
+// Fields the one-step tape of the binomial schedule copies (the others are read in
+// place): the incoming density, and in the mixed engine the FP64 state narrowed to FP32.
+constexpr int kTapeCopied(bool mixed) { return mixed ? 4 : 1; }
+
+template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_fields) {
   const size_t ng = (size_t)g_.ng;
   if (!adj_) {
     if (cudaMalloc(&adj_, (size_t)kAdj * ng * sizeof(T)) != cudaSuccess ||
@@ -42,16 +48,16 @@ template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_steps) {
       return SWC_ERR_OOM;
     }
   }
-  if (tape_steps_ < tape_steps) {
+  if (tape_fields_ < tape_fields) {
     if (tape_) cudaFree(tape_);
     tape_ = nullptr;
-    if (cudaMalloc(&tape_, tape_steps * (size_t)kTape * ng * sizeof(T)) != cudaSuccess) {
+    if (cudaMalloc(&tape_, tape_fields * ng * sizeof(T)) != cudaSuccess) {
       cudaGetLastError();
-      tape_steps_ = 0;
-      set_error("cudaMalloc of the adjoint tape failed (%zu MB)", (tape_steps * kTape * ng * sizeof(T)) >> 20);
+      tape_fields_ = 0;
+      set_error("cudaMalloc of the adjoint tape failed (%zu MB)", (tape_fields * ng * sizeof(T)) >> 20);
       return SWC_ERR_OOM;
     }
-    tape_steps_ = tape_steps;
+    tape_fields_ = tape_fields;
   }
   return SWC_OK;
 }
@@ -291,16 +297,20 @@ template <typename T> int StepEngine<T>::tape_and_adjoint(int64_t n) {
 template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n, bool alias) {
   const size_t ng = (size_t)g_.ng;
   constexpr bool mixed = !std::is_same<T, double>::value;
+  int packed = 0;  // alias mode: the copied fields sit one after another in tp
   auto put = [&](int q, const void* src, bool is_double) -> int {
+    T* dst = tp + (size_t)(alias ? packed++ : q) * ng;
+    if (alias) tape_alias_[q] = dst;
     if (mixed && is_double) {
-      narrow_kernel<<<(unsigned)((ng / 4 + 255) / 256), 256, 0, stream_>>>((const double*)src, (float*)(tp + q * ng),
+      narrow_kernel<<<(unsigned)((ng / 4 + 255) / 256), 256, 0, stream_>>>((const double*)src, (float*)dst,
                                                                            (long long)ng);
       SWC_CK(cudaGetLastError());
     } else {
-      SWC_CK(cudaMemcpyAsync(tp + (size_t)q * ng, src, ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+      SWC_CK(cudaMemcpyAsync(dst, src, ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
     }
     return SWC_OK;
   };
+  for (int q = 0; q < kTape; ++q) tape_alias_[q] = nullptr;
   SWC_TRY(put(TP_RHOIN, rho_, true));
   const bool relax = !(n > p_.divv_switch || p_.load == 1);
   SWC_TRY(run_graph(relax, n == 1, true, true));  // the diagnostic variant keeps psi_old and v_sol
@@ -308,7 +318,6 @@ template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n, bool alia
                             amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
                             vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
   for (int q = 0; q < kTape; ++q) {
-    tape_alias_[q] = nullptr;
     if (!src[q]) continue;
     const bool is_double = q == TP_QOLD || q == TP_QNEW || q == TP_RHONEW;
     if (alias && !(mixed && is_double)) tape_alias_[q] = static_cast<const T*>(src[q]);
@@ -328,8 +337,8 @@ template <typename T> int StepEngine<T>::advance(int64_t from, int64_t k) {
   return SWC_OK;
 }
 
-// C(s + t, t): the most steps s snapshot slots reverse with each step rerun <= t times
-// (saturating).
+// C(s + t, t), saturating: the most steps s held states reverse with each step
+// advanced at most t times.
 static inline int64_t binomial_reach(int64_t s, int64_t t) {
   double c = 1.0;
   for (int64_t i = 1; i <= t; ++i) {
@@ -357,13 +366,19 @@ int StepEngine<T>::reverse_binomial(int64_t l, int64_t n, size_t sl, size_t ff, 
     }
     return SWC_OK;
   }
-  int64_t t = 1;
-  while (binomial_reach(nfree, t) < n) ++t;
-  const int64_t right = std::min<int64_t>(n - 1, binomial_reach(nfree - 1, t));
-  const int64_t m = n - right;
+  // optimal first split (Griewank): with S = nfree + 1 states held (the loaded one
+  // counts) and t the least integer with C(S + t, t) >= n, advance
+  // m = max(n - C(S - 1 + t, t), C(S + t - 2, t - 2)) steps (within [1, n - 1]) before
+  // the next snapshot; the reversal then costs t n - C(S + t, t - 1) advances in all
+  int64_t t = 0;
+  while (binomial_reach(nfree + 1, t) < n) ++t;
+  int64_t m = n - std::min<int64_t>(n, binomial_reach(nfree, t));
+  if (t >= 2) m = std::max<int64_t>(m, binomial_reach(nfree + 1, t - 2));
+  m = std::min<int64_t>(std::max<int64_t>(m, 1), n - 1);
+  const int64_t right = n - m;
   SWC_TRY(restore_ckpt(sl));
   SWC_TRY(advance(l, m));
-  SWC_TRY(save_ckpt(ff));
+  SWC_TRY(save_ckpt(ff, false));
   SWC_TRY(reverse_binomial(l + m, right, ff, ff + 1, nfree - 1));
   return reverse_binomial(l, m, sl, ff, nfree);
 }
@@ -390,16 +405,22 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
   SWC_CK(cudaStreamSynchronize(stream_));
   const size_t ng = (size_t)g_.ng;
   const int64_t Tn = nloop_;
-  SWC_TRY(adjoint_alloc(binomial ? 1 : (size_t)(Tn < K ? (Tn > 0 ? Tn : 1) : K)));
+  constexpr bool mixed = !std::is_same<T, double>::value;
+  const size_t tape_fields = binomial ? (size_t)kTapeCopied(mixed)
+                                      : (size_t)(Tn < K ? (Tn > 0 ? Tn : 1) : K) * kTape;
+  SWC_TRY(adjoint_alloc(tape_fields));
   // the final state, restored when the call returns (slot past the trajectory's)
   const size_t last_slot = binomial ? 1 : (size_t)(Tn / K) + 1;
   SWC_TRY(save_ckpt(last_slot));
   int64_t nsnap = 0;
   if (binomial) {
-    // snapshot slots under the cap: engine arrays + adjoint work + tape + slots 0, 1 + s
-    const size_t slot_bytes = ckpt_slot_bytes();
+    // snapshot slots under the cap: engine arrays + adjoint work + tape + slots 0, 1
+    // (allocated) + s snapshots without psi
+    const size_t slot_bytes = ckpt_slot_bytes(false);
+    size_t held = 0;
+    for (size_t b : ckpt_bytes_) held += b;
     const size_t used = engine_bytes_ + (size_t)kAdj * ng * sizeof(T) + pgrad_doubles() * 8 +
-                        (size_t)kTape * ng * sizeof(T) + ckpt_.size() * slot_bytes + (stage_ ? ng * 8 : 0);
+                        tape_fields_ * ng * sizeof(T) + held + (stage_ ? ng * 8 : 0);
     double cap = p_.adjoint_cap_gb * 1e9;
     if (cap <= 0) {
       size_t fr = 0, tot = 0;

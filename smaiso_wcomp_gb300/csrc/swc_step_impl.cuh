@@ -873,9 +873,10 @@ template <typename T> class StepEngine : public EngineBase {
 
  private:
   // ---- adjoint support (checkpoints here; the adjoint itself in swc_adjoint_impl.cuh)
-  int save_ckpt(size_t slot);
-  size_t ckpt_slot_bytes() const;
+  int save_ckpt(size_t slot, bool with_psi = true);
+  size_t ckpt_slot_bytes(bool with_psi = true) const;
   int restore_ckpt(size_t slot);
+  int psi_from_state();  // psi = DCT-III^3 psiq with the step's own last three passes
   // FP64 engine: the FP64 adjoint (swc_adjoint_impl.cuh, in swc_step_fp64.cu); mixed
   // engine: the same adjoint in FP32 on the mixed trajectory (swc_step_mixed_adj.cu)
   int backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
@@ -884,19 +885,21 @@ template <typename T> class StepEngine : public EngineBase {
   int field_to_host(const T* src, double* dst);
   int stage_alloc();
   int adjoint_step(size_t slot, bool relax, bool first);
-  int adjoint_alloc(size_t tape_steps);
+  int adjoint_alloc(size_t tape_fields);
   int tape_and_adjoint(int64_t n);                        // step n from the loaded state n-1
   int advance(int64_t from, int64_t k);                   // k plain steps from state `from`
   int reverse_binomial(int64_t l, int64_t n, size_t sl, size_t ff, int64_t nfree);
   int64_t fwd_steps_ = 0;          // forward steps rerun by the current swc_backward
   size_t engine_bytes_ = 0;        // device bytes of the engine's own arrays
   std::vector<double*> ckpt_;      // state at steps 0, K, 2K, ... (6 arrays each)
+  std::vector<size_t> ckpt_bytes_; // allocated bytes of each slot
+  std::vector<char> ckpt_psi_;     // the slot holds psi (else restore recomputes it)
   T* tape_ = nullptr;              // forward intermediates of one segment
   // binomial schedule: the tape step's fields read in place (the adjoint step that
   // consumes them runs next on the same stream) instead of copied into tape_
   const T* tape_alias_[32] = {};
   bool tape_alias_on_ = false;
-  size_t tape_steps_ = 0;
+  size_t tape_fields_ = 0;  // tape_ capacity in fields of n^3 values
   T* adj_ = nullptr;               // adjoint work arrays
   double* pgrad_ = nullptr;        // parameter-gradient totals, then per-block cells
   int* status_ = nullptr;          // set by a transform pass whose bounded wait ran out
@@ -994,6 +997,8 @@ template <typename T> void StepEngine<T>::release() {
   copy_stream_ = nullptr;
   for (double* c : ckpt_) cudaFree(c);
   ckpt_.clear();
+  ckpt_bytes_.clear();
+  ckpt_psi_.clear();
   if (tape_) cudaFree(tape_);
   if (adj_) cudaFree(adj_);
   if (pgrad_) cudaFree(pgrad_);
@@ -1333,27 +1338,42 @@ template <typename T> int StepEngine<T>::set_state(const double* psi, const doub
 
 // Checkpoint slot: psiq, psiq_old, rho (FP64), Nl_old, f_rho, psi (the engine's
 // precision: FP64, or FP32 in the mixed engine), packed: ckpt_slot_bytes() each.
-template <typename T> size_t StepEngine<T>::ckpt_slot_bytes() const {
-  return (size_t)g_.ng * (3 * sizeof(double) + 3 * sizeof(T));
+// Without psi (with_psi = false, the binomial schedule's snapshots after step 0): a
+// state that a step wrote has psi = DCT-III^3 psiq from that step's last three passes,
+// which restore_ckpt reruns on the restored psiq, bit for bit (step 0's psi comes from
+// swc_set_state's own transform and is always kept).
+template <typename T> size_t StepEngine<T>::ckpt_slot_bytes(bool with_psi) const {
+  return (size_t)g_.ng * (3 * sizeof(double) + (with_psi ? 3 : 2) * sizeof(T));
 }
 
-template <typename T> int StepEngine<T>::save_ckpt(size_t slot) {
+template <typename T> int StepEngine<T>::save_ckpt(size_t slot, bool with_psi) {
   const size_t ng = (size_t)g_.ng;
   while (ckpt_.size() <= slot) {
+    ckpt_.push_back(nullptr);
+    ckpt_bytes_.push_back(0);
+    ckpt_psi_.push_back(0);
+  }
+  const size_t need = ckpt_slot_bytes(with_psi);
+  if (ckpt_bytes_[slot] < need) {
+    if (ckpt_[slot]) cudaFree(ckpt_[slot]);
+    ckpt_[slot] = nullptr;
+    ckpt_bytes_[slot] = 0;
     double* c = nullptr;
-    if (cudaMalloc(&c, ckpt_slot_bytes()) != cudaSuccess) {
+    if (cudaMalloc(&c, need) != cudaSuccess) {
       cudaGetLastError();
-      set_error("cudaMalloc for an adjoint checkpoint failed (%zu MB)", ckpt_slot_bytes() >> 20);
+      set_error("cudaMalloc for an adjoint checkpoint failed (%zu MB)", need >> 20);
       return SWC_ERR_OOM;
     }
-    ckpt_.push_back(c);
+    ckpt_[slot] = c;
+    ckpt_bytes_[slot] = need;
   }
+  ckpt_psi_[slot] = with_psi ? 1 : 0;
   char* c = reinterpret_cast<char*>(ckpt_[slot]);
   constexpr bool mixed = !std::is_same<T, double>::value;
   const void* src[6] = {psiq_, psiq_old_, rho_, nlq_, mixed ? (const void*)frhot_ : (const void*)frho_, psi_};
   const size_t sz[6] = {8, 8, 8, sizeof(T), sizeof(T), sizeof(T)};
   size_t off = 0;
-  for (int q = 0; q < 6; ++q) {
+  for (int q = 0; q < (with_psi ? 6 : 5); ++q) {
     SWC_CK(cudaMemcpyAsync(c + off, src[q], ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
     off += ng * sz[q];
   }
@@ -1366,12 +1386,24 @@ template <typename T> int StepEngine<T>::restore_ckpt(size_t slot) {
   constexpr bool mixed = !std::is_same<T, double>::value;
   void* dst[6] = {psiq_, psiq_old_, rho_, nlq_, mixed ? (void*)frhot_ : (void*)frho_, psi_};
   const size_t sz[6] = {8, 8, 8, sizeof(T), sizeof(T), sizeof(T)};
+  const bool with_psi = ckpt_psi_[slot] != 0;
   size_t off = 0;
-  for (int q = 0; q < 6; ++q) {
+  for (int q = 0; q < (with_psi ? 6 : 5); ++q) {
     SWC_CK(cudaMemcpyAsync(dst[q], c + off, ng * sz[q], cudaMemcpyDeviceToDevice, stream_));
     off += ng * sz[q];
   }
-  return refresh_copies(2);  // the mixed engine's FP32 copies of rho and psiq (f_rho restored above)
+  SWC_TRY(refresh_copies(2));  // the mixed engine's FP32 copies of rho and psiq (f_rho restored above)
+  return with_psi ? SWC_OK : psi_from_state();
+}
+
+template <typename T> int StepEngine<T>::psi_from_state() {
+  using LP = LdPlain<T, T>;
+  using SP = StPlain<T, T>;
+  if constexpr (std::is_same<T, double>::value) SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{psi_})));
+  else SWC_TRY((pass<K_C3, 2>(LP{psiqf_}, SP{psi_})));
+  SWC_TRY((pass<K_C3, 1>(LP{psi_}, SP{psi_})));
+  SWC_TRY((pass<K_C3, 0>(LP{psi_}, SP{psi_})));
+  return SWC_OK;
 }
 
 template <typename T> int StepEngine<T>::check_step(int nsteps) {

@@ -3,7 +3,7 @@ forward through the C ABI, and a torch.autograd.gradcheck over the thin shim."""
 import numpy as np
 import pytest
 
-from smaiso_wcomp_gb300 import abi, ic
+from smaiso_wcomp_gb300 import abi, ic, schedule
 from smaiso_wcomp_gb300.engine import Engine
 
 pytestmark = pytest.mark.gpu
@@ -97,8 +97,9 @@ def test_torch_gradcheck_through_the_shim(lib):
 def test_binomial_schedule_matches_segments(lib, snapshots):
     """Binomial checkpointing (adjoint_ckpt = -1) with 0, 1, 2, 4 and 12 snapshot slots
     reverses the same trajectory as the fixed-interval schedule: the same gradients
-    (the recompute is deterministic), with each forward step rerun at most t times plus
-    once for the tape, t the least integer with C(s + t, t) >= T."""
+    (the recompute is deterministic, snapshots after step 0 recompute psi from psiq),
+    at the optimal binomial cost (smaiso_wcomp_gb300.schedule) plus one taped rerun per
+    step."""
     shape, ds, nsteps = (16, 16, 32), 4, 13
     rng = np.random.default_rng(3)
     wp, wr = rng.standard_normal(shape), rng.standard_normal(shape)
@@ -114,10 +115,8 @@ def test_binomial_schedule_matches_segments(lib, snapshots):
     a, b = grads[-1], grads[3]
     s = min(snapshots, nsteps - 1) if snapshots > 0 else nsteps - 1
     assert a["snapshots"] == s
-    t = 1
-    while __import__("math").comb(s + t, t) < nsteps:
-        t += 1
-    assert nsteps <= a["forward_steps"] <= (t + 1) * nsteps
+    assert a["forward_steps"] == schedule.forward_steps(nsteps, s)
+    assert a["forward_steps"] == schedule.optimal_advances(nsteps, s) + nsteps
     assert b["forward_steps"] == nsteps
     for key in ("psi0", "rho0"):
         assert np.linalg.norm(a[key] - b[key]) <= 1e-12 * np.linalg.norm(b[key]), key
