@@ -58,6 +58,8 @@ def parse():
                          "its own JSON line (mixed and FP64 steps/s, mixed-vs-FP64 errors)")
     ap.add_argument("--adjoint-steps", type=int, default=None,
                     help="adjoint workloads: steps instead of the configuration's (short profiling runs)")
+    ap.add_argument("--fd-mixed", action="store_true",
+                    help="adjoint256: also 4th-order finite differences of the mixed forward (40 forward runs)")
     ap.add_argument("--divv-switch", type=int, default=None,
                     help="adjoint workloads: relax-phase length instead of the reference's 50")
     ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
@@ -263,7 +265,7 @@ def gradient_forward_ratio(steps, ckpt=20, n=128):
 CAL_COEFFS = ("alpha", "beta", "gamma", "nu", "rho_0")
 
 
-def calibration_adjoint(which, steps=None, divv_switch=None):
+def calibration_adjoint(which, steps=None, divv_switch=None, fd_mixed=False):
     """The calibration-adjoint configurations: adjoint128 -- FP64 forward + FP64 adjoint,
     128^3, 400 steps, checkpoints every 20 steps; adjoint256 -- mixed forward + FP32
     adjoint, 256^3, 2000 steps, binomial checkpoint/recompute under a 40 GB device-memory
@@ -323,6 +325,23 @@ def calibration_adjoint(which, steps=None, divv_switch=None):
            "forward_steps_rerun": g["forward_steps"], "snapshots": g["snapshots"],
            "adjoint_step_over_forward_step": ((t2 - t1) - g["forward_steps"] * (t1 - t0) / steps) / (t1 - t0),
            "gradient": {c: g[c] for c in CAL_COEFFS}}
+    if which == "adjoint256" and fd_mixed:
+        # 4th-order central differences of the mixed forward itself (the trajectory the
+        # FP32 adjoint differentiates) at h = 1e-2 and 1e-3 relative: the forward's FP32
+        # rounding makes L's noise too large for the h = 1e-6 of the FP64 check
+        def at_m(c, x):
+            q = abi.default_params(n, rho_0=0.8, precision=prec, **dv)
+            setattr(q, c, x)
+            return forward(q)
+        for hr in (1e-2, 1e-3):
+            fd4 = {}
+            for c in CAL_COEFFS:
+                v = getattr(p, c)
+                h = hr * abs(v)
+                fd4[c] = (8 * (at_m(c, v + h) - at_m(c, v - h)) - (at_m(c, v + 2 * h) - at_m(c, v - 2 * h))) / (12 * h)
+            res[f"fd4_mixed_h{hr:g}"] = fd4
+            res[f"rel_err_vs_fd4_mixed_h{hr:g}"] = {c: abs(g[c] - fd4[c]) / max(abs(fd4[c]), 1e-300)
+                                                   for c in CAL_COEFFS}
     if which == "adjoint128":
         # central differences with the configuration's h = 1e-6 (relative), and 4th-order
         # central differences with h = 1e-3 (relative): at h = 1e-6 the FP64 roundoff of
@@ -472,7 +491,8 @@ def main():
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
     if args.workload in ("adjoint128", "adjoint256", "adjoint256_fp64"):
-        print(json.dumps(calibration_adjoint(args.workload, args.adjoint_steps, args.divv_switch)), flush=True)
+        print(json.dumps(calibration_adjoint(args.workload, args.adjoint_steps, args.divv_switch, args.fd_mixed)),
+              flush=True)
         return
     if args.workload == "dislocations":
         print(json.dumps(dislocation_run(args.steps, args.warmup, args.accuracy_steps or 50, local)), flush=True)
