@@ -1634,9 +1634,9 @@ template <typename T> int StepEngine<T>::get_field_async(int field, double* dst)
       set_error("cudaMalloc of the field snapshot failed (%zu MB)", (n * sizeof(double)) >> 20);
       return SWC_ERR_OOM;
     }
-    SWC_CK(cudaEventCreateWithFlags(&aready_[b], cudaEventDisableTiming));
-    SWC_CK(cudaEventCreateWithFlags(&adone_[b], cudaEventDisableTiming));
   }
+  if (!aready_[b]) SWC_CK(cudaEventCreateWithFlags(&aready_[b], cudaEventDisableTiming));
+  if (!adone_[b]) SWC_CK(cudaEventCreateWithFlags(&adone_[b], cudaEventDisableTiming));
   if (is_d || std::is_same<T, double>::value) {
     SWC_CK(cudaMemcpyAsync(astage_[b], src, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_));
   } else {
