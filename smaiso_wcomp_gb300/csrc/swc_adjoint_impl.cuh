@@ -313,8 +313,12 @@ template <typename T> int StepEngine<T>::record_tape(T* tp, int64_t n, bool alia
   for (int q = 0; q < kTape; ++q) tape_alias_[q] = nullptr;
   SWC_TRY(put(TP_RHOIN, rho_, true));
   const bool relax = !(n > p_.divv_switch || p_.load == 1);
-  SWC_TRY(run_graph(relax, n == 1, true, true));  // the diagnostic variant keeps psi_old and v_sol
-  const void* src[kTape] = {psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
+  // the diagnostic variant keeps the input psi in psi_old and writes v_sol; the tape
+  // variant (alias mode: nothing runs between this step and its adjoint) writes v_sol and
+  // leaves the input psi in psi_, without the diagnostic reductions
+  if (alias) SWC_TRY(run_graph(relax, n == 1, false, true, true));
+  else SWC_TRY(run_graph(relax, n == 1, true, true));
+  const void* src[kTape] = {alias ? psi_ : psi_old_, psiq_old_, psiq_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2],
                             amp_f_, lpsi_, lapR_, nullptr, rho_, v_[0], v_[1], v_[2], divv_, vsol_[0],
                             vsol_[1], vsol_[2], virr_[0], virr_[1], virr_[2]};
   for (int q = 0; q < kTape; ++q) {

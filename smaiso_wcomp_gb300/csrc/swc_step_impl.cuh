@@ -932,9 +932,12 @@ template <typename T> class StepEngine : public EngineBase {
   int transform_vsol();                                    // (swc_step_part_c.cuh)
   // diag: the diagnostic variant (S15 reductions, psi_old <- psi rotation, energy field);
   // vsol: the Stokes kernel also writes v_sol (the last step of a swc_step call)
-  int run_graph(bool relax, bool first, bool diag, bool vsol);
-  int graph_of(bool relax, bool first, bool diag, bool vsol, cudaGraphExec_t* out, int* key);
+  // tape (swc_backward's one-step tape): the new psi goes to psi_new_, so psi_ keeps
+  // the step's input psi, and no diagnostics run
+  int run_graph(bool relax, bool first, bool diag, bool vsol, bool tape = false);
+  int graph_of(bool relax, bool first, bool diag, bool vsol, bool tape, cudaGraphExec_t* out, int* key);
   bool cap_vsol_ = false;  // vsol flag of the variant being captured
+  bool cap_tape_ = false;  // tape flag of the variant being captured
   int64_t diag_step_ = -1;  // nLoop of the last step that ran the diagnostics
   int64_t pending_diag_ = -1;  // diagnostic step enqueued, its sums not yet read
   int check_step(int nsteps);
@@ -1222,16 +1225,19 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
 
 // The instantiated graph of one step variant, captured on first use.
 template <typename T>
-int StepEngine<T>::graph_of(bool relax, bool first, bool diag, bool vsol, cudaGraphExec_t* out, int* key_out) {
-  vsol = vsol || diag;
-  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0) | (vsol ? 8 : 0);
+int StepEngine<T>::graph_of(bool relax, bool first, bool diag, bool vsol, bool tape, cudaGraphExec_t* out,
+                            int* key_out) {
+  vsol = vsol || diag || tape;
+  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0) | (vsol ? 8 : 0) | (tape ? 16 : 0);
   auto it = graphs_.find(key);
   if (it == graphs_.end()) {
     cudaGraph_t graph = nullptr;
     SWC_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     launches_ = 0;
     cap_vsol_ = vsol;
+    cap_tape_ = tape;
     int rc = enqueue_step(relax, first, diag);
+    cap_tape_ = false;
     cudaError_t e = cudaStreamEndCapture(stream_, &graph);
     if (rc) {
       if (graph) cudaGraphDestroy(graph);
@@ -1256,10 +1262,10 @@ int StepEngine<T>::graph_of(bool relax, bool first, bool diag, bool vsol, cudaGr
   return SWC_OK;
 }
 
-template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag, bool vsol) {
+template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool diag, bool vsol, bool tape) {
   cudaGraphExec_t exec;
   int key;
-  SWC_TRY(graph_of(relax, first, diag, vsol, &exec, &key));
+  SWC_TRY(graph_of(relax, first, diag, vsol, tape, &exec, &key));
   SWC_CK(cudaGraphLaunch(exec, stream_));
   last_launches_ += graph_kernels_[key];
   return SWC_OK;
@@ -1277,7 +1283,7 @@ template <typename T> int StepEngine<T>::prepare() {
   int key;
   for (int relax = 0; relax < 2; ++relax)
     for (int first = 0; first < 2; ++first)
-      for (int v = 0; v < 3; ++v) SWC_TRY(graph_of(relax, first, v == 2, v >= 1, &exec, &key));
+      for (int v = 0; v < 3; ++v) SWC_TRY(graph_of(relax, first, v == 2, v >= 1, false, &exec, &key));
   return SWC_OK;
 }
 

@@ -37,7 +37,7 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
   // space in place; v_sol alone is transformed on demand (transform_vsol)
   for (int ax = 0; ax < 3; ++ax) SWC_TRY(inverse_velocity(ax, v_[ax], v_[ax]));
   // S12 + S13 + S14 (REF:2121-2197): rho update, Nl, its DCT, the psiq update, psi = iDCT(psiq_new)
-  T* pout = diag ? psi_new_ : psi_;
+  T* pout = (diag || cap_tape_) ? psi_new_ : psi_;  // the tape variant keeps the input psi
   if constexpr (std::is_same<T, double>::value) {
     // FP64 engine: the reference's expressions; the CN update in the Nl transform's last pass
     LdNl<T> ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
