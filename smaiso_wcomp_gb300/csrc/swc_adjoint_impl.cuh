@@ -31,7 +31,7 @@ static_assert(kTape <= 32, "tape_alias_ holds one pointer per tape field");
 enum {
   AJ_Q = 0, AJ_QO, AJ_NLO, AJ_R, AJ_F, AJ_NL, AJ_FX, AJ_FY, AJ_FZ, AJ_MU, AJ_A, AJ_PSI, AJ_VX, AJ_VY, AJ_VZ,
   AJ_GPX, AJ_GPY, AJ_GPZ, AJ_GRX, AJ_GRY, AJ_GRZ, AJ_DIVV, AJ_DOTX, AJ_DOTY, AJ_DOTZ, AJ_SDX, AJ_SDY, AJ_SDZ,
-  AJ_FGPX, AJ_FGPY, AJ_FGPZ, AJ_SX, AJ_SY, AJ_SZ, AJ_FG, AJ_E, AJ_LAPR, AJ_L, AJ_RQ, kAdj
+  AJ_FGPX, AJ_FGPY, AJ_FGPZ, AJ_SX, AJ_SY, AJ_SZ, AJ_FG, AJ_E, AJ_LAPR, AJ_L, kAdj
 };
 
 // Fields the one-step tape of the binomial schedule copies (the others are read in
@@ -212,42 +212,29 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
                                                 AJ(AJ_GPZ));
     SWC_CK(cudaGetLastError());
   }
-  // (11) gradients (REF:1166-1250): grad_a = inverse-mixed(-fac Vs shift X); transpose =
-  //      forward-mixed, then the output weights and the shifted gather into X_bar
-  //      (adj_grad_kernel, both gradient families in one pass)
-  for (int which = 0; which < 2; ++which) {
-    T* bgx = adj_ + (which == 0 ? AJ_GPX : AJ_GRX) * ng;
-    T* bgy = adj_ + (which == 0 ? AJ_GPY : AJ_GRY) * ng;
-    T* bgz = adj_ + (which == 0 ? AJ_GPZ : AJ_GRZ) * ng;
-    SWC_TRY((pass<K_C2, 2>(LP{bgx}, SP{bgx})));
-    SWC_TRY((pass<K_C2, 1>(LP{bgx}, SP{bgx})));
-    SWC_TRY((pass<K_S2, 0>(LP{bgx}, SP{bgx})));
-    SWC_TRY((pass<K_C2, 2>(LP{bgy}, SP{bgy})));
-    SWC_TRY((pass<K_S2, 1>(LP{bgy}, SP{bgy})));
-    SWC_TRY((pass<K_C2, 0>(LP{bgy}, SP{bgy})));
-    SWC_TRY((pass<K_S2, 2>(LP{bgz}, SP{bgz})));
-    SWC_TRY((pass<K_C2, 1>(LP{bgz}, SP{bgz})));
-    SWC_TRY((pass<K_C2, 0>(LP{bgz}, SP{bgz})));
-  }
+  // (11) gradients (REF:1166-1250): the forward takes grad_a psi and grad_a rho with one
+  //      derivative pass along axis a each (DCT-II, shifted multiply, DST-III); their
+  //      transposes are one pass each of the transposed kind (DST-II, transposed shift,
+  //      DCT-III), summed into psi_bar and rho_bar by adj_gsum_kernel
   {
-    AdjGradArgs<T> a{AJ(AJ_GPX), AJ(AJ_GPY), AJ(AJ_GPZ), AJ(AJ_GRX), AJ(AJ_GRY), AJ(AJ_GRZ), AJ(AJ_Q), AJ(AJ_RQ),
-                     vs_[0], vs_[1], vs_[2], (T)scale_, sine_w(0, 0.5), sine_w(1, 0.5), sine_w(2, 0.5), w2};
-    adj_grad_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
+    const T cx = (T)(1.0 / (2.0 * g_.nx)), cy = (T)(1.0 / (2.0 * g_.ny)), cz = (T)(1.0 / (2.0 * g_.nz));
+    T* bgp[3] = {AJ(AJ_GPX), AJ(AJ_GPY), AJ(AJ_GPZ)};
+    T* bgr[3] = {AJ(AJ_GRX), AJ(AJ_GRY), AJ(AJ_GRZ)};
+    for (T* const* b : {bgp, bgr}) {
+      SWC_TRY((pass<K_DERIVT, 2>(LP{b[2]}, SP{b[2]}, MulDeriv<T>{vs_[2], cz, 2})));
+      SWC_TRY((pass<K_DERIVT, 1>(LP{b[1]}, SP{b[1]}, MulDeriv<T>{vs_[1], cy, 1})));
+      SWC_TRY((pass<K_DERIVT, 0>(LP{b[0]}, SP{b[0]}, MulDeriv<T>{vs_[0], cx, 0})));
+    }
+    adj_gsum_kernel<T><<<blocks, 256, 0, stream_>>>(g_, bgp[0], bgp[1], bgp[2], bgr[0], bgr[1], bgr[2], AJ(AJ_PSI),
+                                                 AJ(AJ_R));
     SWC_CK(cudaGetLastError());
   }
-  // (12) rho-hat = DCT-II^3 rho (REF:1104-1106): rho_bar += DCT-III^3 D0 rhoq_bar
-  //      (D0 applied by adj_grad_kernel)
-  T* rq = adj_ + AJ_RQ * ng;
-  SWC_TRY((pass<K_C3, 2>(LP{rq}, SP{rq})));
-  SWC_TRY((pass<K_C3, 1>(LP{rq}, SP{rq})));
-  SWC_TRY((pass<K_C3, 0>(LP{rq}, SP{rq})));
-  // (13) the step's psi = DCT-III^3 psiq: psiq_bar += D0^-1 DCT-II^3 psi_bar; then both
-  //      accumulations (adj_fold_kernel)
+  // (13) the step's psi = DCT-III^3 psiq: psiq_bar += D0^-1 DCT-II^3 psi_bar
   T* bp = adj_ + AJ_PSI * ng;
   SWC_TRY((pass<K_C2, 2>(LP{bp}, SP{bp})));
   SWC_TRY((pass<K_C2, 1>(LP{bp}, SP{bp})));
   SWC_TRY((pass<K_C2, 0>(LP{bp}, SP{bp})));
-  adj_fold_kernel<T><<<blocks, 256, 0, stream_>>>(g_, bp, wh, rq, AJ(AJ_Q), AJ(AJ_R));
+  adj_fold_kernel<T><<<blocks, 256, 0, stream_>>>(g_, bp, wh, AJ(AJ_Q));
   SWC_CK(cudaGetLastError());
   return SWC_OK;
 }

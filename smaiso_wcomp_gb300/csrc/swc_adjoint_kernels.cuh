@@ -775,76 +775,44 @@ __global__ void __launch_bounds__(256) adj_amp_kernel(Grid g, const T* y, const 
   bz.store(bgz, x);
 }
 
-// Transpose of the shifted spectral derivatives of the gradients (REF:1166-1250): the
-// forward wrote grad_a-hat[c] = -fac Vs_a[c] X-hat[c+1] (c < n_a - 1), so with g_a the
-// transposed inverse transform of grad_a-bar (without its output weights w[a]),
-//   X-bar[c'] += -fac Vs_a[c'-1] w[a](c'-1) g_a[c'-1]   (c' >= 1).
-// Both families at once: psi-hat (fac 1, added to bQ) and rho-hat (fac = scale,
-// written to bRq times the input weights w2 of the transposed transform it feeds).
-template <typename T> struct AdjGradArgs {
-  const T *gpx, *gpy, *gpz, *grx, *gry, *grz;
-  T *bQ, *bRq;
-  const T *vsx, *vsy, *vsz;
-  T scale;
-  AxisWeights<T> wx, wy, wz, w2;
-};
+// End of step (11) of the adjoint: the transposed derivative passes of both gradient
+// families summed into the cotangents of the step's input psi and rho.
 template <typename T>
-__global__ void __launch_bounds__(256) adj_grad_kernel(Grid g, AdjGradArgs<T> a) {
-  Pt4 p;
-  if (!pt4(g, p)) return;
-  const int i = p.i, j = p.j, k = p.k;
-  const long long x = p.idx, sx = 1LL << (g.ly + g.lz), sy = g.nz;
-  auto gather = [&](const T* fx, const T* fy, const T* fz, T fac, V4<T>& acc) {
-    V4<T> t;
-    if (i >= 1) {
-      t.load(fx, x - sx);
-      const T c = -fac * a.vsx[i - 1];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc.v[e] += c * (t.v[e] * a.wx.at(g, i - 1, j, k + e));
-    }
-    if (j >= 1) {
-      t.load(fy, x - sy);
-      const T c = -fac * a.vsy[j - 1];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc.v[e] += c * (t.v[e] * a.wy.at(g, i, j - 1, k + e));
-    }
-    t.load(fz, x);
-    const T sh[4] = {(k >= 1) ? fz[x - 1] : T(0.0), t.v[0], t.v[1], t.v[2]};
-#pragma unroll
-    for (int e = 0; e < 4; ++e)
-      if (k + e >= 1) acc.v[e] += (-fac * a.vsz[k + e - 1]) * (sh[e] * a.wz.at(g, i, j, k + e - 1));
-  };
-  V4<T> q, r = V4<T>::zero();
-  q.load(a.bQ, x);
-  gather(a.gpx, a.gpy, a.gpz, T(1.0), q);
-  q.store(a.bQ, x);
-  gather(a.grx, a.gry, a.grz, a.scale, r);
-#pragma unroll
-  for (int e = 0; e < 4; ++e) r.v[e] = r.v[e] * a.w2.at(g, i, j, k + e);
-  r.store(a.bRq, x);
-}
-
-// End of the adjoint step, the transposes of psi = DCT-III^3 psiq and of
-// rho-hat = DCT-II^3 rho (REF:1104-1106): bQ += wq ypsi, bR += yrho (ypsi without the
-// output weights wq of its transposed transform).
-template <typename T>
-__global__ void __launch_bounds__(256) adj_fold_kernel(Grid g, const T* ypsi, AxisWeights<T> wq, const T* yrho,
-                                                       T* bQ, T* bR) {
+__global__ void __launch_bounds__(256) adj_gsum_kernel(Grid g, const T* px, const T* py, const T* pz, const T* rx,
+                                                       const T* ry, const T* rz, T* bpsi, T* brho) {
   Pt4 p;
   if (!pt4(g, p)) return;
   const long long x = p.idx;
-  V4<T> yp, yr, q, r;
-  yp.load(ypsi, x);
-  yr.load(yrho, x);
-  q.load(bQ, x);
-  r.load(bR, x);
+  V4<T> a, b, c, o;
+  a.load(px, x);
+  b.load(py, x);
+  c.load(pz, x);
+  o.load(bpsi, x);
 #pragma unroll
-  for (int e = 0; e < 4; ++e) {
-    q.v[e] = q.v[e] + yp.v[e] * wq.at(g, p.i, p.j, p.k + e);
-    r.v[e] += yr.v[e];
-  }
+  for (int e = 0; e < 4; ++e) o.v[e] += a.v[e] + b.v[e] + c.v[e];
+  o.store(bpsi, x);
+  a.load(rx, x);
+  b.load(ry, x);
+  c.load(rz, x);
+  o.load(brho, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] += a.v[e] + b.v[e] + c.v[e];
+  o.store(brho, x);
+}
+
+// End of the adjoint step, the transpose of psi = DCT-III^3 psiq (REF:2194-2197):
+// bQ += wq ypsi (ypsi without the output weights wq of its transposed transform).
+template <typename T>
+__global__ void __launch_bounds__(256) adj_fold_kernel(Grid g, const T* ypsi, AxisWeights<T> wq, T* bQ) {
+  Pt4 p;
+  if (!pt4(g, p)) return;
+  const long long x = p.idx;
+  V4<T> yp, q;
+  yp.load(ypsi, x);
+  q.load(bQ, x);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) q.v[e] = q.v[e] + yp.v[e] * wq.at(g, p.i, p.j, p.k + e);
   q.store(bQ, x);
-  r.store(bR, x);
 }
 
 // out = a * x (+ b * y): small helper for the final dL/dpsi0 = scale C2^T (bQ + bQo).

@@ -22,7 +22,10 @@ namespace swc {
 // K_FILT: DCT-II, spectral multiplier, DCT-III along the axis (one CTA).
 // K_DERIV: DCT-II, then w_i = mul(i) u_{i+1} (w_{n-1} = 0), then DST-III: the shifted
 // spectral derivative of REF:1166-1250 along one axis in one pass.
-enum Kind { K_C2 = 0, K_C3 = 1, K_S2 = 2, K_S3 = 3, K_FILT = 4, K_DERIV = 5 };
+// K_DERIVT: its transpose, DST-II, then u_j = mul(j-1) z_{j-1} (u_0 = 0), then DCT-III
+// (with FFTW's definitions the transposes' mode-0 / last-mode weights drop out: the
+// shift never reads z_{n-1} and writes u_0 = 0).
+enum Kind { K_C2 = 0, K_C3 = 1, K_S2 = 2, K_S3 = 3, K_FILT = 4, K_DERIV = 5, K_DERIVT = 6 };
 
 template <typename T> struct R2RTables {
   const cx_t<T>* fft;   // W_M^t = exp(-2 pi i t/M), t < M
@@ -370,16 +373,16 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
   const int l = tid & (L - 1);
   const int tj = tid >> ps.log2L;
   const long long my_line = line0 + l;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
 
-  stage_tables<T, (KIND == K_DERIV ? K_FILT : KIND)>(ps, tb, sfft, spost, spre);
+  stage_tables<T, ((KIND == K_DERIV || KIND == K_DERIVT) ? K_FILT : KIND)>(ps, tb, sfft, spost, spre);
 
   // ---- load: global -> bufA reals ----
   {
     T* ra = reinterpret_cast<T*>(bufA);
     auto place = [&](int p, int le, T x) {
       if constexpr (fwd_in) {
-        if (KIND == K_S2 && (p & 1)) x = -x;
+        if ((KIND == K_S2 || KIND == K_DERIVT) && (p & 1)) x = -x;
         const int q = (p & 1) ? (n - 1 - (p >> 1)) : (p >> 1);
         ra[ridx(q, le, P)] = x;
       } else {
@@ -425,8 +428,8 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
   bool swapped;  // output components are (im, re)-swapped (inverse FFT result)
   if constexpr (fwd_in) {
     run_stages<T>(ps, src, dst, l, tj, sfft);  // result in src
-    dct2_post<T, (KIND == K_DERIV ? K_C2 : KIND), MulOp>(g, ps, my_line, src, reinterpret_cast<T*>(dst), l, tj,
-                                                          spost, mul);
+    dct2_post<T, (KIND == K_DERIV ? K_C2 : (KIND == K_DERIVT ? K_S2 : KIND)), MulOp>(
+        g, ps, my_line, src, reinterpret_cast<T*>(dst), l, tj, spost, mul);
     __syncthreads();
     if constexpr (KIND == K_DERIV) {
       // w_i = mul(i) u_{i+1}, stored reversed (DST-III input), then the DST-III
@@ -441,6 +444,28 @@ __global__ void __launch_bounds__(256) r2r_pass_kernel(Grid g, PassShape ps, R2R
           v = mul(ii, jj, kk) * u[ridx(i + 1, l, P)];
         }
         w[ridx(n - 1 - i, l, P)] = v;
+      }
+      __syncthreads();
+      dct3_pre<T>(ps, reinterpret_cast<const T*>(src), dst, l, tj, spre);
+      __syncthreads();
+      { C* t = src; src = dst; dst = t; }
+      run_stages<T>(ps, src, dst, l, tj, sfft);
+      res_real = reinterpret_cast<T*>(src);
+      swapped = true;
+    } else if constexpr (KIND == K_DERIVT) {
+      // u_j = mul(j-1) z_{j-1} (u_0 = 0) from the DST-II output z, natural order (the
+      // DCT-III input), then the DCT-III
+      const T* z = reinterpret_cast<const T*>(dst);
+      T* u = reinterpret_cast<T*>(src);
+      for (int j = tj; j < n; j += ps.tpl) {
+        T v = (T)0;
+        if (j >= 1) {
+          int ii, jj, kk;
+          long long idx;
+          line_coords(g, ps.axis, my_line, j - 1, ii, jj, kk, idx);
+          v = mul(ii, jj, kk) * z[ridx(j - 1, l, P)];
+        }
+        u[ridx(j, l, P)] = v;
       }
       __syncthreads();
       dct3_pre<T>(ps, reinterpret_cast<const T*>(src), dst, l, tj, spre);

@@ -321,8 +321,9 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
   using C = cx_t<T>;
   constexpr int M = Cf::M, L = Cf::L, P = Cf::P, NT = Cf::NT, TPL = Cf::TPL, ITERS = Cf::ITERS, CH = Cf::CH;
   constexpr int R1 = Cf::R1, R2 = Cf::R2;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
-  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+  constexpr bool s2_in = (KIND == K_S2 || KIND == K_DERIVT);  // (-1)^p x_p on input
   constexpr bool xy = (AX != 2);  // x/y passes: global memory straight to/from registers
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
@@ -355,7 +356,7 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
       T a = ld(i, j, k, idx);
       xy_coords<AX>(g, my_line, p1, i, j, k, idx);
       T b = ld(i, j, k, idx);
-      if constexpr (KIND == K_S2) {
+      if constexpr (s2_in) {
         if (p0 & 1) a = -a;
         if (p1 & 1) b = -b;
       }
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
         fast_elem<N, NT, L, Cf::LOG2N, Cf::LOG2L, TPL>(g, AX, line0, tid, c0 + c, p, le, i, j, k, idx);
         T x = vals[c];
         if constexpr (fwd_in) {
-          if (KIND == K_S2 && (p & 1)) x = -x;
+          if (s2_in && (p & 1)) x = -x;
           const int q = (p & 1) ? (N - 1 - (p >> 1)) : (p >> 1);
           rb[fridx<P>(q, le)] = x;
         } else {
@@ -398,11 +399,12 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
 
   if constexpr (fwd_in) {
     fast_stage<C, M, R2, R1, TPL, P>(buf, sfft, l, tj);
-    if constexpr (xy && KIND != K_FILT && KIND != K_DERIV) {
+    if constexpr (xy && KIND != K_FILT && KIND != K_DERIV && KIND != K_DERIVT) {
       fast_post_store<T, N, KIND, AX>(g, my_line, buf, spost, l, tj, st);
       return;
     }
-    fast_post<T, N, (KIND == K_DERIV ? K_C2 : KIND), MulOp>(g, AX, line0 + l, buf, spost, l, tj, mul);
+    fast_post<T, N, (KIND == K_DERIV ? K_C2 : (KIND == K_DERIVT ? K_S2 : KIND)), MulOp>(g, AX, line0 + l, buf,
+                                                                                        spost, l, tj, mul);
     if constexpr (KIND == K_DERIV) {
       // w_i = mul(i) u_{i+1} (w_{N-1} = 0), stored reversed as the DST-III input
       constexpr int PER = N / TPL;
@@ -421,6 +423,26 @@ __global__ void __launch_bounds__(FastCfg<T, N>::NT) r2r_fast_kernel(Grid g, R2R
       __syncthreads();
 #pragma unroll
       for (int b = 0; b < PER; ++b) rb[fridx<P>(N - 1 - (tj + b * TPL), l)] = w[b];
+      __syncthreads();
+    }
+    if constexpr (KIND == K_DERIVT) {
+      // u_j = mul(j-1) z_{j-1} (u_0 = 0) from the DST-II output z, natural order (DCT-III input)
+      constexpr int PER = N / TPL;
+      T w[PER];
+#pragma unroll
+      for (int b = 0; b < PER; ++b) {
+        const int j = tj + b * TPL;
+        w[b] = (T)0;
+        if (j >= 1) {
+          int ii, jj, kk;
+          long long idx;
+          line_coords(g, AX, line0 + l, j - 1, ii, jj, kk, idx);
+          w[b] = mul(ii, jj, kk) * rb[fridx<P>(j - 1, l)];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int b = 0; b < PER; ++b) rb[fridx<P>(tj + b * TPL, l)] = w[b];
       __syncthreads();
     }
   }

@@ -446,6 +446,51 @@ __device__ __forceinline__ void pair_filt(const Grid& g, int lineA, PC* buf, con
   __syncthreads();
 }
 
+// K_DERIVT between the two FFTs, in registers (as pair_deriv): the DST-II output is
+// z_q = Y_{N-1-q} of the DCT-II post-processing, the DCT-III input u_j = mul(j-1) z_{j-1}
+// = mul(j-1) Y_{N-j} (u_0 = 0), and the pre-processing of slot pair (k, M-k) reads
+// u_k, u_{N-k}, u_{M-k}, u_{M+k}: the Y at N-k, k, M+k, M-k that its post-processing yields.
+template <int N, int AX, class MUL>
+__device__ __forceinline__ void pair_derivt(const Grid& g, int lineA, PC* buf, const float2* post,
+                                            const float2* pre, int lp, int tj, const MUL& mul) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, NP = (M / 2) / TPL;
+  auto m = [&](int pos) -> float2 {
+    int i, j, k;
+    long long idx;
+    line_coords(g, AX, lineA, pos, i, j, k, idx);
+    return mul_ab<AX>(mul, i, j, k);
+  };
+#pragma unroll
+  for (int b = 0; b < NP; ++b) {
+    const int k = tj + b * TPL;
+    const PC zk = buf[k * PP + lp];
+    const PC zm = buf[((M - k) & (M - 1)) * PP + lp];
+    const PC u0 = pcomb(post[2 * k], zk, post[2 * k + 1], zm);
+    const int km = M - k;
+    const PC u1 = pcomb(post[2 * km], zm, post[2 * km + 1], zk);
+    // Y_k = u0.re, Y_{N-k} = -u0.im, Y_{M-k} = u1.re, Y_{M+k} = -u1.im (k = 0: Y_M = u1.re)
+    const float2 xk = (k > 0) ? mul2(m(k - 1), neg2(u0.im)) : f2(0.f);
+    const float2 xnk = (k > 0) ? mul2(m(N - k - 1), u0.re) : f2(0.f);
+    const float2 xmk = (k > 0) ? mul2(m(M - k - 1), neg2(u1.im)) : mul2(m(M - 1), u1.re);
+    const float2 xmpk = mul2(m(M + k - 1), u1.re);
+    PC z0, z1;
+    pair_pre_one(pre, M, k, xk, xnk, xmk, xmpk, z0, z1);
+    buf[k * PP + lp] = pswap(z0);
+    if (k > 0) buf[(M - k) * PP + lp] = pswap(z1);
+  }
+  if (tj == 0) {
+    const int k = M / 2;
+    const PC z = buf[k * PP + lp];
+    const PC u = pcomb(post[M], z, post[M + 1], z);
+    // u_{M/2} = mul(M/2-1) Y_{N-M/2} = mul(M/2-1) (-u.im), u_{N-M/2} = mul(N-M/2-1) Y_{M/2}
+    const float2 xk = mul2(m(k - 1), neg2(u.im)), xnk = mul2(m(N - k - 1), u.re);
+    const PC U = pmake(xk, neg2(xnk));
+    buf[k * PP + lp] = pswap(pcomb(pre[2 * k], U, pre[2 * k + 1], U));
+  }
+  __syncthreads();
+}
+
 // x/y forward kinds: post-processing with the outputs of both lines stored straight
 // to global memory.
 template <int N, int KIND, int AX, class ST>
@@ -551,8 +596,8 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   using Cf = PairCfg<N>;
   constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
   constexpr int R1 = Cf::R1;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
-  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
   constexpr bool xy = (AX != 2);
   constexpr int ZU = (LP * NQ) / NT;
   constexpr int ZC = (ZU >= 4) ? 4 : ZU;
@@ -568,12 +613,14 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   if constexpr (fwd_in) {
     pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
     if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R3, R1 * Cf::R2, TPL, PP>(buf, sfft, lp, tj);
-    if constexpr (xy && KIND != K_FILT && KIND != K_DERIV) {
+    if constexpr (xy && KIND != K_FILT && KIND != K_DERIV && KIND != K_DERIVT) {
       pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
       return;
     }
     if constexpr (KIND == K_DERIV) {
       pair_deriv<N, AX>(g, lineA, buf, spost, spre, lp, tj, mul);
+    } else if constexpr (KIND == K_DERIVT) {
+      pair_derivt<N, AX>(g, lineA, buf, spost, spre, lp, tj, mul);
     } else if constexpr (KIND == K_FILT) {
       pair_filt<N, AX>(g, lineA, buf, spost, spre, lp, tj, mul);
     } else {
@@ -650,8 +697,8 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_pair_kernel(Grid g, R2RTab
   using Cf = PairCfg<N>;
   constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
   constexpr int R1 = Cf::R1;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
-  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
   constexpr bool xy = (AX != 2);
   constexpr int ZU = (LP * NQ) / NT;  // z phases: (line pair, float4) units per thread
   constexpr int ZC = (ZU >= 4) ? 4 : ZU;
@@ -681,7 +728,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_pair_kernel(Grid g, R2RTab
       float2 a = ld_ab<AX>(g, ld, i, j, k, idx);
       xy_coords<AX>(g, lineA, p1, i, j, k, idx);
       float2 b = ld_ab<AX>(g, ld, i, j, k, idx);
-      if constexpr (KIND == K_S2) {
+      if constexpr (KIND == K_S2 || KIND == K_DERIVT) {
         if (p0 & 1) a = neg2(a);
         if (p1 & 1) b = neg2(b);
       }
@@ -744,7 +791,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_pair_kernel(Grid g, R2RTab
         const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
         float4 A = xa[c], B = xb[c];
         if constexpr (fwd_in) {
-          if constexpr (KIND == K_S2) {  // (-1)^p x_p
+          if constexpr (KIND == K_S2 || KIND == K_DERIVT) {  // (-1)^p x_p
             A.y = -A.y; A.w = -A.w;
             B.y = -B.y; B.w = -B.w;
           }

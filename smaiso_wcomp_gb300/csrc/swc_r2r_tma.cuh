@@ -112,8 +112,8 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   using Tc = TmaCfg<N>;
   constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
   constexpr int R1 = Cf::R1;
-  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV);
-  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV);
+  constexpr bool fwd_in = (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+  constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
   constexpr bool xy = (AX != 2);
   constexpr int ZU = (LP * NQ) / NT;
   extern __shared__ __align__(128) unsigned char tma_smem[];
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
         const int m = tj + r * TPL;
         const int p0 = mk_pos<N>(2 * m), p1 = mk_pos<N>(2 * m + 1);
         float2 a = S2[p0 * LP + lp], b = S2[p1 * LP + lp];
-        if constexpr (KIND == K_S2) {
+        if constexpr (KIND == K_S2 || KIND == K_DERIVT) {
           if (p0 & 1) a = neg2(a);
           if (p1 & 1) b = neg2(b);
         }
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
           const int u = tid + c * NT;
           const int a = u & (NQ - 1), q = u >> Cf::LOG2NQ;
           float4 A = S4[(2 * q) * NQ + a], B = S4[(2 * q + 1) * NQ + a];
-          if constexpr (KIND == K_S2) {
+          if constexpr (KIND == K_S2 || KIND == K_DERIVT) {
             A.y = -A.y; A.w = -A.w;
             B.y = -B.y; B.w = -B.w;
           }

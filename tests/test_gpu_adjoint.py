@@ -134,11 +134,14 @@ def test_binomial_cap_too_small_is_rejected(lib):
             e.backward(dpsi=np.ones((16, 16, 16)))
 
 
-def test_fp32_adjoint_of_the_mixed_engine(lib):
+@pytest.mark.parametrize("shape", [(32, 32, 32), (64, 64, 64)])
+def test_fp32_adjoint_of_the_mixed_engine(lib, shape):
     """The mixed engine's FP32 adjoint (same kernels, T = float, on the mixed trajectory)
     agrees with the FP64 adjoint of the FP64 engine to FP32 accuracy, and its binomial
-    schedule returns its fixed-interval gradients."""
-    shape, ds, nsteps = (32, 32, 32), 3, 10
+    schedule returns its fixed-interval gradients. 32-point lines run the runtime-length
+    passes, 64-point lines the TMA-fed FP32 passes (and the FP64 engine its fixed-length
+    ones), each with its own transposed derivative pass."""
+    ds, nsteps = 3, 10
     rng = np.random.default_rng(5)
     wp, wr = rng.standard_normal(shape), rng.standard_normal(shape)
     g = {}
