@@ -197,11 +197,12 @@ int swc_destroy(swc_ctx* ctx);
  * psi = iDCT(psiq), psiq_old = psiq, step counter = 0. */
 int swc_set_state(swc_ctx* ctx, const double* psi, const double* rho);
 
-/* Advance nsteps time steps (each one loop body :1084-2198). The last step of
- * the call also computes the diagnostics of :2202-2262 and the solenoidal
+/* Advance nsteps time steps (each one loop body :1084-2198). The diagnostics of
+ * :2202-2262 run at the last step of the call (swc_params.diag_interval = 0, the
+ * default) or at every diag_interval-th step; the last step also keeps the solenoidal
  * velocity. Steps run as captured CUDA graphs on the context's stream; the call
- * returns after the stream is idle. Returns SWC_ERR_NONFINITE if the state holds
- * NaN/Inf afterwards. */
+ * returns after the stream is idle. Returns SWC_ERR_NONFINITE if the call's last
+ * diagnostic step found NaN/Inf in psi or rho. */
 int swc_step(swc_ctx* ctx, int nsteps);
 
 /* Capture now the CUDA graphs of every step variant (relax / normal phase, first
@@ -227,7 +228,8 @@ int swc_diagnostics(swc_ctx* ctx, swc_diag* out);
 
 /* Copy one field (SWC_F_*) to host memory as nx*ny*nz doubles. Pinned (page-locked)
  * host memory gets a direct DMA copy; the mixed engine widens FP32 fields on the
- * device into a staging buffer it allocates on the first such call. */
+ * device into a staging buffer it allocates on the first such call. The energy
+ * density (SWC_F_ENERGY) exists after a diagnostic step only (else SWC_ERR_STATE). */
 int swc_get_field(swc_ctx* ctx, int field, double* dst);
 
 /* Asynchronous swc_get_field for a field read after every step (the loop's output,
@@ -237,7 +239,7 @@ int swc_get_field(swc_ctx* ctx, int field, double* dst);
  * follow. dst must stay valid until the copy completes, and must be pinned host memory
  * for the copy to run asynchronously. Two snapshot buffers (2 * nx*ny*nz doubles,
  * allocated on the first call) alternate: a call first waits for the copy issued two
- * calls before it, so when it returns the destination of the call before last holds
+ * calls before it, so when it returns the destination of that earlier call holds
  * its field; swc_get_field_wait completes every pending copy. Errors of a copy are
  * returned by the call that waits for it. */
 int swc_get_field_async(swc_ctx* ctx, int field, double* dst);
