@@ -6,15 +6,20 @@ reference's dt for 8 points per wavelength; dt = 0.01 diverges in the FP64 oracl
 at step 20). A step is one full time step (loop body of smaiso-wcomp.cpp:1084-2198).
 
   value        mixed-path steps/s with the state resident in HBM (graph launches,
-               CUDA events on the context's stream)
+               CUDA events on the context's stream), normal-phase steps: the 50-step
+               relax phase runs untimed first (its rate is reported on the side)
   e2e          the same metric through the C ABI with host buffers: swc_set_state
                from pinned host memory once, then per step swc_step_async(1) + the D2H
                read of that step's psi into pinned host memory
                (swc_get_field_async, overlapping the next step), all inside the
                timed region
+  accuracy     both engines 2000 steps from the initial state: the mixed engine's
+               psi / rho / mass / energy error against the FP64 engine
   roofline     the dominant kernel (the FP32 r2r axis pass, HBM-bound)
-  cpu_baseline the FP64 CPU oracle (restatement of the reference loop; the
-               reference itself needs FFTW3-MPI + MPI C++ bindings) on host cores
+  cpu_baseline the FP64 CPU oracle on host cores (restatement of the reference loop,
+               bit-identical to the reference's own code on the committed
+               reference-run fixtures; the reference binary needs FFTW3-MPI and
+               the MPI C++ bindings)
 
 Multi-GPU: the path does not shard in this build (one GPU, no collectives); N
 ranks run N independent replicas and value = N * steps / max-over-ranks time.
@@ -48,8 +53,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: steps/5, >= 10)")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--accuracy-steps", type=int, default=0,
-                    help="also run both engines this many steps from the initial state and report psi/rho error")
+    ap.add_argument("--accuracy-steps", type=int, default=2000,
+                    help="run both engines this many steps from the initial state and report the mixed "
+                         "engine's psi/rho/mass/energy error against the FP64 engine (0 skips it)")
     ap.add_argument("--grad-steps", type=int, default=40,
                     help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
     ap.add_argument("--workload", choices=["undulated", "dislocations", "adjoint128", "adjoint256", "adjoint256_fp64"],
@@ -140,17 +146,30 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def time_engine(p, psi, rho, warmup, steps):
-    """Device-timed steps of one engine: CUDA events on the context's stream."""
+def time_engine(p, psi, rho, warmup, steps, relax_steps=0):
+    """Device-timed steps of one engine: CUDA events on the context's stream.
+
+    The timed steps are normal-phase steps (the branch 97.5% of a 2000-step run takes):
+    the relax phase (the reference's first divv_switch = 50 steps, REF:1312-1380) is
+    run untimed first, then `warmup` untimed steps, then `steps` timed ones. With
+    relax_steps > 0, that many relax-phase steps (after 3 untimed ones) are timed on the
+    way and their ms/step returned as well."""
     from smaiso_wcomp_gb300.engine import Engine
     e = Engine(p)
     e.set_state(psi, rho)
     e.prepare()  # every step variant's graph (relax and normal phase) before the timed steps
+    relax_ms = None
+    if relax_steps > 0 and p.divv_switch >= relax_steps + 3:
+        e.step(3)
+        e.step(relax_steps)
+        relax_ms = e.last_step_ms() / relax_steps
+    if e.nloop < p.divv_switch:
+        e.step(p.divv_switch - e.nloop)
     e.step(warmup)
     e.step(steps)
     ms = e.last_step_ms()
     launches = e.last_step_launches()
-    return e, ms, launches
+    return e, ms, launches, relax_ms
 
 
 def time_e2e(p, psi_h, rho_h, steps):
@@ -160,11 +179,14 @@ def time_e2e(p, psi_h, rho_h, steps):
     n + 1), all inside the timed region, which ends when the last copy has landed and
     swc_sync has returned the steps' status. The value is the median of three timed
     runs of `steps` steps. The diagnostics run at the reference's cadence, every 50 steps
-    (diag_interval)."""
+    (diag_interval). divv_switch = 0: every timed step takes the normal-phase branch, as
+    the device-timed value's steps do (the relax phase would otherwise fill the first 50
+    steps after swc_set_state, which the timed region has to include)."""
     from smaiso_wcomp_gb300 import abi
     from smaiso_wcomp_gb300.engine import Engine
     p = abi.SwcParams.from_buffer_copy(p)
     p.diag_interval = 50
+    p.divv_switch = 0
     e = Engine(p)
     outs = [pinned((N, N, N)), pinned((N, N, N))]
 
@@ -446,33 +468,54 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(steps):
-    """FP64 CPU oracle on all host cores at the benchmark workload, `steps` steps."""
+def cpu_baseline(steps, warmup=0):
+    """FP64 CPU oracle on all host cores at the benchmark workload: `warmup` untimed and
+    `steps` timed normal-phase steps (divv_switch = 0, so the sample's steps take the
+    branch the GPU arm times; same state, same per-step work)."""
     from oracle import oracle as O
     from smaiso_wcomp_gb300 import abi
     cores = os.cpu_count() or 1
     O.set_threads(cores)
     p = make_params(abi.SWC_PREC_FP64)
+    p.divv_switch = 0
     psi, rho = initial_state(p)
     o = O.Oracle(p)
     o.set_state(psi, rho)
+    if warmup:
+        o.step(warmup)
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
     o.close()
     return {"value": steps / dt, "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} FP64 oracle steps of the 256^3 workload (relax phase), OpenMP {cores} threads"}
+            "sample": f"{steps} timed FP64 oracle steps (after {warmup} untimed) of the 256^3 workload, "
+                      f"normal phase, OpenMP {cores} threads (restatement of the reference loop, "
+                      f"bit-identical to it on the reference-run fixtures)"}
+
+
+# One oracle step of the 256^3 workload takes ~2.8 s on 16 Grace cores: the reference
+# arm runs the declared warm-up and timed steps when they fit in REF_ARM_MAX_STEPS
+# and otherwise the largest prefix that does, and prints the counts it ran.
+REF_ARM_MAX_STEPS = 30
+
+
+def config_of(world):
+    return {"workload": WORKLOAD, "grid": [N, N, N], "parallelism": f"replicas{world}",
+            "l2": f"inputs larger than L2 (working set {working_set_gb():.1f} GB > 129 MB L2)"}
 
 
 def run_reference(args, rank):
     if rank != 0:
         return
-    base = cpu_baseline(max(1, args.warmup + args.steps) if args.steps <= 3 else 3)
+    warmup = min(args.warmup, 3)
+    steps = max(1, min(args.steps, REF_ARM_MAX_STEPS - warmup))
+    base = cpu_baseline(steps, warmup)
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": "steps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
+            "requested": {"steps": args.steps, "warmup": args.warmup},
             "ms_per_step": 1e3 / base["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": [N, N, N]},
+            "config": config_of(args.gpus),
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -508,7 +551,7 @@ def main():
         return
     if args.only:
         prec = abi.SWC_PREC_MIXED if args.only == "mixed" else abi.SWC_PREC_FP64
-        e, ms, launches = time_engine(make_params(prec, device=local), psi, rho, args.warmup, args.steps)
+        e, ms, launches, _ = time_engine(make_params(prec, device=local), psi, rho, args.warmup, args.steps)
         print(json.dumps({"only": args.only, "steps": args.steps, "ms_per_step": ms / args.steps,
                           "steps_per_s": args.steps / (ms * 1e-3), "gpu_launches": launches}), flush=True)
         e.close()
@@ -519,26 +562,18 @@ def main():
         if pg:
             pg.barrier()
 
-    # mixed engine: the headline value
+    # mixed engine: the headline value (normal-phase steps; relax-phase rate on the side)
     barrier()
     with ClockSampler(local) as clk:
-        e_mix, ms_mix, launches = time_engine(p_mix, psi, rho, max(args.warmup, 3), args.steps)
+        e_mix, ms_mix, launches, relax_ms_mix = time_engine(p_mix, psi, rho, max(args.warmup, 3), args.steps,
+                                                            relax_steps=20)
     barrier()
     clocks = clk.summary()
-    # FP64 engine on the same state
+    e_mix.close()
+    # FP64 engine on the same state, normal phase as well
     k64 = args.fp64_steps or max(10, args.steps // 5)
     p64 = make_params(abi.SWC_PREC_FP64, device=local)
-    e_64, ms_64, _ = time_engine(p64, psi, rho, max(args.warmup, 3), k64)
-    # accuracy of mixed vs FP64 after the same number of steps
-    nsteps_mix, nsteps_64 = e_mix.nloop, e_64.nloop
-    if nsteps_64 < nsteps_mix:
-        e_64.step(nsteps_mix - nsteps_64)
-    elif nsteps_64 > nsteps_mix:
-        e_mix.step(nsteps_64 - nsteps_mix)
-    a, b = e_mix.field("psi"), e_64.field("psi")
-    psi_err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    rho_err = float(np.linalg.norm(e_mix.field("rho") - e_64.field("rho")) / np.linalg.norm(e_64.field("rho")))
-    e_mix.close()
+    e_64, ms_64, _, relax_ms_64 = time_engine(p64, psi, rho, max(args.warmup, 3), k64, relax_steps=10)
     e_64.close()
 
     # max over ranks of the device time (replicas: no data-path collective)
@@ -546,6 +581,9 @@ def main():
     ms_mix, ms_64 = replicas.max_over_ranks([ms_mix, ms_64], pg, device="cuda")
     sps_mix = replicas.job_throughput(args.steps, ms_mix * 1e-3, 1)
     sps_64 = replicas.job_throughput(k64, ms_64 * 1e-3, 1)
+    # accuracy: both engines from the initial state through the relax phase and on
+    # (spec bar: psi within 1e-5 of the FP64 engine after 2000 steps)
+    acc = accuracy_run(args.accuracy_steps, local) if args.accuracy_steps > 0 else None
 
     psi_h = pinned((N, N, N))
     rho_h = pinned((N, N, N))
@@ -570,12 +608,16 @@ def main():
         "metric": METRIC, "value": sps_mix * world, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mix / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": [N, N, N], "parallelism": f"replicas{world}",
-                   "l2": f"inputs larger than L2 (working set {working_set_gb():.1f} GB > 129 MB L2)"},
+        "config": config_of(world),
+        "phase": "normal (steps after the 50-step relax phase)",
+        "relax_phase_steps_per_s": 1e3 / relax_ms_mix if relax_ms_mix else None,
         "fp64_steps_per_s": sps_64 * world, "mixed_over_fp64": sps_mix / sps_64,
+        "fp64_relax_phase_steps_per_s": 1e3 / relax_ms_64 if relax_ms_64 else None,
         "grid_point_steps_per_s": sps_mix * world * N ** 3,
-        "psi_rel_l2_mixed_vs_fp64": psi_err, "rho_rel_l2_mixed_vs_fp64": rho_err,
-        "accuracy_steps": max(nsteps_mix, nsteps_64),
+        "psi_rel_l2_mixed_vs_fp64": acc["psi_rel_l2"] if acc else None,
+        "rho_rel_l2_mixed_vs_fp64": acc["rho_rel_l2"] if acc else None,
+        "accuracy_steps": acc["steps"] if acc else 0,
+        "accuracy": acc,
         "gradient_forward_ratio": None,  # filled below
         "e2e": {"value": e2e_sps * world, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roofline,
@@ -591,10 +633,11 @@ def main():
         gr = gradient_forward_ratio(args.grad_steps)
         line["gradient_forward_ratio"] = gr["value"]
         line["gradient"] = gr
-    if args.accuracy_steps > 0:
-        line["accuracy"] = accuracy_run(args.accuracy_steps, local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_sample_steps)
+        # matched precision: the FP64 GPU engine over the FP64 CPU oracle
+        line["fp64_gpu_over_cpu"] = sps_64 / line["cpu_baseline"]["value"]
+        line["mixed_gpu_over_cpu"] = sps_mix / line["cpu_baseline"]["value"]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg:

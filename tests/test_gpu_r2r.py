@@ -76,6 +76,18 @@ def test_round_trip_256(lib, prec):
         assert err <= (1e-14 if prec == abi.SWC_PREC_FP64 else 2e-6), err
 
 
+@pytest.mark.parametrize("plan", ["CT", "iCT", "STx", "iSTy", "STz", "iSTz"])
+def test_fp64_plan_256_against_oracle(lib, oracle_mod, plan):
+    """FP64 plans at the benchmark size (compile-time 256-point passes on every axis)
+    against the oracle's transform of the same array, element by element."""
+    n = 256
+    x = np.random.default_rng(31).standard_normal((n, n, n))
+    ref = oracle_mod.r2r3d(x, PLANS[plan])
+    got = R2RPlan(x.shape, PLANS[plan], abi.SWC_PREC_FP64, lib=lib)(x)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-14
+    assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
 def test_execute_on_device_buffer(lib):
     """swc_r2r_execute on caller-owned device memory (the in-place fftw_execute analogue)."""
     torch = pytest.importorskip("torch")

@@ -65,6 +65,38 @@ def test_fp64_step_parity(lib, oracle_mod, shape, kw, gen, schedule):
     assert de["step"] == do["step"] == sum(schedule)
 
 
+# Every compile-time FP64 line length (64, 128, 256, 512) on every axis: the first
+# pass of a 3D transform runs along z (where the fused loaders LdAmp, LdLpsi,
+# LdRelaxLap, LdRhoL, LdNl sit), the last along x (StNlUpdate), and the derivative
+# passes (LdOffset on rho) along each axis in turn.
+PRODUCTION_SHAPES = [(128, 64, 64), (256, 32, 32), (32, 256, 32), (32, 32, 256), (512, 16, 16),
+                     (16, 512, 16), (16, 16, 512), (32, 128, 128)]
+
+
+@pytest.mark.parametrize("shape", PRODUCTION_SHAPES)
+def test_fp64_production_lengths(lib, oracle_mod, shape):
+    """FP64 engine against the oracle where its compile-time passes and fused
+    loaders/stores run: relax steps 1-2 and normal steps 3-4 (divv_switch = 2), all
+    24 fields and the diagnostics to the FP64 parity bar."""
+    p = abi.default_params(*shape, rho_0=0.8, divv_switch=2)
+    psi, rho = ic.undulated_interface(p)
+    o, e = run_pair(oracle_mod, p, psi, rho, [1, 3])
+    errs = {f: rel(e.field(f), o.field(f)) for f in FIELDS}
+    vectors = {"gpsi": ["gpsix", "gpsiy", "gpsiz"], "grho": ["grhox", "grhoy", "grhoz"],
+               "v": ["vx", "vy", "vz", "vsolx", "vsoly", "vsolz"]}
+    for comps in vectors.values():
+        scale = np.sqrt(sum(np.linalg.norm(o.field(c)) ** 2 for c in comps[:3]))
+        for c in comps:
+            errs[c] = np.linalg.norm(e.field(c) - o.field(c)) / max(scale, 1e-300)
+    bad = {f: v for f, v in errs.items() if not v <= FP64_TOL}
+    assert not bad, bad
+    do, de = o.diagnostics(), e.diagnostics()
+    for k in ("l1", "mass", "energy"):
+        assert abs(de[k] - do[k]) <= FP64_TOL * abs(do[k]), (k, de[k], do[k])
+    e.close()
+    o.close()
+
+
 @pytest.mark.parametrize("shape,nsteps", [((32, 32, 32), 60), ((64, 64, 64), 30), ((128, 64, 64), 16)])
 def test_mixed_step_accuracy(lib, oracle_mod, shape, nsteps):
     """Mixed engine against the FP64 oracle; 64 and 128 point lines run the FP32
