@@ -66,6 +66,8 @@ def parse():
                     help="adjoint workloads: steps instead of the configuration's (short profiling runs)")
     ap.add_argument("--fd-mixed", action="store_true",
                     help="adjoint256: also 4th-order finite differences of the mixed forward (40 forward runs)")
+    ap.add_argument("--energy-lambda", type=float, default=1.0,
+                    help="adjoint workloads: weight of the free-energy diagnostic E(T) in the calibration loss")
     ap.add_argument("--divv-switch", type=int, default=None,
                     help="adjoint workloads: relax-phase length instead of the reference's 50")
     ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
@@ -291,18 +293,18 @@ def gradient_forward_ratio(steps, ckpt=20, n=128):
 CAL_COEFFS = ("alpha", "beta", "gamma", "nu", "rho_0")
 
 
-def calibration_adjoint(which, steps=None, divv_switch=None, fd_mixed=False):
+def calibration_adjoint(which, steps=None, divv_switch=None, fd_mixed=False, lam=1.0):
     """The calibration-adjoint configurations: adjoint128 -- FP64 forward + FP64 adjoint,
     128^3, 400 steps, checkpoints every 20 steps; adjoint256 -- mixed forward + FP32
     adjoint, 256^3, 2000 steps, binomial checkpoint/recompute under a 40 GB device-memory
     cap (adjoint256_fp64: the same with the FP64 engine). Undulated
     interface, density ratio 0.8. psi_target comes from a run whose five coefficients are
-    scaled by 1 + U(-0.1, 0.1) (seeded); loss L = ||psi(T) - psi_target||^2 (the
-    interface free-energy term of the configuration is left out: lambda = 0). Reports the
-    gradient/forward wall-time ratio, the gradient and, for adjoint128, its error against
-    central finite differences of the FP64 forward (h = 1e-6 relative). steps and
-    divv_switch override the configuration's step count and relax-phase length (short
-    profiling runs)."""
+    scaled by 1 + U(-0.1, 0.1) (seeded); loss L = ||psi(T) - psi_target||^2 + lam E(T),
+    E(T) the free-energy diagnostic of the last step (REF:2214-2258; lam = 1 by default),
+    differentiated by swc_backward_energy. Reports the gradient/forward wall-time ratio,
+    the gradient and, for adjoint128, its error against central finite differences of the
+    FP64 forward (h = 1e-6 relative, and 4th order). steps and divv_switch override the
+    configuration's step count and relax-phase length (short profiling runs)."""
     from smaiso_wcomp_gb300 import abi, ic
     from smaiso_wcomp_gb300.engine import Engine
     n, nsteps = (128, 400) if which == "adjoint128" else (256, 2000)
@@ -327,7 +329,7 @@ def calibration_adjoint(which, steps=None, divv_switch=None, fd_mixed=False):
             e.set_state(psi0, rho0)
             e.step(steps)
             d = e.field("psi") - psi_t
-            return float(np.sum(d * d))
+            return float(np.sum(d * d)) + lam * e.diagnostics()["energy"]
 
     p = abi.default_params(n, rho_0=0.8, **mode, **dv)
     with Engine(p) as e:
@@ -338,15 +340,18 @@ def calibration_adjoint(which, steps=None, divv_switch=None, fd_mixed=False):
         t0 = time.perf_counter()
         e.step(steps)
         psi_T = e.field("psi")
+        energy_T = e.diagnostics()["energy"]   # E(T): the diagnostics of the call's last step
         t1 = time.perf_counter()
-        g = e.backward(dpsi=2.0 * (psi_T - psi_t), want_psi0=True)
+        g = e.backward(dpsi=2.0 * (psi_T - psi_t), want_psi0=True, energy_lambda=lam)
         t2 = time.perf_counter()
+    misfit = float(np.sum((psi_T - psi_t) ** 2))
     res = {"workload": f"calibration adjoint {n}^3, {steps} steps"
                        + ("" if divv_switch is None else f" (relax phase {divv_switch} steps)") + ", "
                        + ("mixed forward + FP32 adjoint, " if prec == abi.SWC_PREC_MIXED else
                           "FP64 forward + FP64 adjoint, ")
                        + ("checkpoints every 20 steps" if which == "adjoint128" else
                           "binomial checkpoint/recompute under a 40 GB cap"),
+           "loss": {"lambda": lam, "misfit": misfit, "energy": energy_T, "total": misfit + lam * energy_T},
            "gradient_forward_ratio": (t2 - t1) / (t1 - t0), "forward_s": t1 - t0, "backward_s": t2 - t1,
            "forward_steps_rerun": g["forward_steps"], "snapshots": g["snapshots"],
            "adjoint_step_over_forward_step": ((t2 - t1) - g["forward_steps"] * (t1 - t0) / steps) / (t1 - t0),
@@ -391,7 +396,7 @@ def calibration_adjoint(which, steps=None, divv_switch=None, fd_mixed=False):
                 e.set_state(psi0 + x * d, rho0)
                 e.step(steps)
                 r = e.field("psi") - psi_t
-                return float(np.sum(r * r))
+                return float(np.sum(r * r)) + lam * e.diagnostics()["energy"]
             fd_psi = (fpsi(1e-6) - fpsi(-1e-6)) / 2e-6
             # 4th-order differences at two steps: their truncation error falls as h^4,
             # their roundoff (~1e-13 |L| / h) grows as 1/h
@@ -538,8 +543,8 @@ def main():
     p_mix = make_params(abi.SWC_PREC_MIXED, device=local)
     psi, rho = initial_state(p_mix)
     if args.workload in ("adjoint128", "adjoint256", "adjoint256_fp64"):
-        print(json.dumps(calibration_adjoint(args.workload, args.adjoint_steps, args.divv_switch, args.fd_mixed)),
-              flush=True)
+        print(json.dumps(calibration_adjoint(args.workload, args.adjoint_steps, args.divv_switch, args.fd_mixed,
+                                             args.energy_lambda)), flush=True)
         return
     if args.workload == "dislocations":
         print(json.dumps(dislocation_run(args.steps, args.warmup, args.accuracy_steps or 50, local)), flush=True)

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define SWC_ABI_VERSION 3
+#define SWC_ABI_VERSION 4
 
 /* ---- status codes ---------------------------------------------------------- */
 enum {
@@ -269,10 +269,12 @@ int swc_device_fma_peak(int precision, double* tflops);
 /* Allocation-free variant of the diagnostic reduction. No counterpart in the
  * reference (its sums are plain loops, REF:2214-2231); same arithmetic as the
  * reduction behind swc_diagnostics, applied to caller-owned FP64 device fields of
- * nx*ny*nz doubles: psi (new), psi_old, rho, lpsi (dfDlapPsi) and amp. Geometry and
- * coefficients come from *p (only dt, nw, q0, ep, beta, gamma, zeta and rho_0 are read
- * besides the grid). Result in *out (step = -1); the call returns after `stream` (a
- * cudaStream_t, NULL = legacy default stream) has finished the reduction.
+ * nx*ny*nz doubles: psi (new), psi_old, rho, lpsi (dfDlapPsi) and amp, all on device
+ * p->device. Geometry and coefficients come from *p (only dt, nw, q0, ep, beta, gamma,
+ * zeta, rho_0 and device are read besides the grid). The call makes p->device current
+ * while it runs and restores the caller's current device before it returns; `stream`
+ * (a cudaStream_t, NULL = legacy default stream) must belong to that device. Result in
+ * *out (step = -1); the call returns after the stream has finished the reduction.
  *
  * For callers that must not allocate device memory at this point: a host code that
  * gave this library a fixed device budget and lets its own allocator own the rest, a
@@ -283,14 +285,64 @@ int swc_device_fma_peak(int precision, double* tflops);
  * the process exits. Limits and rules:
  *   - at most SWC_NOALLOC_MAX_POINTS grid points (SWC_ERR_BAD_PARAM beyond);
  *   - the first call on a device looks up the array's device address (set-up, once
- *     per device, for the current device): make that first call before any stream
- *     capture;
+ *     per device, with the device current; again after the device's context changed,
+ *     e.g. after a cudaDeviceReset): make that first call before any stream capture;
  *   - every call shares the one array per device: calls that overlap on the GPU (on
  *     different streams or threads) race. Each call writes every scratch slot it
  *     reads, so no clearing is needed between calls. */
 #define SWC_NOALLOC_MAX_POINTS (1LL << 28)
 int swc_diagnostics_noalloc(const swc_params* p, const double* psi, const double* psi_old, const double* rho,
                             const double* lpsi, const double* amp, void* stream, swc_diag* out);
+
+/* ---- initial conditions generated on the device (replaces smaiso-wcomp.cpp:556-722) */
+enum {
+  SWC_IC_BAND = 0,         /* REF:575-590: psi = Amp cos(q0 k dz) written at k2 = k + round(phi
+                              sin(Qi i dx)) for Nz/2-8 < k < Nz/2+8, 0 elsewhere; rho = 0 */
+  SWC_IC_FLAT = 1,         /* flat smectic/isotropic interface at Lz/2, layers parallel to it:
+                              psi = h(z) A cos(q0 z) + U(-noise, noise), h = (1 + tanh((z - Lz/2)/xi))/2;
+                              rho = rho_i + (rho_s - rho_i) h */
+  SWC_IC_UNDULATED = 2,    /* the same with the interface at z0(x,y) = Lz/2 + 2 (2 pi/q0)
+                              sin(2 pi x/Lx) cos(2 pi y/Ly) and Gaussian psi noise of sigma = noise;
+                              rho = rho_i + (rho_s - rho_i) h */
+  SWC_IC_DISLOCATIONS = 3, /* psi = h A cos(q0 z + sum_c atan2(z - z_c, x - x_c)): ncores edge
+                              dislocations at seeded (x_c, z_c) below a flat interface at 3Lz/4,
+                              h = (1 - tanh((z - 3Lz/4)/xi))/2; rho = rho_0 + (1 - rho_0) h */
+  SWC_IC_FOCAL_CONIC = 4,  /* REF:594-639 (commented out in the reference): one focal conic of
+                              size aE = bE = ae at the bottom of the box; rho = 0 */
+  SWC_IC_FOCAL_CONICS = 5  /* REF:641-707 (commented out): two focal conics side by side along
+                              x, the second of size ae + gap; rho = 0 */
+};
+
+/* Parameters of a device initial condition (swc_default_ic fills the defaults of a kind).
+ * Noise and seeded positions come from SplitMix64(seed XOR linear index): uniform
+ * U[0,1) = top 53 bits; Gaussian by Box-Muller on the index pair (2m, 2m+1). */
+typedef struct swc_ic {
+  int kind;         /* SWC_IC_* */
+  int ncores;       /* DISLOCATIONS: number of cores */
+  uint64_t seed;
+  double amp;       /* IC amplitude A; <= 0: the model's Amp (REF:250), as BAND and the focal
+                       conics use */
+  double xi;        /* interface width */
+  double noise;     /* FLAT: uniform half-width; UNDULATED: Gaussian sigma */
+  double rho_s, rho_i;  /* FLAT, UNDULATED: densities of the smectic and isotropic sides */
+  double phi, qi;   /* BAND: layer perturbation amplitude and wavenumber (REF:282-283, 584) */
+  double ae, gap;   /* FOCAL_CONIC(S): size aE = bE (reference argv[3], REF:230-231) and the
+                       second conic's extra size (REF:227) */
+} swc_ic;
+
+/* Defaults of an initial condition of `kind` for the grid of *p (the values of the
+ * benchmark workloads for FLAT, UNDULATED and DISLOCATIONS; the reference's for BAND;
+ * ae = 3 nz/8 for the focal conics). */
+int swc_default_ic(const swc_params* p, int kind, swc_ic* ic);
+
+/* Write the initial psi and rho (nx*ny*nz doubles each, (i,j,k) layout) of *ic into
+ * caller-owned device memory (rho may be NULL), enqueued on `stream` (a cudaStream_t,
+ * NULL = legacy default stream), on the current device. Allocates nothing. */
+int swc_ic_generate(const swc_params* p, const swc_ic* ic, double* dev_psi, double* dev_rho, void* stream);
+
+/* swc_set_state with the initial state generated on the device (no host arrays):
+ * psi and rho of *ic, then the pre-loop (:968-1010). */
+int swc_set_state_ic(swc_ctx* ctx, const swc_ic* ic);
 
 /* ---- discrete adjoint of the time loop ------------------------------------
  * No counterpart in the reference. Differentiates L(psi(T), rho(T)) after the
@@ -307,6 +359,18 @@ int swc_diagnostics_noalloc(const swc_params* p, const double* psi, const double
  * and their status returned first (as swc_sync). */
 int swc_backward(swc_ctx* ctx, const double* dL_dpsi, const double* dL_drho, double* dL_dpsi0,
                  double* dL_drho0, swc_grad* grad);
+
+/* swc_backward for a loss with the free-energy diagnostic of the last step added:
+ * L = L_user(psi(T), rho(T)) + lambda * E(T), E(T) the energy of REF:2214-2258 at step
+ * T = nLoop: dx^3 sum [rho (-ep/2 psi^2 + (dfDlapPsi)^2/2 - beta/4 psi^4 + gamma/6 psi^6)
+ * + zeta/2 (rho - rho_0 - kp A)^2] with the new psi and rho of step T and the stale
+ * dfDlapPsi (REF:2227) and the filtered amplitude A computed during step T (the value
+ * swc_diagnostics reports for step T). dL_dpsi / dL_drho are the cotangents of L_user
+ * (either may be NULL); lambda = 0 is swc_backward. The coefficient gradients include
+ * E's direct dependence on beta, gamma, rho_0 and, through Amp and kp, on beta, gamma
+ * and rho_0 (REF:250-253). No counterpart in the reference. */
+int swc_backward_energy(swc_ctx* ctx, double lambda, const double* dL_dpsi, const double* dL_drho,
+                        double* dL_dpsi0, double* dL_drho0, swc_grad* grad);
 
 /* ---- full-state checkpoint (lossless; the reference's psi<rank>.dat text dump
  *      at :2334-2345 keeps only psi at 6 digits) ------------------------------ */

@@ -49,12 +49,21 @@ def lib():
         L.swco_r2r1d.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int]
         L.swco_r2r3d.argtypes = [ctypes.c_int] * 6 + [dp, dp, ctypes.c_int]
         L.swco_set_threads.argtypes = [ctypes.c_int]
+        L.swco_reference_ic.argtypes = [P(SwcParams), ctypes.c_int] + [ctypes.c_double] * 5 + [dp]
         _lib = L
     return _lib
 
 
 def set_threads(n):
     return lib().swco_set_threads(int(n))
+
+
+def reference_ic(p, kind, amp=0.0, phi=0.0, qi=0.0625, ae=0.0, gap=0.0):
+    """psi of the reference's band (REF:575-590) and focal-conic (REF:594-707) states."""
+    out = np.empty((p.nx, p.ny, p.nz))
+    rc = lib().swco_reference_ic(ctypes.byref(p), int(kind), amp, phi, qi, ae, gap, as_dptr(out))
+    assert rc == SWC_OK, rc
+    return out
 
 
 def r2r1d(x, kind, direct=False):

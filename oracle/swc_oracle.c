@@ -705,3 +705,63 @@ int swco_set_threads(int n) {
   return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------- */
+/* Initial states of the reference's new-state branch (REF:556-707)           */
+/* ------------------------------------------------------------------------- */
+
+/* psi of the reference's initial conditions on one global domain, restated from its
+ * loops: SWC_IC_BAND -- the live "perturbed smectic" band (REF:575-590: Amp
+ * cos(q0 k dz) written at k2 = k + round(phi sin(Qi i dx)) for Nz/2-8 < k < Nz/2+8);
+ * SWC_IC_FOCAL_CONIC -- the single focal conic (REF:594-639); SWC_IC_FOCAL_CONICS --
+ * two focal conics along x (REF:641-707), the second with aE2 = bE2 = aE + gap. The
+ * focal-conic loops are commented out in the reference; aE = bE = argv[3]
+ * (REF:230-231), mid = Ny/2 (REF:222). amp <= 0 selects the model's Amp (REF:250).
+ * Band writes that would land outside [0, Nz) are dropped (the reference would write
+ * past its slab). */
+int swco_reference_ic(const swc_params* p, int kind, double amp, double phi, double qi, double ae, double gap,
+                      double* psi) {
+  if (!p || !psi) return SWC_ERR_BAD_PARAM;
+  const int Nx = p->nx, Ny = p->ny, Nz = p->nz;
+  const double Amp = amp > 0 ? amp : sqrt((3 * p->beta + sqrt(9 * p->beta * p->beta + 40 * p->ep * p->gamma)) / 5);
+  const double dx = (Nx * 2.0 * M_PI / (p->q0 * p->nw)) / Nx;
+  const double dz = (Nz * 2.0 * M_PI / (p->q0 * p->nw)) / Nz;
+  const double q0 = p->q0;
+  const double mid = Ny / 2;
+  memset(psi, 0, sizeof(double) * (size_t)Nx * Ny * Nz);
+  for (int i = 0; i < Nx; ++i)
+    for (int j = 0; j < Ny; ++j)
+      for (int k = 0; k < Nz; ++k) {
+        const long index = ((long)i * Ny + j) * Nz + k;
+        if (kind == SWC_IC_BAND) {
+          if ((k > Nz / 2 - 8) && (k < Nz / 2 + 8)) {
+            const int k2 = k + (int)round(phi * sin(qi * i * dx));
+            if (k2 >= 0 && k2 < Nz) psi[((long)i * Ny + j) * Nz + k2] = Amp * cos(q0 * k * dz);
+          }
+          continue;
+        }
+        if (kind != SWC_IC_FOCAL_CONIC && kind != SWC_IC_FOCAL_CONICS) return SWC_ERR_BAD_PARAM;
+        int i2 = i, j2 = j;
+        double aE2 = ae, bE2 = ae, mid_translate = 0;
+        if (kind == SWC_IC_FOCAL_CONICS && i >= Nx / 2) {
+          i2 = i - Nx / 2;
+          aE2 = ae + gap;
+          bE2 = ae + gap;
+        }
+        if (k < bE2 + 1) {
+          const double xs = i2 - mid + mid_translate, ys = j2 - mid, zs = k;
+          const double ds = sqrt(xs * xs + ys * ys);
+          if (ds < mid) {
+            if (sqrt(pow((ds - mid) / aE2, 2) + pow(zs / bE2, 2)) > 1)
+              psi[index] = 0.0;
+            else
+              psi[index] = Amp * cos(q0 * dz * sqrt(pow((bE2 / aE2) * (ds - mid), 2) + zs * zs));
+          } else {
+            psi[index] = (fabs(zs) < bE2) ? Amp * cos(q0 * zs * dz) : 0.0;
+          }
+        } else {
+          psi[index] = 0.0;
+        }
+      }
+  return SWC_OK;
+}

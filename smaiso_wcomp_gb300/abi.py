@@ -27,6 +27,9 @@ SWC_PREC_MIXED = 1
 
 SWC_REDFT10, SWC_REDFT01, SWC_RODFT10, SWC_RODFT01 = 0, 1, 2, 3
 
+# device initial conditions (swc_ic.kind)
+SWC_IC_BAND, SWC_IC_FLAT, SWC_IC_UNDULATED, SWC_IC_DISLOCATIONS, SWC_IC_FOCAL_CONIC, SWC_IC_FOCAL_CONICS = range(6)
+
 FIELDS = [
     "psi", "rho", "amp", "divv", "vx", "vy", "vz", "vsolx", "vsoly", "vsolz", "energy",
     "psiq", "psiq_old", "nlq", "frho", "lpsi", "mu", "gpsix", "gpsiy", "gpsiz",
@@ -37,12 +40,13 @@ FIELD_ID = {name: i for i, name in enumerate(FIELDS)}
 # Every symbol include/swc.h declares (checked by the CPU test suite).
 EXPORTS = [
     "swc_abi_version", "swc_strerror", "swc_last_error", "swc_default_params", "swc_derive",
-    "swc_create", "swc_destroy", "swc_set_state", "swc_step", "swc_step_async", "swc_sync",
+    "swc_create", "swc_destroy", "swc_set_state", "swc_set_state_ic", "swc_default_ic", "swc_ic_generate",
+    "swc_step", "swc_step_async", "swc_sync",
     "swc_prepare", "swc_diagnostics",
     "swc_get_field", "swc_get_field_async", "swc_get_field_wait", "swc_field_device_ptr", "swc_get_step",
     "swc_last_step_ms",
     "swc_last_step_launches", "swc_device_fma_peak", "swc_diagnostics_noalloc",
-    "swc_backward", "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
+    "swc_backward", "swc_backward_energy", "swc_save", "swc_load", "swc_r2r_plan_create", "swc_r2r_plan_destroy",
     "swc_r2r_execute", "swc_r2r_execute_axis", "swc_r2r_execute_host", "swc_r2r_plan_set_wait_test",
 ]
 
@@ -57,6 +61,15 @@ class SwcParams(ctypes.Structure):
         ("ref_ranks", ctypes.c_int), ("precision", ctypes.c_int), ("device", ctypes.c_int),
         ("watchdog_s", ctypes.c_double), ("adjoint_ckpt", ctypes.c_int), ("adjoint_cap_gb", ctypes.c_double),
         ("adjoint_snapshots", ctypes.c_int), ("diag_interval", ctypes.c_int),
+    ]
+
+
+class SwcIc(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int), ("ncores", ctypes.c_int), ("seed", ctypes.c_uint64),
+        ("amp", ctypes.c_double), ("xi", ctypes.c_double), ("noise", ctypes.c_double),
+        ("rho_s", ctypes.c_double), ("rho_i", ctypes.c_double), ("phi", ctypes.c_double),
+        ("qi", ctypes.c_double), ("ae", ctypes.c_double), ("gap", ctypes.c_double),
     ]
 
 
@@ -140,6 +153,9 @@ def load_library(path=None):
         "swc_create": (ctypes.c_int, [P(SwcParams), P(vp)]),
         "swc_destroy": (ctypes.c_int, [vp]),
         "swc_set_state": (ctypes.c_int, [vp, dp, dp]),
+        "swc_set_state_ic": (ctypes.c_int, [vp, P(SwcIc)]),
+        "swc_default_ic": (ctypes.c_int, [P(SwcParams), ctypes.c_int, P(SwcIc)]),
+        "swc_ic_generate": (ctypes.c_int, [P(SwcParams), P(SwcIc), vp, vp, vp]),
         "swc_step": (ctypes.c_int, [vp, ctypes.c_int]),
         "swc_diagnostics": (ctypes.c_int, [vp, P(SwcDiag)]),
         "swc_get_field": (ctypes.c_int, [vp, ctypes.c_int, dp]),
@@ -155,6 +171,7 @@ def load_library(path=None):
         "swc_device_fma_peak": (ctypes.c_int, [ctypes.c_int, dp]),
         "swc_diagnostics_noalloc": (ctypes.c_int, [P(SwcParams), vp, vp, vp, vp, vp, vp, P(SwcDiag)]),
         "swc_backward": (ctypes.c_int, [vp, dp, dp, dp, dp, P(SwcGrad)]),
+        "swc_backward_energy": (ctypes.c_int, [vp, ctypes.c_double, dp, dp, dp, dp, P(SwcGrad)]),
         "swc_save": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "swc_load": (ctypes.c_int, [vp, ctypes.c_char_p]),
         "swc_r2r_plan_create": (ctypes.c_int, [ctypes.c_int] * 7 + [P(vp)]),

@@ -14,7 +14,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 SOURCES = ["swc_abi.cu", "swc_plan.cu", "swc_step_fp64.cu", "swc_step_fp64_b.cu", "swc_step_fp64_c.cu",
            "swc_step_mixed.cu", "swc_step_mixed_b.cu", "swc_step_mixed_c.cu", "swc_step_mixed_adj.cu",
-           "swc_noalloc.cu"]
+           "swc_noalloc.cu", "swc_ic.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

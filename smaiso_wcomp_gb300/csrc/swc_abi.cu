@@ -242,6 +242,13 @@ int swc_set_state(swc_ctx* ctx, const double* psi, const double* rho) {
   SWC_GUARD(ctx->eng->set_state(psi, rho));
 }
 
+int swc_set_state_ic(swc_ctx* ctx, const swc_ic* ic) {
+  SWC_NEED_CTX(ctx);
+  const int rc = swc::ic_check(ic);
+  if (rc) return rc;
+  SWC_GUARD(ctx->eng->set_state_ic(*ic));
+}
+
 int swc_step(swc_ctx* ctx, int nsteps) {
   SWC_NEED_CTX(ctx);
   SWC_GUARD(ctx->eng->step(nsteps));
@@ -321,7 +328,15 @@ int swc_backward(swc_ctx* ctx, const double* dL_dpsi, const double* dL_drho, dou
                  swc_grad* grad) {
   SWC_NEED_CTX(ctx);
   if (!grad) { set_error("grad is NULL"); return SWC_ERR_BAD_PARAM; }
-  SWC_GUARD(ctx->eng->backward(dL_dpsi, dL_drho, dL_dpsi0, dL_drho0, grad));
+  SWC_GUARD(ctx->eng->backward(dL_dpsi, dL_drho, 0.0, dL_dpsi0, dL_drho0, grad));
+}
+
+int swc_backward_energy(swc_ctx* ctx, double lambda, const double* dL_dpsi, const double* dL_drho,
+                        double* dL_dpsi0, double* dL_drho0, swc_grad* grad) {
+  SWC_NEED_CTX(ctx);
+  if (!grad) { set_error("grad is NULL"); return SWC_ERR_BAD_PARAM; }
+  if (!std::isfinite(lambda)) { set_error("lambda is not finite"); return SWC_ERR_BAD_PARAM; }
+  SWC_GUARD(ctx->eng->backward(dL_dpsi, dL_drho, lambda, dL_dpsi0, dL_drho0, grad));
 }
 
 int swc_save(swc_ctx* ctx, const char* path) {

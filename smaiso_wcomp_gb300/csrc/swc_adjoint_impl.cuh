@@ -31,7 +31,9 @@ static_assert(kTape <= 32, "tape_alias_ holds one pointer per tape field");
 enum {
   AJ_Q = 0, AJ_QO, AJ_NLO, AJ_R, AJ_F, AJ_NL, AJ_FX, AJ_FY, AJ_FZ, AJ_MU, AJ_A, AJ_PSI, AJ_VX, AJ_VY, AJ_VZ,
   AJ_GPX, AJ_GPY, AJ_GPZ, AJ_GRX, AJ_GRY, AJ_GRZ, AJ_DIVV, AJ_DOTX, AJ_DOTY, AJ_DOTZ, AJ_SDX, AJ_SDY, AJ_SDZ,
-  AJ_FGPX, AJ_FGPY, AJ_FGPZ, AJ_SX, AJ_SY, AJ_SZ, AJ_FG, AJ_E, AJ_LAPR, AJ_L, kAdj
+  AJ_FGPX, AJ_FGPY, AJ_FGPZ, AJ_SX, AJ_SY, AJ_SZ, AJ_FG, AJ_E, AJ_LAPR, AJ_L,
+  AJ_KEEPL, AJ_KEEPA,  // the final step's L and A, put back when swc_backward returns
+  kAdj
 };
 
 // Fields the one-step tape of the binomial schedule copies (the others are read in
@@ -63,7 +65,7 @@ template <typename T> int StepEngine<T>::adjoint_alloc(size_t tape_fields) {
 }
 
 template <typename T>
-int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
+int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first, bool last) {
   const size_t ng = (size_t)g_.ng;
   const T* tp = tape_ + slot * (size_t)kTape * ng;
   auto TP = [&](int q) { return (tape_alias_on_ && tape_alias_[q]) ? tape_alias_[q] : tp + (size_t)q * ng; };
@@ -166,7 +168,8 @@ int StepEngine<T>::adjoint_step(size_t slot, bool relax, bool first) {
                 TP(TP_LAPR), TP(TP_RHOIN), TP(TP_L), TP(TP_PSI), TP(TP_A), TP(TP_GPX), TP(TP_GPY), TP(TP_GPZ),
                 TP(TP_GRX), TP(TP_GRY), TP(TP_GRZ), adj_ + AJ_GPX * ng, adj_ + AJ_GPY * ng, adj_ + AJ_GPZ * ng,
                 adj_ + AJ_GRX * ng, adj_ + AJ_GRY * ng, adj_ + AJ_GRZ * ng, adj_ + AJ_A * ng, adj_ + AJ_PSI * ng,
-                adj_ + AJ_R * ng, adj_ + AJ_LAPR * ng, adj_ + AJ_L * ng, pgrad_, sc, relax ? 1 : 0};
+                adj_ + AJ_R * ng, adj_ + AJ_LAPR * ng, adj_ + AJ_L * ng, pgrad_, sc, relax ? 1 : 0,
+                TP(TP_RHONEW), last ? (T)energy_w_ : (T)0.0};
     adj_s6_kernel<T><<<blocks, 256, 0, stream_>>>(g_, a);
     SWC_CK(cudaGetLastError());
   }
@@ -271,7 +274,7 @@ template <typename T> int StepEngine<T>::tape_and_adjoint(int64_t n) {
   SWC_TRY(record_tape(tape_, n, true));
   const bool relax = !(n > p_.divv_switch || p_.load == 1);
   tape_alias_on_ = true;
-  const int rc = adjoint_step(0, relax, n == 1);
+  const int rc = adjoint_step(0, relax, n == 1, n == nloop_);
   tape_alias_on_ = false;
   return rc;
 }
@@ -375,8 +378,8 @@ int StepEngine<T>::reverse_binomial(int64_t l, int64_t n, size_t sl, size_t ff, 
 }
 
 template <typename T>
-int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0,
-                                 swc_grad* out) {
+int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double energy_lambda, double* dpsi0,
+                                 double* drho0, swc_grad* out) {
   const int K = p_.adjoint_ckpt;
   if (K == 0) {
     set_error("swc_backward needs params.adjoint_ckpt > 0 or -1 at swc_create");
@@ -431,9 +434,23 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
   auto AJ = [&](int q) { return adj_ + (size_t)q * ng; };
   SWC_CK(cudaMemsetAsync(adj_, 0, (size_t)kAdj * ng * sizeof(T), stream_));
   SWC_CK(cudaMemsetAsync(pgrad_, 0, pgrad_doubles() * sizeof(double), stream_));
-  // cotangent of the final state: psi(T) = DCT-III^3 psiq(T), rho(T)
-  if (dpsi) {
-    SWC_TRY(host_to_field(dpsi, AJ(AJ_PSI)));
+  // the final step's L and A (read by the energy term; the recompute overwrites them)
+  SWC_CK(cudaMemcpyAsync(AJ(AJ_KEEPL), lpsi_, ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  SWC_CK(cudaMemcpyAsync(AJ(AJ_KEEPA), amp_f_, ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  // cotangent of the final state: psi(T) = DCT-III^3 psiq(T), rho(T), plus lambda times
+  // that of the free-energy diagnostic of step T (REF:2214-2258)
+  if (dpsi) SWC_TRY(host_to_field(dpsi, AJ(AJ_PSI)));
+  if (drho) SWC_TRY(host_to_field(drho, AJ(AJ_R)));
+  energy_w_ = energy_lambda * dx_ * dx_ * dx_;  // the diagnostic's dx^3 (REF:2258)
+  if (energy_lambda != 0.0) {
+    const AdjScalars<T> sc{(T)p_.ep, (T)p_.alpha, (T)p_.beta, (T)p_.gamma, (T)p_.zeta, (T)kp_, (T)p_.rho_0,
+                           (T)(p_.q0 * p_.q0), (T)p_.dt, (T)(p_.dt / 2), (T)rho_m_, (T)scale_, (T)p_.nu,
+                           (T)(p_.lambda + 2 * p_.nu)};
+    adj_energy_final_kernel<T><<<pt4_blocks(g_), 256, 0, stream_>>>(
+        g_, psi_, rho_, AJ(AJ_KEEPL), AJ(AJ_KEEPA), (T)energy_w_, sc, AJ(AJ_PSI), AJ(AJ_R), pgrad_);
+    SWC_CK(cudaGetLastError());
+  }
+  if (dpsi || energy_lambda != 0.0) {
     using LP = LdPlain<T, T>;
     using SP = StPlain<T, T>;
     const AxisWeights<T> wh{{0, 0, 0}, (T)0.5};
@@ -441,7 +458,6 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
     SWC_TRY((pass<K_C2, 1>(LP{AJ(AJ_PSI)}, SP{AJ(AJ_PSI)})));
     SWC_TRY((pass<K_C2, 0>(LP{AJ(AJ_PSI)}, StW<T>{g_, AJ(AJ_Q), wh, 0})));
   }
-  if (drho) SWC_TRY(host_to_field(drho, AJ(AJ_R)));
   if (binomial) {
     SWC_TRY(reverse_binomial(0, Tn, 0, 2, nsnap));
   } else {
@@ -453,7 +469,7 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
       for (int64_t n = s0 + 1; n <= s1; ++n) SWC_TRY(record_tape(tape_ + (size_t)(n - s0 - 1) * kTape * ng, n));
       for (int64_t n = s1; n > s0; --n) {
         const bool relax = !(n > p_.divv_switch || p_.load == 1);
-        SWC_TRY(adjoint_step((size_t)(n - s0 - 1), relax, n == 1));
+        SWC_TRY(adjoint_step((size_t)(n - s0 - 1), relax, n == 1, n == Tn));
       }
     }
   }
@@ -478,6 +494,8 @@ int StepEngine<T>::backward_impl(const double* dpsi, const double* drho, double*
   double pg[PG_COUNT];
   SWC_CK(cudaMemcpyAsync(pg, pgrad_, sizeof(pg), cudaMemcpyDeviceToHost, stream_));
   SWC_TRY(restore_ckpt(last_slot));
+  SWC_CK(cudaMemcpyAsync(lpsi_, AJ(AJ_KEEPL), ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
+  SWC_CK(cudaMemcpyAsync(amp_f_, AJ(AJ_KEEPA), ng * sizeof(T), cudaMemcpyDeviceToDevice, stream_));
   diag_step_ = -1;  // the recompute overwrote the energy density and the sums
   pending_diag_ = -1;
   SWC_CK(cudaStreamSynchronize(stream_));

@@ -584,6 +584,11 @@ template <typename T> struct AdjS6Args {
   double* pgrad;
   AdjScalars<T> s;
   int relax;
+  // Energy term of the loss, last step only (ew = lambda dx^3, 0 otherwise): the free
+  // energy of REF:2214-2258 reads this step's L (stale, Q5) and A with the step's new
+  // density rho_new, so L_bar += ew rho_new L and A_bar += -ew zeta kp (rho_new - rho_0 - kp A).
+  const T* rho_new;
+  T ew;
 };
 template <typename T>
 __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
@@ -697,6 +702,15 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
         acc[3] += dkp;
         oA.v[e] += bA;
       }
+      if (a.ew != T(0.0)) {
+        V4<T> rn;
+        rn.load(a.rho_new, x);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          oL.v[e] += a.ew * rn.v[e] * L.v[e];
+          oA.v[e] += -a.ew * s.zeta * s.kp * (rn.v[e] - s.rho0 - s.kp * A.v[e]);
+        }
+      }
       oL.store(a.bL, x);
       op.store(a.bpsi, x);
       ol.store(a.blapR, x);
@@ -706,6 +720,46 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
   }
   const int slots[4] = {PG_BETA, PG_GAMMA, PG_RHO0, PG_KP};
   block_accum(acc, slots, g, a.pgrad);
+}
+
+// Energy term of the loss at the final state, E = dx^3 sum [rho e + zeta/2 d^2] with
+// e = -ep/2 psi^2 + L^2/2 - beta/4 psi^4 + gamma/6 psi^6 and d = rho - rho_0 - kp A
+// (REF:2214-2231; psi and rho after the last step, L and A of the last step). With
+// w = lambda dx^3: psi_bar += w rho (-ep psi - beta psi^3 + gamma psi^5),
+// rho_bar += w (e + zeta d), and the direct partials of beta, gamma, rho_0 and kp.
+// (L_bar and A_bar enter in the last step's adj_s6_kernel.)
+template <typename T>
+__global__ void __launch_bounds__(256) adj_energy_final_kernel(Grid g, const T* psi, const double* rho, const T* L,
+                                                               const T* A, T w, AdjScalars<T> s, T* bpsi, T* bR,
+                                                               double* pgrad) {
+  Pt4 p;
+  T acc[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};  // beta, gamma, rho0, kp
+  if (pt4(g, p)) {
+    const long long x = p.idx;
+    V4<T> ps, l, a, bp, br;
+    ps.load(psi, x);
+    l.load(L, x);
+    a.load(A, x);
+    bp.load(bpsi, x);
+    br.load(bR, x);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const T r = (T)rho[x + e], pe = ps.v[e], p2 = pe * pe;
+      const T en = -T(0.5) * s.ep * p2 + T(0.5) * (l.v[e] * l.v[e]) - T(0.25) * s.beta * (p2 * p2) +
+                   (s.gamma / T(6.0)) * (p2 * p2 * p2);
+      const T d = r - s.rho0 - s.kp * a.v[e];
+      bp.v[e] += w * r * (-s.ep * pe - s.beta * (p2 * pe) + s.gamma * (p2 * p2 * pe));
+      br.v[e] += w * (en + s.zeta * d);
+      acc[0] += w * r * (-T(0.25) * (p2 * p2));
+      acc[1] += w * r * ((p2 * p2 * p2) / T(6.0));
+      acc[2] += -w * s.zeta * d;
+      acc[3] += -w * s.zeta * d * a.v[e];
+    }
+    bp.store(bpsi, x);
+    br.store(bR, x);
+  }
+  const int slots[4] = {PG_BETA, PG_GAMMA, PG_RHO0, PG_KP};
+  block_accum(acc, slots, g, pgrad);
 }
 
 // bQ += Lambda(q) Y for the spectral multipliers of the forward (REF:1302 for

@@ -34,6 +34,15 @@ struct Grid {
   long long ng;
 };
 
+// Grid of power-of-two extents (validated by the caller).
+inline Grid make_grid(int nx, int ny, int nz) {
+  Grid g;
+  g.nx = nx; g.ny = ny; g.nz = nz;
+  g.lx = __builtin_ctz((unsigned)nx); g.ly = __builtin_ctz((unsigned)ny); g.lz = __builtin_ctz((unsigned)nz);
+  g.ng = (long long)nx * ny * nz;
+  return g;
+}
+
 // Per-axis wavenumber tables in the work precision T, exactly as the reference builds
 // them (smaiso-wcomp.cpp:445-481): Vq[i] = pi i/(d n), Vs[i] = pi (i+1)/(d n).
 template <typename T> struct Wavenumbers {

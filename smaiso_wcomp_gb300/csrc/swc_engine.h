@@ -2,6 +2,8 @@
 // precision-specific step engines (swc_step_fp64.cu, swc_step_mixed.cu).
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <string>
 
 #include "../../include/swc.h"
@@ -16,6 +18,7 @@ class EngineBase {
  public:
   virtual ~EngineBase() {}
   virtual int set_state(const double* psi, const double* rho) = 0;
+  virtual int set_state_ic(const swc_ic& ic) = 0;
   virtual int step(int nsteps) = 0;
   virtual int step_async(int nsteps) = 0;
   virtual int prepare() = 0;
@@ -30,8 +33,14 @@ class EngineBase {
   virtual int last_launches(int64_t* n) = 0;
   virtual int save(const char* path) = 0;
   virtual int load(const char* path) = 0;
-  virtual int backward(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out) = 0;
+  virtual int backward(const double* dpsi, const double* drho, double energy_lambda, double* dpsi0, double* drho0,
+                       swc_grad* out) = 0;
 };
+
+// Device initial conditions (swc_ic.cu): psi and rho (may be null) as FP64 (i,j,k)
+// arrays, enqueued on `stream`.
+int ic_check(const swc_ic* ic);
+int ic_generate(const swc_params& p, const swc_ic& ic, double* psi, double* rho, cudaStream_t stream);
 
 // Dense FMA throughput probe of the current device (TFLOP/s, FMA = 2 flops).
 int fma_peak(int precision, double* tflops);

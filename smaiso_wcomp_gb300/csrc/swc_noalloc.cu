@@ -16,7 +16,9 @@
 // (kNoAllocMaxChunks chunks = 160 KiB + 64 B). Every device that loads the library
 // holds this array until the process exits. Grids above
 // kNoAllocMaxChunks * kNoAllocChunk = 2^28 points are rejected.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cmath>
 #include <mutex>
@@ -87,30 +89,73 @@ __global__ void __launch_bounds__(32) noalloc_final_kernel(double* scratch, int 
 
 std::mutex g_setup_mu;
 double* g_scratch_ptr[kNoAllocMaxDevices] = {};
+CUcontext g_scratch_ctx[kNoAllocMaxDevices] = {};
 
-// Once per device, with that device current: the device address of the array.
-int scratch_for_current_device(double** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
-    cudaGetLastError();
-    set_error("swc_diagnostics_noalloc: no usable current CUDA device");
-    return SWC_ERR_NO_DEVICE;
-  }
+// The driver context current on this thread (the device's primary context once the
+// runtime has used the device); null if the driver entry point is unavailable.
+CUcontext current_context() {
+  static PFN_cuCtxGetCurrent_v4000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+  }();
+  CUcontext c = nullptr;
+  if (fn && fn(&c) != CUDA_SUCCESS) c = nullptr;
+  return c;
+}
+
+// Set-up, with device `dev` current: the device address of the array in the module
+// loaded into the device's current context. Looked up once per device, and again if
+// that context has changed since (a cudaDeviceReset by the caller recreates the
+// primary context, and with it the module and the array's address).
+int scratch_for_current_device(int dev, double** out) {
   std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
+  const CUcontext ctx = current_context();
+  if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
     double* ptr = nullptr;
     const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr) {
       cudaGetLastError();
+      g_scratch_ptr[dev] = nullptr;
       set_error("swc_diagnostics_noalloc: cudaGetSymbolAddress failed on device %d: %s", dev,
                 cudaGetErrorString(e));
       return SWC_ERR_CUDA;
     }
     g_scratch_ptr[dev] = ptr;
+    g_scratch_ctx[dev] = current_context();  // the lookup may have created the context
   }
   *out = g_scratch_ptr[dev];
   return SWC_OK;
 }
+
+// Makes p->device current for the call and puts the caller's device back on every
+// return path.
+struct DeviceScope {
+  int prev = -1;
+  bool changed = false;
+  int enter(int dev) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices || cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("swc_diagnostics_noalloc: no usable CUDA device %d", dev);
+      return SWC_ERR_NO_DEVICE;
+    }
+    if (prev != dev) {
+      if (cudaSetDevice(dev) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("swc_diagnostics_noalloc: cannot make device %d current", dev);
+        return SWC_ERR_NO_DEVICE;
+      }
+      changed = true;
+    }
+    return SWC_OK;
+  }
+  ~DeviceScope() {
+    if (changed) cudaSetDevice(prev);
+  }
+};
 
 }  // namespace
 }  // namespace swc
@@ -131,8 +176,10 @@ extern "C" int swc_diagnostics_noalloc(const swc_params* p, const double* psi, c
     set_error("swc_diagnostics_noalloc: NULL field or output");
     return SWC_ERR_BAD_PARAM;
   }
+  DeviceScope scope;
+  if ((rc = scope.enter(p->device))) return rc;
   double* scratch = nullptr;
-  if ((rc = scratch_for_current_device(&scratch))) return rc;
+  if ((rc = scratch_for_current_device(p->device, &scratch))) return rc;
   // REF:250-253, 267
   const double Amp = std::sqrt((3 * p->beta + std::sqrt(9 * p->beta * p->beta + 40 * p->ep * p->gamma)) / 5);
   const double kp = (1 - p->rho_0) / Amp;

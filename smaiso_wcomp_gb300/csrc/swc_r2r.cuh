@@ -220,6 +220,23 @@ template <typename T> struct NoMul {
   __device__ __forceinline__ T operator()(int, int, int) const { return (T)1; }
 };
 
+// Plain FP32 load times a pointwise multiplier m(i, j, k) (a spectral multiplier on the
+// input of an inverse pass). The TMA-fed z pass applies m as it reads the staged tile,
+// so such a pass keeps the TMA pipeline; the direct passes use these forms.
+template <class M> struct LdMul {
+  const float* p;
+  M m;
+  __device__ __forceinline__ float operator()(int i, int j, int k, long long idx) const { return p[idx] * m(i, j, k); }
+  __device__ __forceinline__ float2 pair(int i, int j, int k, long long idx) const {
+    const float2 v = ld2v(p, idx);
+    return make_float2(v.x * m(i, j, k), v.y * m(i, j, k + 1));
+  }
+  __device__ __forceinline__ float4 quad(int i, int j, int k, long long idx) const {
+    const float4 v = ld4v(p, idx);
+    return make_float4(v.x * m(i, j, k), v.y * m(i, j, k + 1), v.z * m(i, j, k + 2), v.w * m(i, j, k + 3));
+  }
+};
+
 // ---- the pass kernel ------------------------------------------------------------------
 
 template <typename T>

@@ -9,7 +9,9 @@
 // mbarrier transaction count; every wait is bounded (tables' max_polls): a wait that
 // runs out sets the tables' status flag and the CTA returns after one more bounded wait
 // for its copy in flight. Test support: wait_extra_tx makes every wait expect more bytes
-// than its copy delivers, so the wait runs out while the copy itself is a valid one.
+// than its copy delivers, so the wait runs out while the copy itself is a valid one; on
+// the way out those extra bytes are credited (mbarrier.complete_tx), so the second wait
+// ends when the valid copy has landed.
 // Used for plain FP32 loads (LdPlain<float, float>), any store/multiplier.
 #pragma once
 
@@ -31,6 +33,10 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Credit `bytes` of transaction count to the current phase, as landed copy bytes would.
+__device__ __forceinline__ void mbar_complete_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.complete_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   uint32_t ok;
@@ -103,11 +109,13 @@ __device__ __forceinline__ void tma_issue(const Grid& g, const CUtensorMap* map,
   }
 }
 
-template <int N, int KIND, int AX, class StoreOp, class MulOp>
+// LMUL: a pointwise multiplier of the loaded values (LdMul); the z pass of the inverse
+// cosine kind applies it as it reads the staged tile, the other forms take NoMul only.
+template <int N, int KIND, int AX, class StoreOp, class MulOp, class LMul>
 __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                  const float* __restrict__ zsrc, Grid g,
                                                                  R2RTables<float> tb, StoreOp st, MulOp mul,
-                                                                 int ntiles) {
+                                                                 LMul lmul, int ntiles) {
   using Cf = PairCfg<N>;
   using Tc = TmaCfg<N>;
   constexpr int M = Cf::M, LP = Cf::LP, PP = Cf::PP, NT = Cf::NT, TPL = Cf::TPL, NQ = Cf::NQ;
@@ -116,6 +124,8 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   constexpr bool inv_out = (KIND == K_C3 || KIND == K_S3 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
   constexpr bool xy = (AX != 2);
   constexpr int ZU = (LP * NQ) / NT;
+  constexpr bool load_mul = !std::is_same<LMul, NoMul<float>>::value;
+  static_assert(!load_mul || (AX == 2 && KIND == K_C3), "load multiplier: z pass of the inverse cosine kind only");
   extern __shared__ __align__(128) unsigned char tma_smem[];
   const float* S = reinterpret_cast<const float*>(tma_smem);
   PC* buf = reinterpret_cast<PC*>(tma_smem + Tc::TILE_BYTES);
@@ -140,7 +150,15 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
     if (!__syncthreads_and(ok)) {
       if (tid == 0) {
         if (tb.status) atomicExch(tb.status, 1);
-        mbar_wait_bounded(bar, parity, tb.max_polls);  // the copy in flight must land before the CTA leaves
+        // At most one copy is in flight (the next is issued only after this wait). The
+        // bytes the wait expected beyond the copy's own (wait_extra_tx, the wait test;
+        // 0 otherwise) are credited here, so the phase completes exactly when the real
+        // copy's bytes have landed, and thread 0 -- which keeps the CTA and its shared
+        // memory alive -- leaves only after that. A copy that still has not landed
+        // after this second bounded wait is a failed copy: the status flag is already
+        // set and the host reports SWC_ERR_CUDA for the pass.
+        if (tb.wait_extra_tx > 0) mbar_complete_tx(bar, (uint32_t)tb.wait_extra_tx);
+        mbar_wait_bounded(bar, parity, tb.max_polls);
       }
       return;
     }
@@ -220,7 +238,15 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
             const float2 A = S2[(2 * q) * M + (M - 1 - sl)], B = S2[(2 * q + 1) * M + (M - 1 - sl)];
             buf[sl * PP + q] = pmake(make_float2(A.y, B.y), make_float2(A.x, B.x));
           } else {
-            const float2 A = S2[(2 * q) * M + sl], B = S2[(2 * q + 1) * M + sl];
+            float2 A = S2[(2 * q) * M + sl], B = S2[(2 * q + 1) * M + sl];
+            if constexpr (load_mul) {  // lines (i, j) and (i, j + 1), elements k = 2 sl, 2 sl + 1
+              const int la = 2 * (pair0 + q);
+              const int i = la >> g.ly, j = la & (g.ny - 1);
+              A.x *= lmul(i, j, 2 * sl);
+              A.y *= lmul(i, j, 2 * sl + 1);
+              B.x *= lmul(i, j + 1, 2 * sl);
+              B.y *= lmul(i, j + 1, 2 * sl + 1);
+            }
             buf[sl * PP + q] = pmake(make_float2(A.x, B.x), make_float2(A.y, B.y));
           }
         }
@@ -264,9 +290,9 @@ template <int N, int AX> inline cudaError_t make_pass_map(const Grid& g, const f
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-template <int N, int KIND, int AX, class ST, class MUL>
+template <int N, int KIND, int AX, class ST, class MUL, class LMUL = NoMul<float>>
 cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t stream, const float* src, ST st,
-                       MUL mul) {
+                       MUL mul, LMUL lmul = LMUL()) {
   using Tc = TmaCfg<N>;
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
@@ -274,7 +300,7 @@ cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t s
     const cudaError_t e = make_pass_map<N, AX>(g, src, &map);
     if (e != cudaSuccess) return e;
   }
-  auto kern = r2r_tma_kernel<N, KIND, AX, ST, MUL>;
+  auto kern = r2r_tma_kernel<N, KIND, AX, ST, MUL, LMUL>;
   const size_t smem = Tc::smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -284,7 +310,7 @@ cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t s
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, PairCfg<N>::NT, smem)) != cudaSuccess) return e;
   const int ntiles = (int)((g.ng / N) / Tc::LINES);
   const int blocks = std::min(ntiles, std::max(occ, 1) * sms);
-  kern<<<blocks, PairCfg<N>::NT, smem, stream>>>(map, src, g, tb, st, mul, ntiles);
+  kern<<<blocks, PairCfg<N>::NT, smem, stream>>>(map, src, g, tb, st, mul, lmul, ntiles);
   return cudaGetLastError();
 }
 

@@ -97,10 +97,9 @@ template <typename T> struct MulLap {
   }
 };
 
-// alpha (q0^2 - |q|^2) psiq (REF:1302).
-// psiq: the FP64 state (FP64 engine) or its FP32 copy (mixed engine).
-template <typename T, typename P = double> struct LdLpsi {
-  const P* psiq;
+// FP64 engine: alpha (q0^2 - |q|^2) psiq (REF:1302), on the FP64 state.
+template <typename T> struct LdLpsi {
+  const double* psiq;
   const T *qx, *qy, *qz;
   T alpha, q02;
   __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
@@ -108,17 +107,11 @@ template <typename T, typename P = double> struct LdLpsi {
     const T mq2 = (a * a) + (b * b) + (c * c);
     return alpha * (q02 - mq2) * (T)psiq[idx];
   }
-  __device__ __forceinline__ float4 quad(int i, int j, int k, long long idx) const {
-    const float ab = (float)qx[i] * (float)qx[i] + (float)qy[j] * (float)qy[j];
-    const float4 c = ld4v(qz, k), p = ld4v(psiq, idx);
-    auto f = [&](float cz, float ps) { return (float)alpha * ((float)q02 - (ab + cz * cz)) * ps; };
-    return make_float4(f(c.x, p.x), f(c.y, p.y), f(c.z, p.z), f(c.w, p.w));
-  }
 };
 
-// relax phase: -|q|^2 alpha (q0^2 - |q|^2) psiq (REF:1356-1357).
-template <typename T, typename P = double> struct LdRelaxLap {
-  const P* psiq;
+// FP64 engine, relax phase: -|q|^2 alpha (q0^2 - |q|^2) psiq (REF:1356-1357).
+template <typename T> struct LdRelaxLap {
+  const double* psiq;
   const T *qx, *qy, *qz;
   T alpha, q02;
   __device__ __forceinline__ T operator()(int i, int j, int k, long long idx) const {
@@ -126,31 +119,66 @@ template <typename T, typename P = double> struct LdRelaxLap {
     const T mq2 = (a * a) + (b * b) + (c * c);
     return -mq2 * alpha * (q02 - mq2) * (T)psiq[idx];
   }
-  __device__ __forceinline__ float4 quad(int i, int j, int k, long long idx) const {
-    const float ab = (float)qx[i] * (float)qx[i] + (float)qy[j] * (float)qy[j];
-    const float4 c = ld4v(qz, k), p = ld4v(psiq, idx);
-    auto f = [&](float cz, float ps) {
-      const float mq2 = ab + cz * cz;
-      return -mq2 * (float)alpha * ((float)q02 - mq2) * ps;
-    };
-    return make_float4(f(c.x, p.x), f(c.y, p.y), f(c.z, p.z), f(c.w, p.w));
+};
+
+// alpha (q0^2 - |q|^2) (REF:1302) and, RELAX, the relax phase's -|q|^2 alpha (q0^2 - |q|^2)
+// (REF:1356-1357): the multipliers of the mixed engine's FP32 psiq copy (LdMul), which
+// keep the first pass of these inverse transforms on the TMA pipeline.
+template <int RELAX> struct LapMul {
+  const float *qx, *qy, *qz;
+  float alpha, q02;
+  __device__ __forceinline__ float operator()(int i, int j, int k) const {
+    const float mq2 = (qx[i] * qx[i] + qy[j] * qy[j]) + qz[k] * qz[k];
+    const float m = alpha * (q02 - mq2);
+    return RELAX ? -mq2 * m : m;
   }
 };
 
-// rho * dfDlapPsi (REF:1321).
-// rho: the FP64 state with off = 0 (FP64 engine) or the mixed engine's FP32 copy
-// rho - off with off = (rho_0 + rho_s)/2.
-template <typename T, typename P = double> struct LdRhoL {
-  const P* rho;
+// Last pass of dfDlapPsi in the mixed engine's normal phase: stores dfDlapPsi and
+// rho * dfDlapPsi (REF:1321, with rho = rhof + off), so the Delta(rho L) transform
+// starts with a plain TMA-fed pass.
+struct StLpsiRhoL {
+  float *lpsi, *rhoL;
+  const float* rhof;
+  float off;
+  __device__ __forceinline__ void operator()(int, int, int, long long idx, float v) const {
+    lpsi[idx] = v;
+    rhoL[idx] = (rhof[idx] + off) * v;
+  }
+  __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const {
+    st2v(lpsi, idx, v);
+    const float2 r = ld2v(rhof, idx);
+    st2v(rhoL, idx, make_float2((r.x + off) * v.x, (r.y + off) * v.y));
+  }
+  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 v) const {
+    st4v(lpsi, idx, v);
+    const float4 r = ld4v(rhof, idx);
+    st4v(rhoL, idx, make_float4((r.x + off) * v.x, (r.y + off) * v.y, (r.z + off) * v.z, (r.w + off) * v.w));
+  }
+};
+
+// FP64 engine: rho * dfDlapPsi (REF:1321).
+template <typename T> struct LdRhoL {
+  const double* rho;
   const T* lpsi;
   T off;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
     return ((T)rho[idx] + off) * lpsi[idx];
   }
-  __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
-    const float4 r = ld4v(rho, idx), l = ld4v(lpsi, idx);
-    const float o = (float)off;
-    return make_float4((r.x + o) * l.x, (r.y + o) * l.y, (r.z + o) * l.z, (r.w + o) * l.w);
+};
+
+// Store v + other[idx] (a running sum over passes, read where it is written).
+template <typename T> struct StAdd {
+  T* p;
+  const T* other;
+  __device__ __forceinline__ void operator()(int, int, int, long long idx, T v) const { p[idx] = v + other[idx]; }
+  __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const {
+    const float2 o = ld2v(other, idx);
+    st2v(p, idx, make_float2(v.x + o.x, v.y + o.y));
+  }
+  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 v) const {
+    const float4 o = ld4v(other, idx);
+    st4v(p, idx, make_float4(v.x + o.x, v.y + o.y, v.z + o.z, v.w + o.w));
   }
 };
 
@@ -234,6 +262,7 @@ struct LdNlMixed {
   float *frho, *rhof;
   double offd;
   float dt, kp, zeta, rho0, off;
+  const float* mdivf;  // -grad.f in real space (REF:2078-2090, the transposed-derivative passes)
   __device__ __forceinline__ float point(float ux, float uy, float uz, float gx, float gy, float gz, float dv,
                                          float m, float a, float ps, float px, float py, float pz, float rf,
                                          float fp, double& r, float& s, float& rfn) const {
@@ -252,7 +281,7 @@ struct LdNlMixed {
     rho[idx] = r;
     frho[idx] = sr;
     rhof[idx] = rfn;
-    return out;
+    return out + mdivf[idx];
   }
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
@@ -272,42 +301,33 @@ struct LdNlMixed {
     *reinterpret_cast<double2*>(rho + idx + 2) = make_double2(r[2], r[3]);
     st4v(frho, idx, make_float4(sr[0], sr[1], sr[2], sr[3]));
     st4v(rhof, idx, make_float4(rfn[0], rfn[1], rfn[2], rfn[3]));
-    return make_float4(o[0], o[1], o[2], o[3]);
+    const float4 df = ld4g(mdivf, idx);
+    return make_float4(o[0] + df.x, o[1] + df.y, o[2] + df.z, o[3] + df.w);
   }
 };
 
 // Last pass of the Nl transform: Nlq = DCT(Nl) - q.f, then the CN/AB2 update of psiq
-// (REF:2170-2190). FP64 engine: the reference's expression; mixed engine: the same
-// update in increment form psiq + (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
-// which follows from C1 - C2 = 1/2 and avoids cancelling C1 psiq against psiq_old.
-// The mixed engine reads 1/C2 from an FP64 table (inv_c2, built once in FP64) so
-// the pass does no FP64 division; the FP64 engine evaluates C1, C2 per mode.
+// (REF:2170-2190), the FP64 engine's form: the reference's expression with C1, C2
+// evaluated per mode (the mixed engine's increment form is LdNlUpdate below).
 template <typename T> struct StNlUpdate {
   const T* dq;
   double *psiq, *psiq_old;
   T* nlq;
   const double *qx, *qy, *qz;
-  const double* inv_c2;  // mixed engine only
   double ep, alpha, q02, dt, rho_m, dtd2, scale;
   int first;
-  int increment;
   __device__ __forceinline__ void operator()(int i, int j, int k, long long idx, T v) const {
     const T nl = v - dq[idx];
     const T nlo = first ? nl : nlq[idx];
     const double pq = psiq[idx], pqo = psiq_old[idx];
     const double src = dtd2 * scale * (3.0 * (double)nl - (double)nlo);
-    double pn;
-    if (increment) {
-      pn = pq + (0.5 * (pq - pqo) + src) * inv_c2[idx];
-    } else {
-      const double a = qx[i], b = qy[j], c = qz[k];
-      const double mq2 = a * a + b * b + c * c;
-      const double s = q02 - mq2;
-      const double aLin = ep - alpha * (s * s);
-      const double C1 = (2.0 - dt * rho_m * aLin);
-      const double C2 = (1.5 - dt * rho_m * aLin);
-      pn = (C1 * pq - 0.5 * pqo + src) / C2;
-    }
+    const double a = qx[i], b = qy[j], c = qz[k];
+    const double mq2 = a * a + b * b + c * c;
+    const double s = q02 - mq2;
+    const double aLin = ep - alpha * (s * s);
+    const double C1 = (2.0 - dt * rho_m * aLin);
+    const double C2 = (1.5 - dt * rho_m * aLin);
+    const double pn = (C1 * pq - 0.5 * pqo + src) / C2;
     psiq_old[idx] = pq;
     psiq[idx] = pn;
     nlq[idx] = nl;
@@ -327,21 +347,14 @@ template <typename T> struct StNlUpdate {
     const double2 pqo = ld2dg(psiq_old, idx);
     const double s0 = dtd2 * scale * (3.0 * (double)nl0 - (double)nlo0);
     const double s1 = dtd2 * scale * (3.0 * (double)nl1 - (double)nlo1);
-    double pn0, pn1;
-    if (increment) {
-      const double2 ic = ld2dg(inv_c2, idx);
-      pn0 = pq.x + (0.5 * (pq.x - pqo.x) + s0) * ic.x;
-      pn1 = pq.y + (0.5 * (pq.y - pqo.y) + s1) * ic.y;
-    } else {
-      const double ab = qx[i] * qx[i] + qy[j] * qy[j];
-      auto upd = [&](double cz, double p, double po, double src) {
-        const double s = q02 - (ab + cz * cz);
-        const double aLin = ep - alpha * (s * s);
-        return ((2.0 - dt * rho_m * aLin) * p - 0.5 * po + src) / (1.5 - dt * rho_m * aLin);
-      };
-      pn0 = upd(qz[k], pq.x, pqo.x, s0);
-      pn1 = upd(qz[k + 1], pq.y, pqo.y, s1);
-    }
+    const double ab = qx[i] * qx[i] + qy[j] * qy[j];
+    auto upd = [&](double cz, double p, double po, double src) {
+      const double s = q02 - (ab + cz * cz);
+      const double aLin = ep - alpha * (s * s);
+      return ((2.0 - dt * rho_m * aLin) * p - 0.5 * po + src) / (1.5 - dt * rho_m * aLin);
+    };
+    const double pn0 = upd(qz[k], pq.x, pqo.x, s0);
+    const double pn1 = upd(qz[k + 1], pq.y, pqo.y, s1);
     *reinterpret_cast<double2*>(psiq_old + idx) = pq;
     *reinterpret_cast<double2*>(psiq + idx) = make_double2(pn0, pn1);
     st2v(nlq, idx, make_float2(nl0, nl1));
@@ -354,7 +367,10 @@ template <typename T> struct StNlUpdate {
 // psiq_old, psiq, nlq and psiqf. The increment (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
 // a small correction built from FP32 data, is formed in FP32 with an FP32 1/C2 table;
 // FP64 holds the state: two FP64 adds per point (psiq - psiq_old, psiq + increment),
-// conversions on the integer pipes.
+// conversions on the integer pipes. The modes the table flags (a negative entry: the
+// k = 0 mode, and the modes near the q0 shell whose denominator differs from 1.5 by
+// less than FP32 resolves, inv_c2_kernel) form the increment in FP64 with C2
+// evaluated in FP64.
 struct LdNlUpdate {
   const float *nlw, *dq;
   float* nlq;
@@ -363,14 +379,26 @@ struct LdNlUpdate {
   float* psiqf;
   float srcs;  // dt/2 scale
   int first;
-  __device__ __forceinline__ float point(float nl, float nlo, double pq, double pqo, float ic, double& pn) const {
+  Grid g;
+  const double *qx, *qy, *qz;        // FP64 wavenumbers of the flagged modes' C2
+  double ep, alpha, q02, dtrm, srcs_d;  // dtrm = dt rho_m, srcs_d = dt/2 scale
+  __device__ __forceinline__ float point(float nl, float nlo, double pq, double pqo, float ic, double& pn,
+                                         long long idx) const {
+    if (ic < 0.0f) {  // flagged mode: FP64 increment, FP64 C2 (REF:957-958)
+      const int k = (int)(idx & (g.nz - 1)), j = (int)((idx >> g.lz) & (g.ny - 1)), i = (int)(idx >> (g.ly + g.lz));
+      const double s = q02 - (qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k]);
+      const double c2 = 1.5 - dtrm * (ep - alpha * (s * s));
+      pn = pq + (0.5 * (pq - pqo) + srcs_d * (3.0 * (double)nl - (double)nlo)) / c2;
+      return narrow_f64(pn);
+    }
     const float inc = (0.5f * narrow_f64(pq - pqo) + srcs * (3.0f * nl - nlo)) * ic;
     pn = pq + widen_f32(inc);
     return narrow_f64(pn);
   }
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
-    const float4 w = ld4g(nlw, idx), d = ld4g(dq, idx), ic = ld4g(inv_c2, idx);
+    const float4 w = ld4g(nlw, idx), ic = ld4g(inv_c2, idx);
+    const float4 d = dq ? ld4g(dq, idx) : make_float4(0.f, 0.f, 0.f, 0.f);  // null: grad.f is in Nl
     const float nl[4] = {w.x - d.x, w.y - d.y, w.z - d.z, w.w - d.w};
     float nlo[4] = {nl[0], nl[1], nl[2], nl[3]};
     if (!first) {
@@ -381,10 +409,10 @@ struct LdNlUpdate {
     const double2 o01 = ld2dg(psiq_old, idx), o23 = ld2dg(psiq_old, idx + 2);
     double pn[4];
     float pf[4];
-    pf[0] = point(nl[0], nlo[0], p01.x, o01.x, ic.x, pn[0]);
-    pf[1] = point(nl[1], nlo[1], p01.y, o01.y, ic.y, pn[1]);
-    pf[2] = point(nl[2], nlo[2], p23.x, o23.x, ic.z, pn[2]);
-    pf[3] = point(nl[3], nlo[3], p23.y, o23.y, ic.w, pn[3]);
+    pf[0] = point(nl[0], nlo[0], p01.x, o01.x, ic.x, pn[0], idx);
+    pf[1] = point(nl[1], nlo[1], p01.y, o01.y, ic.y, pn[1], idx + 1);
+    pf[2] = point(nl[2], nlo[2], p23.x, o23.x, ic.z, pn[2], idx + 2);
+    pf[3] = point(nl[3], nlo[3], p23.y, o23.y, ic.w, pn[3], idx + 3);
     *reinterpret_cast<double2*>(psiq_old + idx) = p01;
     *reinterpret_cast<double2*>(psiq_old + idx + 2) = p23;
     *reinterpret_cast<double2*>(psiq + idx) = make_double2(pn[0], pn[1]);
@@ -553,19 +581,24 @@ template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S
   fx.store(a.fx, idx); fy.store(a.fy, idx); fz.store(a.fz, idx);
 }
 
-// 1/C2 per spectral mode (REF:957-958), evaluated in FP64 and stored as O, built once
-// for the mixed engine.
-template <typename O>
-__global__ void __launch_bounds__(256) inv_c2_kernel(Grid g, const double* qx, const double* qy, const double* qz,
+// 1/C2 per spectral mode (REF:957-958), evaluated in FP64 and stored in FP32, built
+// once for the mixed engine. C2 = 1.5 - dt rho_m aLin > 1.5, so the sign is free to flag
+// the modes whose update the mixed engine keeps in FP64 (negative entry): the k = 0
+// mode (the mean) and the modes near the q0 shell, where dt rho_m |aLin| -- what sets
+// the semi-implicit damping, C2 - 1.5 -- is below 8 FP32 ulps of 1.5 (9.5e-7).
+static __global__ void __launch_bounds__(256) inv_c2_kernel(Grid g, const double* qx, const double* qy, const double* qz,
                                                      double ep, double alpha, double q02, double dt, double rho_m,
-                                                     O* out) {
+                                                     float* out) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= g.ng) return;
   const int k = (int)(idx & (g.nz - 1)), j = (int)((idx >> g.lz) & (g.ny - 1)), i = (int)(idx >> (g.ly + g.lz));
   const double mq2 = qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k];
   const double s = q02 - mq2;
   const double aLin = ep - alpha * (s * s);
-  out[idx] = (O)(1.0 / (1.5 - dt * rho_m * aLin));
+  const double damp = dt * rho_m * aLin;
+  const float ic = (float)(1.0 / (1.5 - damp));
+  const bool fp64 = idx == 0 || -damp < 8.0 * 1.1920928955078125e-7 * 1.5;
+  out[idx] = fp64 ? -ic : ic;
 }
 
 // S8 + S9 (REF:1479-1974): Stokes solve on the three staggered grids, spectral.
@@ -578,12 +611,24 @@ template <typename T> struct StokesArgs {
   int block;  // x-slab size of the reference decomposition (REF:299)
   T *vsumx, *vsumy, *vsumz;  // v_sol + v_irr per component, the input of the S11 transforms
   int write_vsol;            // v_sol itself only when it is transformed for output
+  int write_virr;            // v_irr itself: for the divergence kernel, or for the adjoint's tape
+  T* divv;                   // stokes_kernel<T, true>: div v-hat of REF:2042-2076 (cosine grid)
 };
 
 // Four consecutive points along z per thread, with 32-bit indices (n^3 <= 2^30). The
 // staggered neighbours at k-1 / k+1 come from the aligned 4-vector of the neighbouring
 // row plus one scalar at its edge; every per-point expression is the one-point form.
-template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid g, StokesArgs<T> a) {
+//
+// DIVV: the kernel also writes div v-hat (i, j, k) = qx v_irr,x(i-1, j, k) + qy
+// v_irr,y(i, j-1, k) + qz v_irr,z(i, j, k-1) (REF:2042-2076). The three staggered points
+// it reads share the point's own inputs: since Vs[n-1] = Vq[n] (and so gs[n-1] = gq[n],
+// bit for bit: same expression), each has |q|^2 = |q(i,j,k)|^2, the Gaussian G(i,j,k),
+// fg = fgrad + E G at (i,j,k), and the same q.S = D = qx Sx(i-1,j,k) + qy Sy(i,j-1,k) +
+// qz Sz(i,j,k-1). With the reference's index ranges (v_x for i-1 < nx-1, v_y and v_z
+// for j', k' < n-1, REF:1584, 1760-1812) and the rank-count quirk of v_z at k' = 0
+// (REF:1932):
+//   div v-hat = scale/((lambda + 2 nu) |q|^2) sum_valid q_a^2 (fg + D G_a / |q|^2).
+template <typename T, bool DIVV> __global__ void __launch_bounds__(256) stokes_kernel(Grid g, StokesArgs<T> a) {
   const int idx = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (idx >= (int)g.ng) return;
   const int k0 = idx & (g.nz - 1), j = (idx >> g.lz) & (g.ny - 1), i = idx >> (g.ly + g.lz);
@@ -626,7 +671,7 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
     vi = V4<T>::zero();
   }
   if (a.write_vsol) vs.store(a.vsolx, idx);
-  vi.store(a.virrx, idx);
+  if (a.write_virr) vi.store(a.virrx, idx);
 #pragma unroll
   for (int c = 0; c < 4; ++c) vs.v[c] = vs.v[c] + vi.v[c];
   vs.store(a.vsumx, idx);
@@ -698,8 +743,10 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
     ys.store(a.vsoly, idx);
     zs.store(a.vsolz, idx);
   }
-  yi.store(a.virry, idx);
-  zi.store(a.virrz, idx);
+  if (a.write_virr) {
+    yi.store(a.virry, idx);
+    zi.store(a.virrz, idx);
+  }
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     ys.v[c] = ys.v[c] + yi.v[c];
@@ -707,6 +754,45 @@ template <typename T> __global__ void __launch_bounds__(256) stokes_kernel(Grid 
   }
   ys.store(a.vsumy, idx);
   zs.store(a.vsumz, idx);
+  if constexpr (DIVV) {
+    V4<T> sxm = V4<T>::zero(), sym = V4<T>::zero(), F, E, dv;
+    if (i > 0) sxm.load(a.Sx, idx - sx);
+    if (j > 0) sym.load(a.Sy, idx - sy);
+    F.load(a.fgrad, idx);
+    E.load(a.ener, idx);
+    const T szp = (k0 != 0) ? a.Sz[idx - 1] : (T)0;  // Sz(i, j, k0 - 1)
+    const T Gxy = a.gqx[i] * a.gqy[j];
+    const T qx2 = qxi * qxi, qy2 = qyj * qyj;
+    const bool off_first_slab = (i % a.block) != 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int k = k0 + c;
+      const bool vx = i > 0, vy = (j > 0) && (k < g.nz - 1), vz = (k > 0) && (j < g.ny - 1);
+      T out = (T)0;
+      if (vx || vy || vz) {
+        const T qzk = qz.v[c];
+        const T qz2 = qzk * qzk;
+        const T Szm = (c == 0) ? szp : Szc.v[c - 1];
+        const T D = qxi * sxm.v[c] + qyj * sym.v[c] + qzk * Szm;
+        const T inv = (T)1 / (qx2 + qy2 + qz2);
+        const T G = Gxy * gqz.v[c];
+        const T fg = F.v[c] + E.v[c] * G;
+        const T t = D * inv;
+        T sum = (T)0;
+        if (vx) sum += qx2 * (fg + t * G);
+        if (vy) sum += qy2 * (fg + t * G);
+        if (vz) {
+          // v_z at k' = k - 1 = 0, j > 0, off a rank's first x slab: CM1y's filter
+          // gqx[i] gsy[j] gqz[k'] (REF:1932) instead of G
+          const T Gz = (k == 1 && j > 0 && off_first_slab) ? a.gqx[i] * a.gsy[j] * a.gqz[0] : G;
+          sum += qz2 * (fg + t * Gz);
+        }
+        out = a.scale * a.inv_lam2nu * inv * sum;
+      }
+      dv.v[c] = out;
+    }
+    dv.store(a.divv, idx);
+  }
 }
 
 // S10 (REF:2042-2079): div v and q.f on the cosine grid (q.f without `scale`).
@@ -841,6 +927,8 @@ template <typename T> class StepEngine : public EngineBase {
 
   int init();
   int set_state(const double* psi, const double* rho) override;
+  int set_state_ic(const swc_ic& ic) override;
+  int preloop(bool have_rho);  // the pre-loop from psi staged in frho_ (and rho_)
   int step(int nsteps) override;
   int step_async(int nsteps) override;
   int prepare() override;
@@ -867,8 +955,9 @@ template <typename T> class StepEngine : public EngineBase {
   }
   int save(const char* path) override;
   int load(const char* path) override;
-  int backward(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out) override {
-    return backward_impl(dpsi, drho, dpsi0, drho0, out);
+  int backward(const double* dpsi, const double* drho, double energy_lambda, double* dpsi0, double* drho0,
+               swc_grad* out) override {
+    return backward_impl(dpsi, drho, energy_lambda, dpsi0, drho0, out);
   }
 
  private:
@@ -879,12 +968,14 @@ template <typename T> class StepEngine : public EngineBase {
   int psi_from_state();  // psi = DCT-III^3 psiq with the step's own last three passes
   // FP64 engine: the FP64 adjoint (swc_adjoint_impl.cuh, in swc_step_fp64.cu); mixed
   // engine: the same adjoint in FP32 on the mixed trajectory (swc_step_mixed_adj.cu)
-  int backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0, swc_grad* out);
+  int backward_impl(const double* dpsi, const double* drho, double energy_lambda, double* dpsi0, double* drho0,
+                    swc_grad* out);
+  double energy_w_ = 0.0;          // lambda dx^3 of the current swc_backward's energy term
   int record_tape(T* tp, int64_t n, bool alias = false);
   int host_to_field(const double* src, T* dst);
   int field_to_host(const T* src, double* dst);
   int stage_alloc();
-  int adjoint_step(size_t slot, bool relax, bool first);
+  int adjoint_step(size_t slot, bool relax, bool first, bool last);
   int adjoint_alloc(size_t tape_fields);
   int tape_and_adjoint(int64_t n);                        // step n from the loaded state n-1
   int advance(int64_t from, int64_t k);                   // k plain steps from state `from`
@@ -1123,7 +1214,7 @@ template <typename T> int StepEngine<T>::init() {
       if ((rc = dalloc(nt, (void**)b))) return rc;
       SWC_CK(cudaMemsetAsync(*b, 0, nt, stream_));
     }
-    inv_c2_kernel<T><<<(unsigned)((g_.ng + 255) / 256), 256, 0, stream_>>>(
+    inv_c2_kernel<<<(unsigned)((g_.ng + 255) / 256), 256, 0, stream_>>>(
         g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt, rho_m_, inv_c2f_);
     SWC_CK(cudaGetLastError());
     SWC_CK(cudaStreamSynchronize(stream_));
@@ -1196,18 +1287,22 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
   SWC_TRY((pass<K_C3, 2>(LP{amp_f_}, SP{amp_f_})));
   // S4 (REF:1293-1308): dfDlapPsi
   const T alpha = (T)p_.alpha, q02 = (T)(p_.q0 * p_.q0);
-  if constexpr (std::is_same<T, double>::value)
+  if constexpr (std::is_same<T, double>::value) {
     SWC_TRY((pass<K_C3, 2>(LdLpsi<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
-  else
-    SWC_TRY((pass<K_C3, 2>(LdLpsi<T, T>{psiqf_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lpsi_})));
-  SWC_TRY((pass<K_C3, 1>(LP{lpsi_}, SP{lpsi_})));
-  SWC_TRY((pass<K_C3, 0>(LP{lpsi_}, SP{lpsi_})));
+    SWC_TRY((pass<K_C3, 1>(LP{lpsi_}, SP{lpsi_})));
+    SWC_TRY((pass<K_C3, 0>(LP{lpsi_}, SP{lpsi_})));
+  } else {
+    SWC_TRY((pass<K_C3, 2>(LdMul<LapMul<0>>{psiqf_, LapMul<0>{vq_[0], vq_[1], vq_[2], alpha, q02}}, SP{lpsi_})));
+    SWC_TRY((pass<K_C3, 1>(LP{lpsi_}, SP{lpsi_})));
+    if (relax) SWC_TRY((pass<K_C3, 0>(LP{lpsi_}, SP{lpsi_})));
+    else SWC_TRY((pass<K_C3, 0>(LP{lpsi_}, StLpsiRhoL{lpsi_, lapR_, rhof_, (T)rho_off_})));
+  }
   // S5 (REF:1312-1380)
   if (!relax) {
     if constexpr (std::is_same<T, double>::value)
       SWC_TRY((pass<K_C2, 2>(LdRhoL<T>{rho_, lpsi_, (T)0}, SP{lapR_})));
-    else
-      SWC_TRY((pass<K_C2, 2>(LdRhoL<T, T>{rhof_, lpsi_, (T)rho_off_}, SP{lapR_})));
+    else  // rho L written by the last pass of dfDlapPsi
+      SWC_TRY((pass<K_C2, 2>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_C2, 1>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_FILT, 0>(LP{lapR_}, SP{lapR_}, MulLap<T>{vq_[0], vq_[1], vq_[2], (T)scale_})));
     SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
@@ -1216,7 +1311,7 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
     if constexpr (std::is_same<T, double>::value)
       SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T>{psiq_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
     else
-      SWC_TRY((pass<K_C3, 2>(LdRelaxLap<T, T>{psiqf_, vq_[0], vq_[1], vq_[2], alpha, q02}, SP{lapR_})));
+      SWC_TRY((pass<K_C3, 2>(LdMul<LapMul<1>>{psiqf_, LapMul<1>{vq_[0], vq_[1], vq_[2], alpha, q02}}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 1>(LP{lapR_}, SP{lapR_})));
     SWC_TRY((pass<K_C3, 0>(LP{lapR_}, SP{lapR_})));
   }
@@ -1309,15 +1404,30 @@ template <typename T> int StepEngine<T>::refresh_copies(int frho_mode) {
 
 template <typename T> int StepEngine<T>::set_state(const double* psi, const double* rho) {
   SWC_CK(cudaSetDevice(p_.device));
+  const size_t nd = (size_t)g_.ng * sizeof(double);
+  // psi staged in frho_, rho (or the reference's zero fill, REF:1053) in rho_
+  SWC_CK(cudaMemcpyAsync(frho_, psi, nd, cudaMemcpyHostToDevice, stream_));
+  if (rho) SWC_CK(cudaMemcpyAsync(rho_, rho, nd, cudaMemcpyHostToDevice, stream_));
+  return preloop(rho != nullptr);
+}
+
+// The initial psi and rho written by the device generator into the same staging
+// arrays: no host arrays, no host-to-device copy.
+template <typename T> int StepEngine<T>::set_state_ic(const swc_ic& ic) {
+  SWC_CK(cudaSetDevice(p_.device));
+  SWC_TRY(ic_generate(p_, ic, frho_, rho_, stream_));
+  const bool has_rho = ic.kind == SWC_IC_FLAT || ic.kind == SWC_IC_UNDULATED || ic.kind == SWC_IC_DISLOCATIONS;
+  return preloop(has_rho);
+}
+
+template <typename T> int StepEngine<T>::preloop(bool have_rho) {
   const size_t nd = (size_t)g_.ng * sizeof(double), nt = (size_t)g_.ng * sizeof(T);
   // REF:968-982: psiq = scale * DCT(psi), in FP64 for both engines (psi staged in frho_)
-  SWC_CK(cudaMemcpyAsync(frho_, psi, nd, cudaMemcpyHostToDevice, stream_));
   SWC_TRY((passU<double, K_C2, 2>(LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
   SWC_TRY((passU<double, K_C2, 1>(LdPlain<double, double>{frho_}, StPlain<double, double>{frho_})));
   SWC_TRY((passU<double, K_C2, 0>(LdPlain<double, double>{frho_}, StScaleD{psiq_, scale_})));
   // REF:1052-1071 (+ caller's rho); f_rho, Nl_old and the work arrays start at zero
-  if (rho) SWC_CK(cudaMemcpyAsync(rho_, rho, nd, cudaMemcpyHostToDevice, stream_));
-  else SWC_CK(cudaMemsetAsync(rho_, 0, nd, stream_));
+  if (!have_rho) SWC_CK(cudaMemsetAsync(rho_, 0, nd, stream_));
   SWC_CK(cudaMemsetAsync(frho_, 0, nd, stream_));
   SWC_CK(cudaMemcpyAsync(psiq_old_, psiq_, nd, cudaMemcpyDeviceToDevice, stream_));  // REF:1005
   T* zero[] = {nlq_, psi_old_, gp_[0], gp_[1], gp_[2], gr_[0], gr_[1], gr_[2], amp_f_, divv_, v_[0], v_[1], v_[2],

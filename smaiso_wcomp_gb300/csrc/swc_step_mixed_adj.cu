@@ -4,6 +4,6 @@
 #include "swc_adjoint_impl.cuh"
 
 namespace swc {
-template int StepEngine<float>::backward_impl(const double* dpsi, const double* drho, double* dpsi0, double* drho0,
-                                              swc_grad* out);
+template int StepEngine<float>::backward_impl(const double* dpsi, const double* drho, double energy_lambda,
+                                              double* dpsi0, double* drho0, swc_grad* out);
 }  // namespace swc

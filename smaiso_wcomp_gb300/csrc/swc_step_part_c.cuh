@@ -44,21 +44,23 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
                rho_, frho_, p_.dt, kp_, p_.zeta, p_.rho_0};
     SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
     SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
-    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], nullptr, p_.ep, p_.alpha,
-                     p_.q0 * p_.q0, p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0, 0};
+    StNlUpdate<T> st{dq_, psiq_, psiq_old_, nlq_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha,
+                     p_.q0 * p_.q0, p_.dt, rho_m_, p_.dt / 2, scale_, first ? 1 : 0};
     SWC_TRY((pass<K_C2, 0>(LP{nlw_}, st)));
     SWC_TRY((pass<K_C3, 2>(LdPlain<T, double>{psiq_}, SP{pout})));
   } else {
     // mixed engine: FP64-lean density update fused into the Nl transform, then the CN update
     LdNlMixed ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
                  rho_, frhot_, rhof_, rho_off_, (float)p_.dt, (float)kp_, (float)p_.zeta, (float)p_.rho_0,
-                 (float)rho_off_};
+                 (float)rho_off_, f_[0]};
     SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
     SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
     SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
     // the CN update as a full-occupancy pointwise kernel (it writes the FP32 copy psiqf of
     // the new psiq), then a plain TMA-fed pass from that copy
-    LdNlUpdate lu{nlw_, dq_, nlq_, psiq_, psiq_old_, inv_c2f_, psiqf_, (float)(p_.dt / 2 * scale_), first ? 1 : 0};
+    LdNlUpdate lu{nlw_, nullptr, nlq_, psiq_, psiq_old_, inv_c2f_, psiqf_, (float)(p_.dt / 2 * scale_), first ? 1 : 0,
+                  g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt * rho_m_,
+                  p_.dt / 2 * scale_};
     nl_update_kernel<<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_.ng, lu);
     SWC_CK(cudaGetLastError());
     ++launches_;

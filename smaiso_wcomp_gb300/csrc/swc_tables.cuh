@@ -124,6 +124,9 @@ cudaError_t launch_pair(const Grid& g, const R2RTables<float>& tb, cudaStream_t 
   return cudaGetLastError();
 }
 
+template <class F> struct IsLdMul : std::false_type {};
+template <class M> struct IsLdMul<LdMul<M>> : std::true_type {};
+
 // Launch one axis pass on `stream` (in place or out of place per the functors): for
 // line lengths 64..512 the compile-time kernels (FP32: two lines per thread with packed
 // arithmetic; FP64: one line per thread group), the runtime one otherwise.
@@ -142,6 +145,24 @@ cudaError_t launch_pass(const Grid& g, const R2RTables<U>& tb, cudaStream_t stre
       return launch_tma<512, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul);
     if (n == 64 && tma_pass_supported<64>(g, axis))
       return launch_tma<64, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul);
+  } else if constexpr (std::is_same<U, float>::value && IsLdMul<LD>::value && AX == 2 && KIND == K_C3) {
+    // plain FP32 input times a pointwise multiplier: TMA-fed, applied to the staged tile
+    if (n == 256 && tma_pass_supported<256>(g, axis))
+      return launch_tma<256, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul, ld.m);
+    if (n == 128 && tma_pass_supported<128>(g, axis))
+      return launch_tma<128, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul, ld.m);
+    if (n == 512 && tma_pass_supported<512>(g, axis))
+      return launch_tma<512, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul, ld.m);
+    if (n == 64 && tma_pass_supported<64>(g, axis))
+      return launch_tma<64, KIND, AX, ST, MUL>(g, tb, stream, ld.p, st, mul, ld.m);
+    if (n == 256 && pair_pass_supported<256>(g, axis))
+      return launch_pair<256, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 128 && pair_pass_supported<128>(g, axis))
+      return launch_pair<128, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 512 && pair_pass_supported<512>(g, axis))
+      return launch_pair<512, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
+    if (n == 64 && pair_pass_supported<64>(g, axis))
+      return launch_pair<64, KIND, AX, LD, ST, MUL>(g, tb, stream, ld, st, mul);
   } else if constexpr (std::is_same<U, float>::value) {
     // fused FP32 loaders: two lines per thread, direct loads
     if (n == 256 && pair_pass_supported<256>(g, axis))

@@ -56,6 +56,13 @@ class Engine:
             rp = abi.as_dptr(rho)
         _check(self.lib, self.lib.swc_set_state(self._h, abi.as_dptr(psi), rp), "swc_set_state")
 
+    def set_state_ic(self, kind, **fields):
+        """swc_set_state_ic: the initial state generated on the device (swc_default_ic of
+        `kind`, with the given swc_ic fields overridden)."""
+        ic = default_ic(self.p, kind, lib=self.lib, **fields)
+        _check(self.lib, self.lib.swc_set_state_ic(self._h, ctypes.byref(ic)), "swc_set_state_ic")
+        return ic
+
     def step(self, n=1, check=True):
         rc = self.lib.swc_step(self._h, int(n))
         if check:
@@ -118,8 +125,10 @@ class Engine:
         _check(self.lib, self.lib.swc_last_step_launches(self._h, ctypes.byref(n)), "swc_last_step_launches")
         return n.value
 
-    def backward(self, dpsi=None, drho=None, want_psi0=True, want_rho0=False):
-        """swc_backward: gradients of a loss with dL/dpsi(T) = dpsi, dL/drho(T) = drho."""
+    def backward(self, dpsi=None, drho=None, want_psi0=True, want_rho0=False, energy_lambda=0.0):
+        """swc_backward: gradients of a loss with dL/dpsi(T) = dpsi, dL/drho(T) = drho;
+        energy_lambda != 0: swc_backward_energy, the loss plus energy_lambda times the
+        free-energy diagnostic of the last step."""
         n = self.shape
         dp = None if dpsi is None else np.ascontiguousarray(dpsi, dtype=np.float64).reshape(n)
         dr = None if drho is None else np.ascontiguousarray(drho, dtype=np.float64).reshape(n)
@@ -127,8 +136,12 @@ class Engine:
         o_rho = np.empty(n) if want_rho0 else None
         g = abi.SwcGrad()
         ptr = lambda a: None if a is None else abi.as_dptr(a)  # noqa: E731
-        _check(self.lib, self.lib.swc_backward(self._h, ptr(dp), ptr(dr), ptr(o_psi), ptr(o_rho),
-                                               ctypes.byref(g)), "swc_backward")
+        if energy_lambda:
+            _check(self.lib, self.lib.swc_backward_energy(self._h, float(energy_lambda), ptr(dp), ptr(dr), ptr(o_psi),
+                                                          ptr(o_rho), ctypes.byref(g)), "swc_backward_energy")
+        else:
+            _check(self.lib, self.lib.swc_backward(self._h, ptr(dp), ptr(dr), ptr(o_psi), ptr(o_rho),
+                                                   ctypes.byref(g)), "swc_backward")
         out = g.as_dict()
         out["psi0"], out["rho0"] = o_psi, o_rho
         return out
@@ -138,6 +151,18 @@ class Engine:
 
     def load(self, path):
         _check(self.lib, self.lib.swc_load(self._h, str(path).encode()), "swc_load")
+
+
+def default_ic(params, kind, lib=None, **fields):
+    """swc_default_ic of `kind` for the grid of `params`, with fields overridden."""
+    lib = lib or abi.load_library()
+    ic = abi.SwcIc()
+    _check(lib, lib.swc_default_ic(ctypes.byref(params), int(kind), ctypes.byref(ic)), "swc_default_ic")
+    for k, v in fields.items():
+        if not hasattr(ic, k):
+            raise AttributeError(f"swc_ic has no field {k}")
+        setattr(ic, k, v)
+    return ic
 
 
 def device_fma_peak(precision, lib=None):

@@ -7,7 +7,8 @@ stated number of MPI ranks, and stores the sampled fields, their norms and the
 full-precision diagnostics. Needs the reference source (default
 /root/reference/smaiso-wcomp.cpp, or SWC_REFERENCE_SRC).
 
-Run: python tests/golden/make_ref_fixtures.py
+Run: python tests/golden/make_ref_fixtures.py [--all]
+(without --all, the cases already in the file are kept and only new ones are run)
 """
 import os
 import sys
@@ -25,12 +26,20 @@ import ref_cases  # noqa: E402
 
 
 def main():
+    path = os.path.join(HERE, "ref_fixtures.npz")
     out = {}
+    if "--all" not in sys.argv and os.path.exists(path):
+        out = dict(np.load(path))
     for case, c in ref_cases.CASES.items():
+        if f"{case}.diag" in out:
+            continue
         p = default_params(*c["shape"])
         d = derived(p)
-        prof = ref_cases.profiles(case, d["dx"], d["dz"])
-        psi0 = ref_cases.initial_psi(prof, c["shape"], c["seed"], c["noise"])
+        if c["ic"] == "ref":   # the reference's own initial state: no psi file
+            prof, psi0 = {}, None
+        else:
+            prof = ref_cases.profiles(case, d["dx"], d["dz"])
+            psi0 = ref_cases.initial_psi(prof, c["shape"], c["seed"], c["noise"])
         res = ref_run.run(c["shape"], c["ranks"], c["steps"], sorted(c["dumps"]), psi0=psi0)
         for k, v in prof.items():
             out[f"{case}.{k}"] = v
@@ -43,7 +52,6 @@ def main():
                 out[f"{case}.s{step}.{f}.norm"] = np.float64(np.linalg.norm(full))
         print(f"{case}: {c['shape']} x {c['ranks']} ranks, {c['steps']} steps, "
               f"diag rows {len(res['diag'])}", flush=True)
-    path = os.path.join(HERE, "ref_fixtures.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB)")
 

@@ -11,7 +11,9 @@ with IEEE additions and products only:
     psi0[i,j,k] = (P[k] + (X[i] * Y[j]) * Z[k]) + noise[i,j,k]
     noise = SplitMix64 uniform on [-a, a] (smaiso_wcomp_gb300.ic.uniform_noise)
 "sep" cases carry a 3D perturbation at the interface (X, Y, Z); "flat" is the 64^3
-flat-interface state (P only; a = 1e-4, seed 1001).
+flat-interface state (P only; a = 1e-4, seed 1001); "ref" is the reference's own
+initial state (the band of smaiso-wcomp.cpp:575-590, no file read), rebuilt here by
+smaiso_wcomp_gb300.ic.reference_band.
 
 At each dump step the fixture holds, per field, its values at `sample` seeded
 point indices (every point when sample is None) and the whole field's L2 norm.
@@ -36,6 +38,9 @@ CASES = {
     # 1e-4, seed 1001) at the reference's dt = 0.001, 500 steps.
     "flat64_p2": dict(shape=(64, 64, 64), ranks=2, steps=500, dumps={100: 1024, 500: 1024},
                       ic="flat", seed=1001, noise=1e-4),
+    # the reference's own band initial state, 16 x 16 x 64
+    "band_p2": dict(shape=(16, 16, 64), ranks=2, steps=100, dumps={1: 1024, 100: 1024},
+                    ic="ref", seed=2006, noise=0.0),
 }
 
 FIELDS = [
@@ -98,8 +103,13 @@ class Fixture:
         self.spec = CASES[case]
         self.shape = self.spec["shape"]
         self._z = npz
-        prof = {k: npz[f"{case}.{k}"] for k in "PXYZ"}
-        self.psi0 = initial_psi(prof, self.shape, self.spec["seed"], self.spec["noise"])
+        if self.spec["ic"] == "ref":
+            from smaiso_wcomp_gb300.abi import default_params
+            from smaiso_wcomp_gb300.ic import reference_band
+            self.psi0 = reference_band(default_params(*self.shape))[0]
+        else:
+            prof = {k: npz[f"{case}.{k}"] for k in "PXYZ"}
+            self.psi0 = initial_psi(prof, self.shape, self.spec["seed"], self.spec["noise"])
         self.diag = npz[f"{case}.diag"]   # rows: step, L1, sumA, sumB, mass, energy
 
     def index(self, step):

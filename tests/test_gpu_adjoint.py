@@ -72,6 +72,65 @@ def test_adjoint_matches_finite_differences(lib, shape, ds, nsteps, ckpt):
     assert not bad, bad
 
 
+def energy_loss(e, wp, lam):
+    return float(np.sum(wp * e.field("psi"))) + lam * e.diagnostics()["energy"]
+
+
+@pytest.mark.parametrize("ckpt", [2, -1])
+def test_energy_term_adjoint_matches_finite_differences(lib, ckpt):
+    """swc_backward_energy: L = sum(w psi(T)) + lambda E(T), E(T) the free-energy
+    diagnostic of the last step (its stale dfDlapPsi and the step's filtered amplitude),
+    against 4th-order central differences of the FP64 forward: directional derivatives
+    along psi0 and rho0 and the five coefficient gradients within 1e-6. A second call
+    returns the same gradients (the last step's dfDlapPsi and amplitude are put back)."""
+    shape, ds, nsteps, lam = (16, 16, 16), 2, 5, 0.7
+    rng = np.random.default_rng(11)
+    p = abi.default_params(*shape, rho_0=0.8, divv_switch=ds, adjoint_ckpt=ckpt, ref_ranks=2)
+    psi0, rho0 = ic.undulated_interface(p, sigma=1e-2)
+    wp = rng.standard_normal(shape)
+
+    def L_run(q, a, b):
+        with Engine(q) as e:
+            e.set_state(a, b)
+            e.step(nsteps)
+            return energy_loss(e, wp, lam)
+
+    with Engine(p) as e:
+        e.set_state(psi0, rho0)
+        e.step(nsteps)
+        L0 = energy_loss(e, wp, lam)
+        g = e.backward(dpsi=wp, want_psi0=True, want_rho0=True, energy_lambda=lam)
+        g2 = e.backward(dpsi=wp, want_psi0=True, want_rho0=True, energy_lambda=lam)
+        g0 = e.backward(dpsi=wp, want_psi0=True, want_rho0=True)
+    for key in ("psi0", "rho0"):
+        assert np.array_equal(g[key], g2[key]), key
+        assert not np.allclose(g[key], g0[key]), key   # the energy term contributes
+    # 4th-order differences: truncation O(h^4), FP64 roundoff about 1e-14 |L| / h, the
+    # floor under the 1e-6 bar. psi0 (L strongly nonlinear in it) at h = 1e-4; rho0 at
+    # h = 1e-3: its directional derivative is ~5e-6 |L| (the relax phase resets rho, REF:1371)
+    for key, h in (("psi0", 1e-4), ("rho0", 1e-3)):
+        d = rng.standard_normal(shape)
+        at = lambda t: L_run(p, psi0 + t * d, rho0) if key == "psi0" else L_run(p, psi0, rho0 + t * d)  # noqa: E731
+        fd = (8 * (at(h) - at(-h)) - (at(2 * h) - at(-2 * h))) / (12 * h)
+        ad = float(np.sum(g[key] * d))
+        assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-14 * abs(L0) / h, (key, ad, fd)
+    errs = {}
+    for name in COEFFS:
+        v = getattr(p, name)
+        h = 1e-3 * max(abs(v), 1e-3)
+
+        def L_at(x):
+            q = abi.SwcParams.from_buffer_copy(p)
+            setattr(q, name, x)
+            return L_run(q, psi0, rho0)
+
+        fd = (8 * (L_at(v + h) - L_at(v - h)) - (L_at(v + 2 * h) - L_at(v - 2 * h))) / (12 * h)
+        errs[name] = (g[name], fd, abs(g[name] - fd) / max(abs(fd), 1e-9))
+        assert g2[name] == g[name], name
+    bad = {k: v for k, v in errs.items() if not v[2] <= 1e-6}
+    assert not bad, bad
+
+
 def test_backward_needs_checkpoints_and_fp64(lib):
     from smaiso_wcomp_gb300.engine import SwcError
     with Engine(abi.default_params(8)) as e:
