@@ -69,7 +69,8 @@ def parse():
     ap.add_argument("--energy-lambda", type=float, default=1.0,
                     help="adjoint workloads: weight of the free-energy diagnostic E(T) in the calibration loss")
     ap.add_argument("--divv-switch", type=int, default=None,
-                    help="adjoint workloads: relax-phase length instead of the reference's 50")
+                    help="adjoint workloads and --only mixed/fp64: relax-phase length instead of the "
+                         "reference's 50 (short profiling runs)")
     ap.add_argument("--only", choices=["mixed", "fp64", "pass"], default=None,
                     help="profiling mode: run only this engine's warm-up + timed steps and print its timing")
     return ap.parse_args()
@@ -230,8 +231,10 @@ def pass_roofline(precision, reps=5, fields=8):
     distinct fields (8 x 67 MB FP32 = 537 MB, four times the 129 MB L2) each take a
     DCT-II axis pass, axis-major (all z passes, then all y, then all x), so every pass
     reads its field from DRAM and pays for the write-back of an earlier pass's output,
-    as the passes of a step do. Returns the mean time of one pass (ms), the per-axis
-    means and the algorithmic bytes of one pass (one read + one write of the field)."""
+    as the passes of a step do; each axis's passes are replayed from a CUDA graph, as a
+    step's are (the gaps between them included). Returns the mean time of one pass (ms),
+    the per-axis means and the algorithmic bytes of one pass (one read + one write of
+    the field)."""
     import torch
     from smaiso_wcomp_gb300 import abi
     from smaiso_wcomp_gb300.engine import R2RPlan
@@ -243,12 +246,20 @@ def pass_roofline(precision, reps=5, fields=8):
     s = torch.cuda.Stream()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     per_axis = [[], [], []]
+    # each axis's `fields` launches captured in one CUDA graph, as a step's passes are
+    # (no host launch overhead between the passes)
+    graphs = []
+    for axis in (2, 1, 0):
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr, stream=s, capture_error_mode="relaxed"):
+            for x in xs:
+                plan.execute_axis(axis, x.data_ptr(), s.cuda_stream)
+        graphs.append(gr)
     with torch.cuda.stream(s):
         for r in range(reps + 2):
             evs[0].record(s)
-            for q, axis in enumerate((2, 1, 0)):
-                for x in xs:
-                    plan.execute_axis(axis, x.data_ptr(), s.cuda_stream)
+            for q, gr in enumerate(graphs):
+                gr.replay()
                 evs[q + 1].record(s)
             evs[3].synchronize()
             for x in xs:
@@ -259,7 +270,7 @@ def pass_roofline(precision, reps=5, fields=8):
     per_axis = [float(np.median(t)) for t in per_axis]
     elem = 4 if precision == abi.SWC_PREC_MIXED else 8
     alg_bytes = 2 * N ** 3 * elem
-    del xs
+    del graphs, xs
     plan.close()
     return float(np.mean(per_axis)), per_axis, alg_bytes
 
@@ -556,7 +567,10 @@ def main():
         return
     if args.only:
         prec = abi.SWC_PREC_MIXED if args.only == "mixed" else abi.SWC_PREC_FP64
-        e, ms, launches, _ = time_engine(make_params(prec, device=local), psi, rho, args.warmup, args.steps)
+        po = make_params(prec, device=local)
+        if args.divv_switch is not None:   # profiling runs: a shorter relax phase before the timed steps
+            po.divv_switch = args.divv_switch
+        e, ms, launches, _ = time_engine(po, psi, rho, args.warmup, args.steps)
         print(json.dumps({"only": args.only, "steps": args.steps, "ms_per_step": ms / args.steps,
                           "steps_per_s": args.steps / (ms * 1e-3), "gpu_launches": launches}), flush=True)
         e.close()

@@ -136,23 +136,25 @@ template <int RELAX> struct LapMul {
 
 // Last pass of dfDlapPsi in the mixed engine's normal phase: stores dfDlapPsi and
 // rho * dfDlapPsi (REF:1321, with rho = rhof + off), so the Delta(rho L) transform
-// starts with a plain TMA-fed pass.
+// starts with a plain TMA-fed pass. rhof is not written by the pass: its loads take
+// the read-only path, so they need not wait for the stores issued before them.
 struct StLpsiRhoL {
   float *lpsi, *rhoL;
   const float* rhof;
   float off;
   __device__ __forceinline__ void operator()(int, int, int, long long idx, float v) const {
+    const float r = __ldg(rhof + idx);
     lpsi[idx] = v;
-    rhoL[idx] = (rhof[idx] + off) * v;
+    rhoL[idx] = (r + off) * v;
   }
   __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const {
+    const float2 r = ld2g(rhof, idx);
     st2v(lpsi, idx, v);
-    const float2 r = ld2v(rhof, idx);
     st2v(rhoL, idx, make_float2((r.x + off) * v.x, (r.y + off) * v.y));
   }
   __device__ __forceinline__ void quad(int, int, int, long long idx, float4 v) const {
+    const float4 r = ld4g(rhof, idx);
     st4v(lpsi, idx, v);
-    const float4 r = ld4v(rhof, idx);
     st4v(rhoL, idx, make_float4((r.x + off) * v.x, (r.y + off) * v.y, (r.z + off) * v.z, (r.w + off) * v.w));
   }
 };
@@ -164,21 +166,6 @@ template <typename T> struct LdRhoL {
   T off;
   __device__ __forceinline__ T operator()(int, int, int, long long idx) const {
     return ((T)rho[idx] + off) * lpsi[idx];
-  }
-};
-
-// Store v + other[idx] (a running sum over passes, read where it is written).
-template <typename T> struct StAdd {
-  T* p;
-  const T* other;
-  __device__ __forceinline__ void operator()(int, int, int, long long idx, T v) const { p[idx] = v + other[idx]; }
-  __device__ __forceinline__ void pair(int, int, int, long long idx, float2 v) const {
-    const float2 o = ld2v(other, idx);
-    st2v(p, idx, make_float2(v.x + o.x, v.y + o.y));
-  }
-  __device__ __forceinline__ void quad(int, int, int, long long idx, float4 v) const {
-    const float4 o = ld4v(other, idx);
-    st4v(p, idx, make_float4(v.x + o.x, v.y + o.y, v.z + o.z, v.w + o.w));
   }
 };
 
@@ -262,7 +249,8 @@ struct LdNlMixed {
   float *frho, *rhof;
   double offd;
   float dt, kp, zeta, rho0, off;
-  const float* mdivf;  // -grad.f in real space (REF:2078-2090, the transposed-derivative passes)
+  const float *mdfx, *mdfy, *mdfz;  // -grad.f in real space by component (REF:2078-2090, the
+                                     // transposed-derivative passes): Nl += their sum
   __device__ __forceinline__ float point(float ux, float uy, float uz, float gx, float gy, float gz, float dv,
                                          float m, float a, float ps, float px, float py, float pz, float rf,
                                          float fp, double& r, float& s, float& rfn) const {
@@ -281,7 +269,7 @@ struct LdNlMixed {
     rho[idx] = r;
     frho[idx] = sr;
     rhof[idx] = rfn;
-    return out + mdivf[idx];
+    return out + ((mdfx[idx] + mdfy[idx]) + mdfz[idx]);
   }
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
@@ -301,8 +289,9 @@ struct LdNlMixed {
     *reinterpret_cast<double2*>(rho + idx + 2) = make_double2(r[2], r[3]);
     st4v(frho, idx, make_float4(sr[0], sr[1], sr[2], sr[3]));
     st4v(rhof, idx, make_float4(rfn[0], rfn[1], rfn[2], rfn[3]));
-    const float4 df = ld4g(mdivf, idx);
-    return make_float4(o[0] + df.x, o[1] + df.y, o[2] + df.z, o[3] + df.w);
+    const float4 dx = ld4g(mdfx, idx), dy = ld4g(mdfy, idx), dz = ld4g(mdfz, idx);
+    return make_float4(o[0] + ((dx.x + dy.x) + dz.x), o[1] + ((dx.y + dy.y) + dz.y), o[2] + ((dx.z + dy.z) + dz.z),
+                       o[3] + ((dx.w + dy.w) + dz.w));
   }
 };
 

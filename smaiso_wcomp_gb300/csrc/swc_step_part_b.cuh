@@ -48,12 +48,12 @@ template <typename T> int StepEngine<T>::enqueue_part_b(bool relax, bool first, 
     // mixed forward transform of f_a (DST-II along a). Along the two other axes
     // DCT-III DCT-II = 2n: component a is (1/2n_a) DCT-III_a(q_a(m) z_(m-1)), z = DST-II_a f_a,
     // and q_a(m) = Vs_a(m-1) -- minus the transposed-derivative pass DCT-III_a M^T DST-II_a
-    // with M the derivative's multiplier -Vs/(2n). One pass per component, summed in
-    // place (f_[0] ends with -grad.f), read by the first pass of the Nl transform.
+    // with M the derivative's multiplier -Vs/(2n). One pass per component, in place;
+    // the first pass of the Nl transform reads the three and adds them.
     const T cx = (T)(1.0 / (2.0 * g_.nx)), cy = (T)(1.0 / (2.0 * g_.ny)), cz = (T)(1.0 / (2.0 * g_.nz));
     SWC_TRY((pass<K_DERIVT, 2>(LP{f_[2]}, SP{f_[2]}, MulDeriv<T>{vs_[2], cz, 2})));
-    SWC_TRY((pass<K_DERIVT, 1>(LP{f_[1]}, StAdd<T>{f_[1], f_[2]}, MulDeriv<T>{vs_[1], cy, 1})));
-    SWC_TRY((pass<K_DERIVT, 0>(LP{f_[0]}, StAdd<T>{f_[0], f_[1]}, MulDeriv<T>{vs_[0], cx, 0})));
+    SWC_TRY((pass<K_DERIVT, 1>(LP{f_[1]}, SP{f_[1]}, MulDeriv<T>{vs_[1], cy, 1})));
+    SWC_TRY((pass<K_DERIVT, 0>(LP{f_[0]}, SP{f_[0]}, MulDeriv<T>{vs_[0], cx, 0})));
   }
   // S8 + S9 (REF:1468-1974); the mixed engine's Stokes kernel also writes div v-hat (S10)
   // and writes v_irr itself only for the adjoint's tape (the steps that keep v_sol)

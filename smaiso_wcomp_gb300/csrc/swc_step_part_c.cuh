@@ -52,7 +52,7 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
     // mixed engine: FP64-lean density update fused into the Nl transform, then the CN update
     LdNlMixed ld{v_[0], v_[1], v_[2], gr_[0], gr_[1], gr_[2], divv_, mu_, amp_f_, psi_, gp_[0], gp_[1], gp_[2],
                  rho_, frhot_, rhof_, rho_off_, (float)p_.dt, (float)kp_, (float)p_.zeta, (float)p_.rho_0,
-                 (float)rho_off_, f_[0]};
+                 (float)rho_off_, f_[0], f_[1], f_[2]};
     SWC_TRY((pass<K_C2, 2>(ld, SP{nlw_})));
     SWC_TRY((pass<K_C2, 1>(LP{nlw_}, SP{nlw_})));
     SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
