@@ -490,6 +490,17 @@ template <typename T> struct V4 {
       v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
     }
   }
+  // the same through the read-only data path: for inputs the kernel does not write
+  __device__ __forceinline__ void loadg(const T* p, long long idx) {
+    if constexpr (sizeof(T) == 4) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p + idx));
+      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+      const double2 q0 = __ldg(reinterpret_cast<const double2*>(p + idx));
+      const double2 q1 = __ldg(reinterpret_cast<const double2*>(p + idx + 2));
+      v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+    }
+  }
   __device__ __forceinline__ void store(T* p, long long idx) const {
     if constexpr (sizeof(T) == 4) {
       *reinterpret_cast<float4*>(p + idx) = make_float4(v[0], v[1], v[2], v[3]);
@@ -499,6 +510,12 @@ template <typename T> struct V4 {
     }
   }
 };
+template <typename T> __device__ __forceinline__ T ldg1(const T* p) { return __ldg(p); }
+// 1/x for x a positive normal number (|q|^2 of a nonzero mode). FP32: __fdividef's
+// approximate reciprocal (within 2 ulp), without the special-case path of the
+// correctly rounded division; FP64: the division itself.
+__device__ __forceinline__ float rcp_pos(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double rcp_pos(double x) { return 1.0 / x; }
 
 // Four consecutive points per thread (n^3 is a multiple of 4: every extent is >= 4).
 // The mixed engine takes its FP32 density from rhof + off and touches the FP64 rho
@@ -617,39 +634,50 @@ template <typename T> struct StokesArgs {
 // for j', k' < n-1, REF:1584, 1760-1812) and the rank-count quirk of v_z at k' = 0
 // (REF:1932):
 //   div v-hat = scale/((lambda + 2 nu) |q|^2) sum_valid q_a^2 (fg + D G_a / |q|^2).
-template <typename T, bool DIVV> __global__ void __launch_bounds__(256) stokes_kernel(Grid g, StokesArgs<T> a) {
+// FP32: three 256-thread blocks per SM (80 registers; uncapped it takes 95 and runs
+// two blocks, measured slower at 256^3: 172 us against 132 us per launch).
+template <typename T, bool DIVV>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) stokes_kernel(Grid g, StokesArgs<T> a) {
   const int idx = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (idx >= (int)g.ng) return;
   const int k0 = idx & (g.nz - 1), j = (idx >> g.lz) & (g.ny - 1), i = idx >> (g.ly + g.lz);
   const int sx = 1 << (g.ly + g.lz), sy = g.nz;
   const bool has_next = k0 + 4 < g.nz;  // k0 + 4 is in this row
+  const bool ip = i > 0, jp = j > 0, kp = k0 != 0;
+  // The inputs are read-only here: every load takes the read-only path, so none has to
+  // wait for the output stores issued before it.
   V4<T> Sxc, Syc, Szc, qz, szv, gqz, gsz;
-  Sxc.load(a.Sx, idx);
-  Syc.load(a.Sy, idx);
-  Szc.load(a.Sz, idx);
-  qz.load(a.vqz, k0);
-  szv.load(a.vsz, k0);
-  gqz.load(a.gqz, k0);
-  gsz.load(a.gsz, k0);
+  Sxc.loadg(a.Sx, idx);
+  Syc.loadg(a.Sy, idx);
+  Szc.loadg(a.Sz, idx);
+  qz.loadg(a.vqz, k0);
+  szv.loadg(a.vsz, k0);
+  gqz.loadg(a.gqz, k0);
+  gsz.loadg(a.gsz, k0);
   const T qxi = a.vqx[i], qyj = a.vqy[j];
+  // plane i-1, row j-1 and the point's own row: read by v_y, v_z and div v-hat
+  V4<T> Sxm = V4<T>::zero(), Sym = V4<T>::zero(), F3, E3;
+  if (ip) Sxm.loadg(a.Sx, idx - sx);
+  if (jp) Sym.loadg(a.Sy, idx - sy);
+  F3.loadg(a.fgrad, idx);
+  E3.loadg(a.ener, idx);
   // v_x on the x-sine grid, i < nx-1 (REF:1581-1699)
   V4<T> vs, vi;
   if (i < g.nx - 1) {
     const T sxi = a.vsx[i];
-    V4<T> Sy1, Szn, F1, E1;
-    if (j != 0) Sy1.load(a.Sy, idx + sx - sy);
-    else Sy1 = V4<T>::zero();
-    Szn.load(a.Sz, idx + sx);
-    const T Szp = (k0 != 0) ? a.Sz[idx + sx - 1] : (T)0;
-    F1.load(a.fgrad, idx + sx);
-    E1.load(a.ener, idx + sx);
+    V4<T> Sy1 = V4<T>::zero(), Szn, F1, E1;
+    if (jp) Sy1.loadg(a.Sy, idx + sx - sy);
+    Szn.loadg(a.Sz, idx + sx);
+    const T Szp = kp ? ldg1(a.Sz + idx + sx - 1) : (T)0;
+    F1.loadg(a.fgrad, idx + sx);
+    E1.loadg(a.ener, idx + sx);
     const T Gx = a.gqx[i + 1] * a.gqy[j], Gsx = a.gsx[i] * a.gqy[j];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const T Sz = (c == 0) ? Szp : Szn.v[c - 1];
       const T dot = sxi * Sxc.v[c] + qyj * Sy1.v[c] + qz.v[c] * Sz;
       const T mq2 = sxi * sxi + qyj * qyj + qz.v[c] * qz.v[c];
-      const T inv = (T)1 / mq2;
+      const T inv = rcp_pos(mq2);
       const T CM1 = a.scale * inv, CM2 = sxi * inv;
       const T fg = F1.v[c] + E1.v[c] * (Gx * gqz.v[c]);
       vs.v[c] = (CM1 * a.inv_nu) * (Sxc.v[c] - CM2 * dot);
@@ -664,69 +692,59 @@ template <typename T, bool DIVV> __global__ void __launch_bounds__(256) stokes_k
 #pragma unroll
   for (int c = 0; c < 4; ++c) vs.v[c] = vs.v[c] + vi.v[c];
   vs.store(a.vsumx, idx);
-  // v_y, v_z for j < ny-1, k < nz-1 (REF:1758-1974); other modes stay 0
+  // v_y, v_z for j < ny-1, k < nz-1 (REF:1758-1974); other modes stay 0. Only the last
+  // group of a row holds k = nz-1: its fourth results are computed from zero neighbours
+  // and then cleared.
   V4<T> ys = V4<T>::zero(), yi = V4<T>::zero(), zs = V4<T>::zero(), zi = V4<T>::zero();
   if (j < g.ny - 1) {
     const T syj = a.vsy[j];
-    V4<T> Sx2, Szn2, F2, E2, Sxm, Sym, F3, E3;
-    if (i > 0) Sx2.load(a.Sx, idx - sx + sy);
-    else Sx2 = V4<T>::zero();
-    Szn2.load(a.Sz, idx + sy);
-    const T Szp2 = (k0 != 0) ? a.Sz[idx + sy - 1] : (T)0;
-    F2.load(a.fgrad, idx + sy);
-    E2.load(a.ener, idx + sy);
+    V4<T> Sx2 = V4<T>::zero(), Szn2, F2, E2;
+    if (ip) Sx2.loadg(a.Sx, idx - sx + sy);
+    Szn2.loadg(a.Sz, idx + sy);
+    const T Szp2 = kp ? ldg1(a.Sz + idx + sy - 1) : (T)0;
+    F2.loadg(a.fgrad, idx + sy);
+    E2.loadg(a.ener, idx + sy);
     // z: Sx[idx - sx + 1], Sy[idx - sy + 1], fgrad/ener[idx + 1] (k + 1 in the same row)
-    T Sxn = (T)0, Syn = (T)0;
-    if (i > 0) {
-      Sxm.load(a.Sx, idx - sx);
-      if (has_next) Sxn = a.Sx[idx - sx + 4];
-    } else {
-      Sxm = V4<T>::zero();
+    T Sxn = (T)0, Syn = (T)0, Fn = (T)0, En = (T)0, gzn = (T)0;
+    if (has_next) {
+      if (ip) Sxn = ldg1(a.Sx + idx - sx + 4);
+      if (jp) Syn = ldg1(a.Sy + idx - sy + 4);
+      Fn = ldg1(a.fgrad + idx + 4);
+      En = ldg1(a.ener + idx + 4);
+      gzn = a.gqz[k0 + 4];
     }
-    if (j != 0) {
-      Sym.load(a.Sy, idx - sy);
-      if (has_next) Syn = a.Sy[idx - sy + 4];
-    } else {
-      Sym = V4<T>::zero();
-    }
-    const T Fn = has_next ? a.fgrad[idx + 4] : (T)0, En = has_next ? a.ener[idx + 4] : (T)0;
-    F3.load(a.fgrad, idx);
-    E3.load(a.ener, idx);
     const T Gy = a.gqx[i] * a.gqy[j + 1], Gsy = a.gqx[i] * a.gsy[j], Gz = a.gqx[i] * a.gqy[j];
-    const bool off_first_slab = (i % a.block) != 0;
+    // REF:1932: off the first slab of a rank, the k = 0, j > 0 modes use CM1y's filter
+    const bool q1 = !kp && jp && (i % a.block) != 0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const int k = k0 + c;
-      if (k < g.nz - 1) {
-        const T szk = szv.v[c];
-        {
-          const T Sz = (c == 0) ? Szp2 : Szn2.v[c - 1];
-          const T dot = qxi * Sx2.v[c] + syj * Syc.v[c] + qz.v[c] * Sz;
-          const T mq2 = qxi * qxi + syj * syj + qz.v[c] * qz.v[c];
-          const T inv = (T)1 / mq2;
-          const T CM1 = a.scale * inv, CM2 = syj * inv;
-          const T fg = F2.v[c] + E2.v[c] * (Gy * gqz.v[c]);
-          ys.v[c] = (CM1 * a.inv_nu) * (Syc.v[c] - CM2 * dot);
-          yi.v[c] = (CM1 * a.inv_lam2nu) * (syj * fg + CM2 * dot * (Gsy * gqz.v[c]));
-        }
-        {
-          const T Sx = (c < 3) ? Sxm.v[c + 1] : Sxn;
-          const T Sy = (c < 3) ? Sym.v[c + 1] : Syn;
-          const T dot = qxi * Sx + qyj * Sy + szk * Szc.v[c];
-          const T mq2 = qxi * qxi + qyj * qyj + szk * szk;
-          const T inv = (T)1 / mq2;
-          const T CM1 = a.scale * inv, CM2 = szk * inv;
-          const T f1 = (c < 3) ? F3.v[c + 1] : Fn, e1 = (c < 3) ? E3.v[c + 1] : En;
-          const T gz1 = (c < 3) ? gqz.v[c + 1] : a.gqz[k + 1];
-          const T fg = f1 + e1 * (Gz * gz1);
-          // REF:1932: off the first slab of a rank, the k = 0, j > 0 modes use CM1y's filter
-          const bool q1 = (k == 0) && (j > 0) && off_first_slab;
-          const T G = q1 ? (Gsy * gqz.v[c]) : (Gz * gsz.v[c]);
-          zs.v[c] = (CM1 * a.inv_nu) * (Szc.v[c] - CM2 * dot);
-          zi.v[c] = (CM1 * a.inv_lam2nu) * (szk * fg + CM2 * dot * G);
-        }
+      const T szk = szv.v[c];
+      {
+        const T Sz = (c == 0) ? Szp2 : Szn2.v[c - 1];
+        const T dot = qxi * Sx2.v[c] + syj * Syc.v[c] + qz.v[c] * Sz;
+        const T mq2 = qxi * qxi + syj * syj + qz.v[c] * qz.v[c];
+        const T inv = rcp_pos(mq2);
+        const T CM1 = a.scale * inv, CM2 = syj * inv;
+        const T fg = F2.v[c] + E2.v[c] * (Gy * gqz.v[c]);
+        ys.v[c] = (CM1 * a.inv_nu) * (Syc.v[c] - CM2 * dot);
+        yi.v[c] = (CM1 * a.inv_lam2nu) * (syj * fg + CM2 * dot * (Gsy * gqz.v[c]));
+      }
+      {
+        const T Sx = (c < 3) ? Sxm.v[c + 1] : Sxn;
+        const T Sy = (c < 3) ? Sym.v[c + 1] : Syn;
+        const T dot = qxi * Sx + qyj * Sy + szk * Szc.v[c];
+        const T mq2 = qxi * qxi + qyj * qyj + szk * szk;
+        const T inv = rcp_pos(mq2);
+        const T CM1 = a.scale * inv, CM2 = szk * inv;
+        const T f1 = (c < 3) ? F3.v[c + 1] : Fn, e1 = (c < 3) ? E3.v[c + 1] : En;
+        const T gz1 = (c < 3) ? gqz.v[c + 1] : gzn;
+        const T fg = f1 + e1 * (Gz * gz1);
+        const T G = (c == 0 && q1) ? (Gsy * gqz.v[c]) : (Gz * gsz.v[c]);
+        zs.v[c] = (CM1 * a.inv_nu) * (Szc.v[c] - CM2 * dot);
+        zi.v[c] = (CM1 * a.inv_lam2nu) * (szk * fg + CM2 * dot * G);
       }
     }
+    if (!has_next) ys.v[3] = yi.v[3] = zs.v[3] = zi.v[3] = (T)0;
   }
   if (a.write_vsol) {
     ys.store(a.vsoly, idx);
@@ -744,41 +762,31 @@ template <typename T, bool DIVV> __global__ void __launch_bounds__(256) stokes_k
   ys.store(a.vsumy, idx);
   zs.store(a.vsumz, idx);
   if constexpr (DIVV) {
-    V4<T> sxm = V4<T>::zero(), sym = V4<T>::zero(), F, E, dv;
-    if (i > 0) sxm.load(a.Sx, idx - sx);
-    if (j > 0) sym.load(a.Sy, idx - sy);
-    F.load(a.fgrad, idx);
-    E.load(a.ener, idx);
-    const T szp = (k0 != 0) ? a.Sz[idx - 1] : (T)0;  // Sz(i, j, k0 - 1)
+    V4<T> dv;
+    const T szp = kp ? ldg1(a.Sz + idx - 1) : (T)0;  // Sz(i, j, k0 - 1)
     const T Gxy = a.gqx[i] * a.gqy[j];
     const T qx2 = qxi * qxi, qy2 = qyj * qyj;
     const bool off_first_slab = (i % a.block) != 0;
+    const T Gz1 = (jp && off_first_slab) ? a.gqx[i] * a.gsy[j] * a.gqz[0] : (T)0;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const int k = k0 + c;
-      const bool vx = i > 0, vy = (j > 0) && (k < g.nz - 1), vz = (k > 0) && (j < g.ny - 1);
-      T out = (T)0;
-      if (vx || vy || vz) {
-        const T qzk = qz.v[c];
-        const T qz2 = qzk * qzk;
-        const T Szm = (c == 0) ? szp : Szc.v[c - 1];
-        const T D = qxi * sxm.v[c] + qyj * sym.v[c] + qzk * Szm;
-        const T inv = (T)1 / (qx2 + qy2 + qz2);
-        const T G = Gxy * gqz.v[c];
-        const T fg = F.v[c] + E.v[c] * G;
-        const T t = D * inv;
-        T sum = (T)0;
-        if (vx) sum += qx2 * (fg + t * G);
-        if (vy) sum += qy2 * (fg + t * G);
-        if (vz) {
-          // v_z at k' = k - 1 = 0, j > 0, off a rank's first x slab: CM1y's filter
-          // gqx[i] gsy[j] gqz[k'] (REF:1932) instead of G
-          const T Gz = (k == 1 && j > 0 && off_first_slab) ? a.gqx[i] * a.gsy[j] * a.gqz[0] : G;
-          sum += qz2 * (fg + t * Gz);
-        }
-        out = a.scale * a.inv_lam2nu * inv * sum;
-      }
-      dv.v[c] = out;
+      const bool vx = ip, vy = jp && (k < g.nz - 1), vz = (k > 0) && (j < g.ny - 1);
+      const T qzk = qz.v[c];
+      const T qz2 = qzk * qzk;
+      const T Szm = (c == 0) ? szp : Szc.v[c - 1];
+      const T D = qxi * Sxm.v[c] + qyj * Sym.v[c] + qzk * Szm;
+      const T inv = rcp_pos(qx2 + qy2 + qz2);
+      const T G = Gxy * gqz.v[c];
+      const T fg = F3.v[c] + E3.v[c] * G;
+      const T t = D * inv;
+      // v_z at k' = k - 1 = 0, j > 0, off a rank's first x slab: CM1y's filter
+      // gqx[i] gsy[j] gqz[k'] (REF:1932) instead of G
+      const T Gz = (k == 1 && jp && off_first_slab) ? Gz1 : G;
+      const T w = fg + t * G;
+      const T sum = (vx ? qx2 : (T)0) * w + (vy ? qy2 : (T)0) * w + (vz ? qz2 * (fg + t * Gz) : (T)0);
+      // at i = j = k = 0 no term is valid (and |q|^2 = 0): the mode stays 0
+      dv.v[c] = (vx || vy || vz) ? a.scale * a.inv_lam2nu * inv * sum : (T)0;
     }
     dv.store(a.divv, idx);
   }
