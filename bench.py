@@ -666,7 +666,7 @@ def main():
 # DRAM bytes (read + write) per launch of the dominant kernel in the steady state that
 # pass_roofline times (mean of its z/y/x passes), from the ncu capture with
 # --cache-control none summarised in profiles/r2r_tma_fp32_n256_256cubed.md.
-PASS_TRAFFIC = {"fp32": 133.0e6}
+PASS_TRAFFIC = {"fp32": 132.3e6}
 
 
 def working_set_gb():
