@@ -589,7 +589,9 @@ __device__ __forceinline__ void pair_tables(const R2RTables<float>& tb, float4* 
 // entry the PC buffer holds, per kind and axis: x/y forward -> stage-1 output; z forward
 // -> the Makhoul-ordered z; x/y inverse -> the pre-processed, swapped Z; z inverse ->
 // the natural-order reals. Outputs go to global memory through `st`.
-template <int N, int KIND, int AX, class StoreOp, class MulOp>
+// ZT (z forward kinds): the loader has already run the first stage, of radix R1/2, so
+// the forward FFT ends with one stage of radix 2 R2.
+template <int N, int KIND, int AX, class StoreOp, class MulOp, bool ZT = false>
 __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int tj, int tid, PC* buf,
                                           const float4* sfft, const float2* spost, const float2* spre,
                                           const StoreOp& st, const MulOp& mul) {
@@ -604,15 +606,20 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   static_assert(ZU * NT == LP * NQ && ZU % ZC == 0, "z units");
   float2* rb2 = reinterpret_cast<float2*>(buf);
   const int lineA = 2 * (pair0 + lp);
-  if constexpr (!xy) {
+  if constexpr (!xy && !ZT) {
     if constexpr (fwd_in) pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
     else pair_pre<N>(buf, spre, lp, tj);
   }
 
   // ---------------- forward FFT + post ----------------
   if constexpr (fwd_in) {
-    pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
-    if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R3, R1 * Cf::R2, TPL, PP>(buf, sfft, lp, tj);
+    if constexpr (ZT) {
+      static_assert(Cf::R3 == 1, "two-stage plan");
+      pair_stage<M, 2 * Cf::R2, R1 / 2, TPL, PP>(buf, sfft, lp, tj);
+    } else {
+      pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
+      if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R3, R1 * Cf::R2, TPL, PP>(buf, sfft, lp, tj);
+    }
     if constexpr (xy && KIND != K_FILT && KIND != K_DERIV && KIND != K_DERIVT) {
       pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
       return;

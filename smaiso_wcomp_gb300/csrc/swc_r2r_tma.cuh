@@ -73,12 +73,18 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
 template <int N> struct TmaCfg {
   using Cf = PairCfg<N>;
   static constexpr int LINES = 2 * Cf::LP;              // lines per tile
-  static constexpr int TILE_BYTES = LINES * N * 4;      // staging buffer
+  static constexpr int TILE_BYTES = LINES * N * 4;      // bytes one tile copy delivers
   static constexpr int BOXN = (N < 256) ? N : 256;      // tensor box extent along the pass axis
   static constexpr int NBOX = N / BOXN;
+  // Row staging of z tiles (zrow_kind): line l of the tile in row (l >> 1) + LP (l & 1)
+  // of pitch N + 4 floats, so that lanes on consecutive line pairs read float4 a of
+  // their lines from consecutive 16-byte bank groups.
+  static constexpr bool ZROW = (N == 256 && Cf::R3 == 1 && LINES == 32);
+  static constexpr int ZPITCH = N + 4;
+  static constexpr int STAGE_BYTES = ZROW ? LINES * ZPITCH * 4 : TILE_BYTES;
   static_assert(TILE_BYTES < (1 << 20), "mbarrier transaction count");
   // staging tile + PC work buffer + tables + mbarrier
-  static constexpr size_t smem_bytes() { return (size_t)TILE_BYTES + Cf::smem_bytes() + 16; }
+  static constexpr size_t smem_bytes() { return (size_t)STAGE_BYTES + Cf::smem_bytes() + 16; }
 };
 
 // x/y: a tile must not straddle rows of the array (nz a multiple of the tile's lines).
@@ -109,9 +115,25 @@ __device__ __forceinline__ void tma_issue(const Grid& g, const CUtensorMap* map,
   }
 }
 
+// one warp: the z tile in row staging, one line per lane (a contiguous bulk copy of N
+// floats into row (l >> 1) + LP (l & 1)); lane 0 expects the tile's bytes first
+template <int N>
+__device__ __forceinline__ void tma_issue_zrow(const float* zsrc, int t, uint32_t sdst, uint32_t bar, int extra_tx,
+                                               int lane) {
+  using Tc = TmaCfg<N>;
+  static_assert(Tc::ZROW, "row staging");
+  if (lane == 0) mbar_expect_tx(bar, Tc::TILE_BYTES + extra_tx);
+  __syncwarp();
+  const uint32_t row = (uint32_t)((lane >> 1) + PairCfg<N>::LP * (lane & 1));
+  bulk_load(sdst + row * (uint32_t)(Tc::ZPITCH * 4), zsrc + ((size_t)t * Tc::LINES + lane) * N, N * 4, bar);
+}
+
 // LMUL: a pointwise multiplier of the loaded values (LdMul); the z pass of the inverse
 // cosine kind applies it as it reads the staged tile, the other forms take NoMul only.
-template <int N, int KIND, int AX, class StoreOp, class MulOp, class LMul>
+// ZT: z pass of a forward kind with the row staging (tma_issue_zrow): each thread loads
+// the inputs of its two first-stage butterflies straight from the staged tile, and the
+// line-pair re-layout of the z tile is not needed.
+template <int N, int KIND, int AX, class StoreOp, class MulOp, class LMul, bool ZT = false>
 __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                  const float* __restrict__ zsrc, Grid g,
                                                                  R2RTables<float> tb, StoreOp st, MulOp mul,
@@ -126,9 +148,10 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   constexpr int ZU = (LP * NQ) / NT;
   constexpr bool load_mul = !std::is_same<LMul, NoMul<float>>::value;
   static_assert(!load_mul || (AX == 2 && KIND == K_C3), "load multiplier: z pass of the inverse cosine kind only");
+  static_assert(!ZT || (AX == 2 && fwd_in && !load_mul && Tc::ZROW && R1 % 2 == 0), "z row staging");
   extern __shared__ __align__(128) unsigned char tma_smem[];
   const float* S = reinterpret_cast<const float*>(tma_smem);
-  PC* buf = reinterpret_cast<PC*>(tma_smem + Tc::TILE_BYTES);
+  PC* buf = reinterpret_cast<PC*>(tma_smem + Tc::STAGE_BYTES);
   float4* sfft = reinterpret_cast<float4*>(buf + M * PP);
   float2* spost = reinterpret_cast<float2*>(sfft + M);
   float2* spre = spost + 2 * (M + 1);
@@ -138,9 +161,12 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   const int lp = tid & (LP - 1), tj = tid >> Cf::LOG2LP;
 
   pair_tables<N, fwd_in, inv_out>(tb, sfft, spost, spre, tid);
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    if ((int)blockIdx.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, blockIdx.x, sdst, bar, tb.wait_extra_tx);
+  if (tid == 0) mbar_init(bar, 1);
+  if constexpr (ZT) {
+    __syncthreads();  // the barrier initialised before warp 0 starts the copies
+    if (tid < 32 && (int)blockIdx.x < ntiles) tma_issue_zrow<N>(zsrc, blockIdx.x, sdst, bar, tb.wait_extra_tx, tid);
+  } else {
+    if (tid == 0 && (int)blockIdx.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, blockIdx.x, sdst, bar, tb.wait_extra_tx);
   }
   __syncthreads();
 
@@ -164,7 +190,42 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
     }
     const int pair0 = t * LP;
     // ---- staging tile -> PC buffer ----
-    if constexpr (xy && fwd_in) {
+    if constexpr (ZT) {
+      // First Stockham stage of radix R = R1/2 (2 TPL butterflies per line pair, elements
+      // m = b + 2 TPL r), two butterflies per thread: b0 = tj and b1 = 2 TPL - 1 - tj. The
+      // float4 a of a line holds z_a = (x_4a, x_4a+2) and z_(M-1-a) = (x_4a+3, x_4a+1)
+      // (Makhoul order); for a = b + 2 TPL q (q < R/2), z_a is element q of butterfly b
+      // and z_(M-1-a) element R-1-q of butterfly 2 TPL - 1 - b, so the 2 R/2 float4 per
+      // line at a = b0 + 2 TPL q and a = b1 + 2 TPL q fill both butterflies.
+      constexpr int R = R1 / 2, TB = 2 * TPL, ZP4 = Tc::ZPITCH / 4;
+      const float4* S4 = reinterpret_cast<const float4*>(S);
+      const int b0 = tj, b1 = TB - 1 - tj;
+      PC v0[R], v1[R];
+      auto quad = [&](int a, int par) -> float4 {  // float4 a of line 2 lp + par
+        float4 x = S4[(lp + LP * par) * ZP4 + a];
+        if constexpr (KIND == K_S2 || KIND == K_DERIVT) {  // (-1)^p x_p: odd positions 4a+1, 4a+3
+          x.y = -x.y;
+          x.w = -x.w;
+        }
+        return x;
+      };
+#pragma unroll
+      for (int q = 0; q < R / 2; ++q) {
+        const float4 A0 = quad(b0 + TB * q, 0), B0 = quad(b0 + TB * q, 1);
+        const float4 A1 = quad(b1 + TB * q, 0), B1 = quad(b1 + TB * q, 1);
+        v0[q] = pmake(make_float2(A0.x, B0.x), make_float2(A0.z, B0.z));
+        v1[R - 1 - q] = pmake(make_float2(A0.w, B0.w), make_float2(A0.y, B0.y));
+        v1[q] = pmake(make_float2(A1.x, B1.x), make_float2(A1.z, B1.z));
+        v0[R - 1 - q] = pmake(make_float2(A1.w, B1.w), make_float2(A1.y, B1.y));
+      }
+      PDft<R>::run(v0);
+      PDft<R>::run(v1);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        buf[(b0 * R + r) * PP + lp] = v0[r];
+        buf[(b1 * R + r) * PP + lp] = v1[r];
+      }
+    } else if constexpr (xy && fwd_in) {
       // rows p of the tile hold the tile's lines side by side: (A, B) = one float2
       const float2* S2 = reinterpret_cast<const float2*>(S);
       PC v[R1];
@@ -253,9 +314,14 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
       }
     }
     __syncthreads();  // the staging tile is free: start the next one
-    if (tid == 0 && t + (int)gridDim.x < ntiles)
-      tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx);
-    pair_tail<N, KIND, AX>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
+    if constexpr (ZT) {
+      if (tid < 32 && t + (int)gridDim.x < ntiles)
+        tma_issue_zrow<N>(zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx, tid);
+    } else {
+      if (tid == 0 && t + (int)gridDim.x < ntiles)
+        tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx);
+    }
+    pair_tail<N, KIND, AX, StoreOp, MulOp, ZT>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
   }
 }
 
@@ -290,17 +356,11 @@ template <int N, int AX> inline cudaError_t make_pass_map(const Grid& g, const f
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-template <int N, int KIND, int AX, class ST, class MUL, class LMUL = NoMul<float>>
-cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t stream, const float* src, ST st,
-                       MUL mul, LMUL lmul = LMUL()) {
+template <int N, int KIND, int AX, class ST, class MUL, class LMUL, bool ZT>
+cudaError_t launch_tma_map(const Grid& g, const R2RTables<float>& tb, cudaStream_t stream, const CUtensorMap& map,
+                           const float* src, ST st, MUL mul, LMUL lmul) {
   using Tc = TmaCfg<N>;
-  CUtensorMap map;
-  std::memset(&map, 0, sizeof(map));
-  if constexpr (AX != 2) {
-    const cudaError_t e = make_pass_map<N, AX>(g, src, &map);
-    if (e != cudaSuccess) return e;
-  }
-  auto kern = r2r_tma_kernel<N, KIND, AX, ST, MUL, LMUL>;
+  auto kern = r2r_tma_kernel<N, KIND, AX, ST, MUL, LMUL, ZT>;
   const size_t smem = Tc::smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -312,6 +372,25 @@ cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t s
   const int blocks = std::min(ntiles, std::max(occ, 1) * sms);
   kern<<<blocks, PairCfg<N>::NT, smem, stream>>>(map, src, g, tb, st, mul, lmul, ntiles);
   return cudaGetLastError();
+}
+
+// Forward kinds along z take the row staging where the tile allows it (N = 256).
+template <int N, int KIND> constexpr bool zt_kind() {
+  return TmaCfg<N>::ZROW && (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+}
+
+template <int N, int KIND, int AX, class ST, class MUL, class LMUL = NoMul<float>>
+cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t stream, const float* src, ST st,
+                       MUL mul, LMUL lmul = LMUL()) {
+  CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  if constexpr (AX == 2 && zt_kind<N, KIND>() && std::is_same<LMUL, NoMul<float>>::value)
+    return launch_tma_map<N, KIND, AX, ST, MUL, LMUL, true>(g, tb, stream, map, src, st, mul, lmul);
+  if constexpr (AX != 2) {
+    const cudaError_t e = make_pass_map<N, AX>(g, src, &map);
+    if (e != cudaSuccess) return e;
+  }
+  return launch_tma_map<N, KIND, AX, ST, MUL, LMUL, false>(g, tb, stream, map, src, st, mul, lmul);
 }
 
 }  // namespace swc

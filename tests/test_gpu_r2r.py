@@ -99,12 +99,14 @@ def test_execute_on_device_buffer(lib):
     np.testing.assert_allclose(t.cpu().numpy(), plan(a), rtol=0, atol=1e-12 * np.abs(plan(a)).max())
 
 
-def test_tma_wait_that_runs_out_reports_status_and_recovers(lib, oracle_mod):
+@pytest.mark.parametrize("shape", [(256, 64, 64), (64, 64, 256)])
+def test_tma_wait_that_runs_out_reports_status_and_recovers(lib, oracle_mod, shape):
     """The TMA-fed pass's bounded wait: a wait that expects 16 bytes more than its copy
     delivers runs out after 4096 polls, the CTA sets the status flag and returns, the host
-    reads SWC_ERR_CUDA; the context stays usable and the next run is correct."""
+    reads SWC_ERR_CUDA; the context stays usable and the next run is correct. Every axis
+    takes the TMA-fed pass; in the second shape the z pass is the 256-point one whose
+    tile arrives as 32 line copies (row staging)."""
     from smaiso_wcomp_gb300.engine import SwcError
-    shape = (256, 64, 64)  # all three axes take the TMA-fed pass
     a = np.random.default_rng(11).standard_normal(shape)
     plan = R2RPlan(shape, (0, 0, 0), abi.SWC_PREC_MIXED, lib=lib)
     plan.set_wait_test(16, 4096)
