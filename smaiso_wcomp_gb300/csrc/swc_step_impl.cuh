@@ -362,7 +362,7 @@ template <typename T> struct StNlUpdate {
 // evaluated in FP64.
 struct LdNlUpdate {
   const float *nlw, *dq;
-  float* nlq;
+  const float* nlq;
   double *psiq, *psiq_old;
   const float* inv_c2;
   float* psiqf;
@@ -387,7 +387,7 @@ struct LdNlUpdate {
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
     const float4 w = ld4g(nlw, idx), ic = ld4g(inv_c2, idx);
-    const float4 d = dq ? ld4g(dq, idx) : make_float4(0.f, 0.f, 0.f, 0.f);  // null: grad.f is in Nl
+    const float4 d = dq ? ld4g(dq, idx) : make_float4(0.f, 0.f, 0.f, 0.f);  // null (always): grad.f is in Nl
     const float nl[4] = {w.x - d.x, w.y - d.y, w.z - d.z, w.w - d.w};
     float nlo[4] = {nl[0], nl[1], nl[2], nl[3]};
     if (!first) {
@@ -402,11 +402,10 @@ struct LdNlUpdate {
     pf[1] = point(nl[1], nlo[1], p01.y, o01.y, ic.y, pn[1], idx + 1);
     pf[2] = point(nl[2], nlo[2], p23.x, o23.x, ic.z, pn[2], idx + 2);
     pf[3] = point(nl[3], nlo[3], p23.y, o23.y, ic.w, pn[3], idx + 3);
-    *reinterpret_cast<double2*>(psiq_old + idx) = p01;
-    *reinterpret_cast<double2*>(psiq_old + idx + 2) = p23;
-    *reinterpret_cast<double2*>(psiq + idx) = make_double2(pn[0], pn[1]);
-    *reinterpret_cast<double2*>(psiq + idx + 2) = make_double2(pn[2], pn[3]);
-    st4v(nlq, idx, make_float4(nl[0], nl[1], nl[2], nl[3]));
+    // the new psiq over psiq_old: the engine then exchanges the two buffers (and Nl-hat's
+    // buffer with Nl_old's, Nl = Nl-hat here), so neither old value is copied
+    *reinterpret_cast<double2*>(psiq_old + idx) = make_double2(pn[0], pn[1]);
+    *reinterpret_cast<double2*>(psiq_old + idx + 2) = make_double2(pn[2], pn[3]);
     const float4 out = make_float4(pf[0], pf[1], pf[2], pf[3]);
     st4v(psiqf, idx, out);
     return out;
@@ -417,9 +416,10 @@ struct LdNlUpdate {
 // Pointwise kernels
 // ---------------------------------------------------------------------------------
 
-// The mixed engine's CN/AB2 update (REF:2177-2190), four points per thread: psiq_old <-
-// psiq, psiq <- psiq + FP32 increment, Nl_old <- Nl, and the FP32 copy psiqf of the new
-// psiq that the inverse transform then reads.
+// The mixed engine's CN/AB2 update (REF:2177-2190), four points per thread: the new psiq
+// = psiq + FP32 increment into psiq_old's buffer, and its FP32 copy psiqf that the inverse
+// transform then reads. The engine exchanges psiq_ with psiq_old_ and nlw_ with nlq_
+// after the step (StepEngine::run_graph): psiq_old <- psiq and Nl_old <- Nl without copies.
 static __global__ void __launch_bounds__(256) nl_update_kernel(long long n, LdNlUpdate lu) {
   const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
   if (idx < n) (void)lu.quad(0, 0, 0, idx);
@@ -1024,6 +1024,17 @@ template <typename T> class StepEngine : public EngineBase {
   // the step's input psi, and no diagnostics run
   int run_graph(bool relax, bool first, bool diag, bool vsol, bool tape = false);
   int graph_of(bool relax, bool first, bool diag, bool vsol, bool tape, cudaGraphExec_t* out, int* key);
+  // Mixed engine: after each step the CN update's ping-pong buffers change roles (the new
+  // psiq is in psiq_old_'s buffer, the step's Nl-hat in nlw_'s); pp_ is the parity of the
+  // assignment, part of the graph key (a captured graph holds the pointers).
+  int pp_ = 0;
+  void swap_pp() {
+    if constexpr (!std::is_same<T, double>::value) {
+      std::swap(psiq_, psiq_old_);
+      std::swap(nlw_, nlq_);
+      pp_ ^= 1;
+    }
+  }
   bool cap_vsol_ = false;  // vsol flag of the variant being captured
   bool cap_tape_ = false;  // tape flag of the variant being captured
   int64_t diag_step_ = -1;  // nLoop of the last step that ran the diagnostics
@@ -1320,7 +1331,7 @@ template <typename T>
 int StepEngine<T>::graph_of(bool relax, bool first, bool diag, bool vsol, bool tape, cudaGraphExec_t* out,
                             int* key_out) {
   vsol = vsol || diag || tape;
-  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0) | (vsol ? 8 : 0) | (tape ? 16 : 0);
+  const int key = (relax ? 1 : 0) | (first ? 2 : 0) | (diag ? 4 : 0) | (vsol ? 8 : 0) | (tape ? 16 : 0) | (pp_ << 5);
   auto it = graphs_.find(key);
   if (it == graphs_.end()) {
     cudaGraph_t graph = nullptr;
@@ -1360,6 +1371,7 @@ template <typename T> int StepEngine<T>::run_graph(bool relax, bool first, bool 
   SWC_TRY(graph_of(relax, first, diag, vsol, tape, &exec, &key));
   SWC_CK(cudaGraphLaunch(exec, stream_));
   last_launches_ += graph_kernels_[key];
+  swap_pp();
   return SWC_OK;
 }
 
@@ -1373,9 +1385,20 @@ template <typename T> int StepEngine<T>::prepare() {
   SWC_CK(cudaSetDevice(p_.device));
   cudaGraphExec_t exec;
   int key;
-  for (int relax = 0; relax < 2; ++relax)
-    for (int first = 0; first < 2; ++first)
-      for (int v = 0; v < 3; ++v) SWC_TRY(graph_of(relax, first, v == 2, v >= 1, false, &exec, &key));
+  // both assignments of the ping-pong buffers (the mixed engine alternates them)
+  const int npp = std::is_same<T, double>::value ? 1 : 2;
+  for (int q = 0; q < npp; ++q) {
+    for (int relax = 0; relax < 2; ++relax)
+      for (int first = 0; first < 2; ++first)
+        for (int v = 0; v < 3; ++v) {
+          const int rc = graph_of(relax, first, v == 2, v >= 1, false, &exec, &key);
+          if (rc) {
+            if (q) swap_pp();
+            return rc;
+          }
+        }
+    if (npp > 1) swap_pp();
+  }
   return SWC_OK;
 }
 
