@@ -352,19 +352,21 @@ template <typename T> struct StNlUpdate {
 
 // Mixed engine: the CN/AB2 update of psiq (REF:2170-2190) in increment form, applied by
 // nl_update_kernel before the first pass of psi = DCT-III^3 psiq_new (REF:2194-2197),
-// which reads the FP32 copy psiqf. It reads the Nl transform's output nl_hat, writes
-// psiq_old, psiq, nlq and psiqf. The increment (0.5 (psiq - psiq_old) + dt/2 scale (3 Nl - Nl_old))/C2,
-// a small correction built from FP32 data, is formed in FP32 with an FP32 1/C2 table;
-// FP64 holds the state: two FP64 adds per point (psiq - psiq_old, psiq + increment),
-// conversions on the integer pipes. The modes the table flags (a negative entry: the
-// k = 0 mode, and the modes near the q0 shell whose denominator differs from 1.5 by
-// less than FP32 resolves, inv_c2_kernel) form the increment in FP64 with C2
-// evaluated in FP64.
+// which reads the FP32 copy psiqf. It reads the Nl transform's output nl_hat and Nl_old,
+// psiq and psiq_old, writes the new psiq and psiqf. The increment (0.5 (psiq - psiq_old)
+// + dt/2 scale (3 Nl - Nl_old))/C2, a small correction built from FP32 data, is formed in
+// FP32 with 1/C2 evaluated in FP32 from the FP32 wavenumbers (C2 = 1.5 - dt rho_m
+// (ep - alpha (q0^2 - |q|^2)^2), REF:957-958); FP64 holds the state: two FP64 adds per
+// point (psiq - psiq_old, psiq + increment), conversions on the integer pipes. The k = 0
+// mode and the modes near the q0 shell whose denominator differs from 1.5 by less than
+// FP32 resolves (|1.5 - C2| < 8 eps_32 1.5) form the increment in FP64 with C2 evaluated
+// in FP64.
 struct LdNlUpdate {
   const float *nlw, *dq;
   const float* nlq;
   double *psiq, *psiq_old;
-  const float* inv_c2;
+  const float *qxf, *qyf, *qzf;  // FP32 wavenumbers
+  float q02f, epf, alphaf, dtrmf;
   float* psiqf;
   float srcs;  // dt/2 scale
   int first;
@@ -384,9 +386,24 @@ struct LdNlUpdate {
     pn = pq + widen_f32(inc);
     return narrow_f64(pn);
   }
+  // 1/C2 of mode (i, j, k), negative for the modes that take the FP64 increment
+  __device__ __forceinline__ float inv_c2(float mq2, bool zero_mode) const {
+    const float s = q02f - mq2;
+    const float damp = dtrmf * (epf - alphaf * (s * s));
+    const float ic = 1.0f / (1.5f - damp);
+    return (zero_mode || -damp < 8.0f * 1.1920928955078125e-7f * 1.5f) ? -ic : ic;
+  }
   // four consecutive elements; each read, then written, by this thread only
   __device__ __forceinline__ float4 quad(int, int, int, long long idx) const {
-    const float4 w = ld4g(nlw, idx), ic = ld4g(inv_c2, idx);
+    const float4 w = ld4g(nlw, idx);
+    float4 ic;
+    {
+      const int k = (int)(idx & (g.nz - 1)), j = (int)((idx >> g.lz) & (g.ny - 1)), i = (int)(idx >> (g.ly + g.lz));
+      const float qxy = qxf[i] * qxf[i] + qyf[j] * qyf[j];
+      const float4 qz = ld4g(qzf, k);
+      ic = make_float4(inv_c2(qxy + qz.x * qz.x, idx == 0), inv_c2(qxy + qz.y * qz.y, false),
+                       inv_c2(qxy + qz.z * qz.z, false), inv_c2(qxy + qz.w * qz.w, false));
+    }
     const float4 d = dq ? ld4g(dq, idx) : make_float4(0.f, 0.f, 0.f, 0.f);  // null (always): grad.f is in Nl
     const float nl[4] = {w.x - d.x, w.y - d.y, w.z - d.z, w.w - d.w};
     float nlo[4] = {nl[0], nl[1], nl[2], nl[3]};
@@ -587,25 +604,6 @@ template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S
   fx.store(a.fx, idx); fy.store(a.fy, idx); fz.store(a.fz, idx);
 }
 
-// 1/C2 per spectral mode (REF:957-958), evaluated in FP64 and stored in FP32, built
-// once for the mixed engine. C2 = 1.5 - dt rho_m aLin > 1.5, so the sign is free to flag
-// the modes whose update the mixed engine keeps in FP64 (negative entry): the k = 0
-// mode (the mean) and the modes near the q0 shell, where dt rho_m |aLin| -- what sets
-// the semi-implicit damping, C2 - 1.5 -- is below 8 FP32 ulps of 1.5 (9.5e-7).
-static __global__ void __launch_bounds__(256) inv_c2_kernel(Grid g, const double* qx, const double* qy, const double* qz,
-                                                     double ep, double alpha, double q02, double dt, double rho_m,
-                                                     float* out) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.ng) return;
-  const int k = (int)(idx & (g.nz - 1)), j = (int)((idx >> g.lz) & (g.ny - 1)), i = (int)(idx >> (g.ly + g.lz));
-  const double mq2 = qx[i] * qx[i] + qy[j] * qy[j] + qz[k] * qz[k];
-  const double s = q02 - mq2;
-  const double aLin = ep - alpha * (s * s);
-  const double damp = dt * rho_m * aLin;
-  const float ic = (float)(1.0 / (1.5 - damp));
-  const bool fp64 = idx == 0 || -damp < 8.0 * 1.1920928955078125e-7 * 1.5;
-  out[idx] = fp64 ? -ic : ic;
-}
 
 // S8 + S9 (REF:1479-1974): Stokes solve on the three staggered grids, spectral.
 template <typename T> struct StokesArgs {
@@ -1066,7 +1064,7 @@ template <typename T> class StepEngine : public EngineBase {
   double *partial_ = nullptr, *dsum_ = nullptr;
   // mixed engine: FP32 1/C2 per spectral mode, FP32 f_rho, and FP32 copies of the FP64
   // state kept where the state is written: rhof = rho - rho_off_, psiqf = psiq
-  T *inv_c2f_ = nullptr, *frhot_ = nullptr, *rhof_ = nullptr, *psiqf_ = nullptr;
+  T *frhot_ = nullptr, *rhof_ = nullptr, *psiqf_ = nullptr;
   double rho_off_ = 0;  // (rho_0 + rho_s)/2 in the mixed engine, 0 in the FP64 engine
   int refresh_copies(int frho_mode);
   int diag_blocks_ = 0;
@@ -1217,14 +1215,11 @@ template <typename T> int StepEngine<T>::init() {
   for (double** b : dbufs) SWC_CK(cudaMemsetAsync(*b, 0, nd, stream_));
   SWC_CK(cudaStreamSynchronize(stream_));
   if constexpr (!std::is_same<T, double>::value) {
-    T** mbufs[] = {&inv_c2f_, &frhot_, &rhof_, &psiqf_};
+    T** mbufs[] = {&frhot_, &rhof_, &psiqf_};
     for (T** b : mbufs) {
       if ((rc = dalloc(nt, (void**)b))) return rc;
       SWC_CK(cudaMemsetAsync(*b, 0, nt, stream_));
     }
-    inv_c2_kernel<<<(unsigned)((g_.ng + 255) / 256), 256, 0, stream_>>>(
-        g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt, rho_m_, inv_c2f_);
-    SWC_CK(cudaGetLastError());
     SWC_CK(cudaStreamSynchronize(stream_));
   }
   int sms = 0;

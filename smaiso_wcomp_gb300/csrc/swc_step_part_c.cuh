@@ -58,7 +58,8 @@ template <typename T> int StepEngine<T>::enqueue_part_c(bool relax, bool first, 
     SWC_TRY((pass<K_C2, 0>(LP{nlw_}, SP{nlw_})));
     // the CN update as a full-occupancy pointwise kernel (it writes the FP32 copy psiqf of
     // the new psiq), then a plain TMA-fed pass from that copy
-    LdNlUpdate lu{nlw_, nullptr, nlq_, psiq_, psiq_old_, inv_c2f_, psiqf_, (float)(p_.dt / 2 * scale_), first ? 1 : 0,
+    LdNlUpdate lu{nlw_, nullptr, nlq_, psiq_, psiq_old_, vq_[0], vq_[1], vq_[2], (float)(p_.q0 * p_.q0), (float)p_.ep,
+                  (float)p_.alpha, (float)(p_.dt * rho_m_), psiqf_, (float)(p_.dt / 2 * scale_), first ? 1 : 0,
                   g_, vqd_[0], vqd_[1], vqd_[2], p_.ep, p_.alpha, p_.q0 * p_.q0, p_.dt * rho_m_,
                   p_.dt / 2 * scale_};
     nl_update_kernel<<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(g_.ng, lu);
