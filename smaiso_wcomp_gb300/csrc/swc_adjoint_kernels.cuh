@@ -345,7 +345,9 @@ __global__ void __launch_bounds__(256) adj_nl_kernel(Grid g, AdjNlArgs<T> a) {
 // with bar vsol = bar v-hat_a, bar virr = bar v-hat_a + Vq_a[o_a+1] bar divv-hat(o + e_a);
 // zero elsewhere. nu_bar += bar vsol (-vsol/nu) + bar virr (-2 virr/(lam + 2nu)).
 // bar v-hat_a and bar divv-hat arrive without the output weights of the transposed
-// transforms that made them (wv[a], wdq), which are applied here.
+// transforms that made them (wv[a], wdq), which are applied here. Inputs and outputs are
+// distinct arrays: the inputs take the read-only load path; FP32 forms 1/|q|^2 with the
+// approximate reciprocal (rcp_pos), FP64 with the division.
 template <typename T> struct AdjStokesArgs {
   const T *bvx, *bvy, *bvz, *bdq, *vsx_, *vsy_, *vsz_, *vix, *viy, *viz;
   T *bdotx, *bdoty, *bdotz, *bsx, *bsy, *bsz, *bgx, *bgy, *bgz;
@@ -366,15 +368,15 @@ __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs<
     V4<T> d = V4<T>::zero(), sd = V4<T>::zero(), fp = V4<T>::zero();
     if (i < g.nx - 1) {
       V4<T> bv, dq, vs, vi;
-      bv.load(a.bvx, x);
-      dq.load(a.bdq, x + sx);
-      vs.load(a.vsx_, x);
-      vi.load(a.vix, x);
+      bv.loadg(a.bvx, x);
+      dq.loadg(a.bdq, x + sx);
+      vs.loadg(a.vsx_, x);
+      vi.loadg(a.vix, x);
       const T s_ = a.vsx[i], q1 = a.vqx[i + 1], gxy = a.gsx[i] * a.gqy[j];
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const T qzk = a.vqz[k + e];
-        const T inv = T(1.0) / (s_ * s_ + qyj * qyj + qzk * qzk);
+        const T inv = rcp_pos(s_ * s_ + qyj * qyj + qzk * qzk);
         const T CM1 = a.scale * inv, CM2 = s_ * inv, G = gxy * a.gqz[k + e];
         const T bvs = bv.v[e] * a.wvx.at(g, i, j, k + e);
         const T bvi = bvs + q1 * (dq.v[e] * a.wdq.at(g, i + 1, j, k + e));
@@ -391,14 +393,14 @@ __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs<
     V4<T> dz = V4<T>::zero(), sdz = V4<T>::zero(), fpz = V4<T>::zero();
     if (j < g.ny - 1) {
       V4<T> bvy, dqy, vsy, viy, bvz, dqz, vsz, viz;
-      bvy.load(a.bvy, x);
-      dqy.load(a.bdq, x + sy);
-      vsy.load(a.vsy_, x);
-      viy.load(a.viy, x);
-      bvz.load(a.bvz, x);
-      dqz.load(a.bdq, x);
-      vsz.load(a.vsz_, x);
-      viz.load(a.viz, x);
+      bvy.loadg(a.bvy, x);
+      dqy.loadg(a.bdq, x + sy);
+      vsy.loadg(a.vsy_, x);
+      viy.loadg(a.viy, x);
+      bvz.loadg(a.bvz, x);
+      dqz.loadg(a.bdq, x);
+      vsz.loadg(a.vsz_, x);
+      viz.loadg(a.viz, x);
       const T dq4 = (k + 4 < g.nz) ? a.bdq[x + 4] : T(0.0);
       const T dzs[4] = {dqz.v[1], dqz.v[2], dqz.v[3], dq4};  // bar divv-hat at k + e + 1
       const T sy_ = a.vsy[j], qy1 = a.vqy[j + 1];
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs<
         if (k + e >= g.nz - 1) continue;
         const T qzk = a.vqz[k + e];
         {
-          const T inv = T(1.0) / (qxi * qxi + sy_ * sy_ + qzk * qzk);
+          const T inv = rcp_pos(qxi * qxi + sy_ * sy_ + qzk * qzk);
           const T CM1 = a.scale * inv, CM2 = sy_ * inv, G = a.gqx[i] * a.gsy[j] * a.gqz[k + e];
           const T bvs = bvy.v[e] * a.wvy.at(g, i, j, k + e);
           const T bvi = bvs + qy1 * (dqy.v[e] * a.wdq.at(g, i, j + 1, k + e));
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(256) adj_stokes1_kernel(Grid g, AdjStokesArgs<
         }
         {
           const T s_ = a.vsz[k + e];
-          const T inv = T(1.0) / (qxi * qxi + qyj * qyj + s_ * s_);
+          const T inv = rcp_pos(qxi * qxi + qyj * qyj + s_ * s_);
           const T CM1 = a.scale * inv, CM2 = s_ * inv;
           const bool q1 = (k + e == 0) && (j > 0) && (i % a.block != 0);  // REF:1932
           const T G = q1 ? (a.gqx[i] * a.gsy[j] * a.gqz[k + e]) : (a.gqx[i] * a.gqy[j] * a.gsz[k + e]);
@@ -597,35 +599,37 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
   if (pt4(g, p)) {
     const long long x = p.idx;
     const AdjScalars<T>& s = a.s;
-    V4<T> A, L, rho, lraw;
-    A.load(a.A, x);
-    L.load(a.L, x);
-    lraw.load(a.lapR, x);
+    V4<T> A, L, rho, lraw, rden;  // rden = 1/(A + 0.001), A >= 0; inputs on the read-only path
+    A.loadg(a.A, x);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) rden.v[e] = rcp_pos(A.v[e] + T(0.001));
+    L.loadg(a.L, x);
+    lraw.loadg(a.lapR, x);
     if (a.relax) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) rho.v[e] = s.rho0 + s.kp * A.v[e];
     } else {
-      rho.load(a.rho_in, x);
+      rho.loadg(a.rho_in, x);
     }
     // bmu1 = bS . gpsi, bc = bf . gpsi, bEn = bS . grho + rho bEr, EbE = E bEr
     V4<T> bSx, bSy, bSz, bmu1, bc, bEn, EbE;
-    bSx.load(a.bSx, x);
-    bSy.load(a.bSy, x);
-    bSz.load(a.bSz, x);
+    bSx.loadg(a.bSx, x);
+    bSy.loadg(a.bSy, x);
+    bSz.loadg(a.bSz, x);
     {
       V4<T> bfx, bfy, bfz, gx, gy, gz, mu1, c;
-      bfx.load(a.bfx, x);
-      bfy.load(a.bfy, x);
-      bfz.load(a.bfz, x);
-      gx.load(a.gpx, x);
-      gy.load(a.gpy, x);
-      gz.load(a.gpz, x);
+      bfx.loadg(a.bfx, x);
+      bfy.loadg(a.bfy, x);
+      bfz.loadg(a.bfz, x);
+      gx.loadg(a.gpx, x);
+      gy.loadg(a.gpy, x);
+      gz.loadg(a.gpz, x);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const T t = s.rho0 + s.kp * A.v[e], den = A.v[e] + T(0.001);
+        const T t = s.rho0 + s.kp * A.v[e];
         const T lapR = a.relax ? rho.v[e] * lraw.v[e] : lraw.v[e];
         mu1.v[e] = lapR + rho.v[e] * L.v[e];
-        c.v[e] = s.kp * s.zeta * (rho.v[e] - t) / den;
+        c.v[e] = s.kp * s.zeta * (rho.v[e] - t) * rden.v[e];
         bmu1.v[e] = bSx.v[e] * gx.v[e] + bSy.v[e] * gy.v[e] + bSz.v[e] * gz.v[e];
         bc.v[e] = bfx.v[e] * gx.v[e] + bfy.v[e] * gy.v[e] + bfz.v[e] * gz.v[e];
       }
@@ -642,10 +646,10 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
     }
     {
       V4<T> bEr, gx, gy, gz, E;
-      bEr.load(a.bE, x);
-      gx.load(a.grx, x);
-      gy.load(a.gry, x);
-      gz.load(a.grz, x);
+      bEr.loadg(a.bE, x);
+      gx.loadg(a.grx, x);
+      gy.loadg(a.gry, x);
+      gz.loadg(a.grz, x);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         E.v[e] = T(0.5) * (L.v[e] * L.v[e]);
@@ -665,25 +669,25 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
     }
     {
       V4<T> psi, bmu, bfg, oA, op, oR, ol, oL;
-      psi.load(a.psi, x);
-      bmu.load(a.bmu, x);
-      bfg.load(a.bfgrad, x);
+      psi.loadg(a.psi, x);
+      bmu.loadg(a.bmu, x);
+      bfg.loadg(a.bfgrad, x);
       oA.load(a.bA, x);
       op.load(a.bpsi, x);
       oR.load(a.bR, x);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const T Ae = A.v[e], Le = L.v[e], pe = psi.v[e], re = rho.v[e], bm = bmu.v[e], bf = bfg.v[e];
-        const T t = s.rho0 + s.kp * Ae, den = Ae + T(0.001);
+        const T t = s.rho0 + s.kp * Ae, rd = rden.v[e];
         const T p2 = pe * pe;
         const T P5 = Le - s.ep * pe - s.beta * (p2 * pe) + s.gamma * (p2 * p2 * pe);
         const T blap = bmu1.v[e] + bm;
-        T brho = Le * bmu1.v[e] + P5 * bm + EbE.v[e] + s.zeta * re * bf + (s.kp * s.zeta / den) * bc.v[e];
+        T brho = Le * bmu1.v[e] + P5 * bm + EbE.v[e] + s.zeta * re * bf + (s.kp * s.zeta * rd) * bc.v[e];
         oL.v[e] = re * bmu1.v[e] + re * bm + Le * bEn.v[e];
         op.v[e] += re * (-s.ep - T(3.0) * s.beta * p2 + T(5.0) * s.gamma * (p2 * p2)) * bm;
-        const T bt = -s.zeta * t * bf - (s.kp * s.zeta / den) * bc.v[e];
-        T bA = s.kp * bt + bc.v[e] * (-s.kp * s.zeta * (re - t) / (den * den));
-        T dkp = bt * Ae + bc.v[e] * s.zeta * (re - t) / den, drho0 = bt;
+        const T bt = -s.zeta * t * bf - (s.kp * s.zeta * rd) * bc.v[e];
+        T bA = s.kp * bt + bc.v[e] * (-s.kp * s.zeta * (re - t) * (rd * rd));
+        T dkp = bt * Ae + bc.v[e] * s.zeta * (re - t) * rd, drho0 = bt;
         acc[0] += bm * re * (-(p2 * pe));
         acc[1] += bm * re * (p2 * p2 * pe);
         if (a.relax) {
@@ -704,7 +708,7 @@ __global__ void __launch_bounds__(256) adj_s6_kernel(Grid g, AdjS6Args<T> a) {
       }
       if (a.ew != T(0.0)) {
         V4<T> rn;
-        rn.load(a.rho_new, x);
+        rn.loadg(a.rho_new, x);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           oL.v[e] += a.ew * rn.v[e] * L.v[e];
