@@ -589,8 +589,10 @@ __device__ __forceinline__ void pair_tables(const R2RTables<float>& tb, float4* 
 // entry the PC buffer holds, per kind and axis: x/y forward -> stage-1 output; z forward
 // -> the Makhoul-ordered z; x/y inverse -> the pre-processed, swapped Z; z inverse ->
 // the natural-order reals. Outputs go to global memory through `st`.
-// ZT (z forward kinds): the loader has already run the first stage, of radix R1/2, so
-// the forward FFT ends with one stage of radix 2 R2.
+// ZT (row-staged z passes): the loader has already run the first stage, of radix R1/2,
+// of the FFT that follows the load -- the forward FFT of the forward kinds, or the
+// inverse FFT (after the DCT-III pre-processing) of the inverse kinds -- so that FFT
+// ends with one stage of radix 2 R2.
 template <int N, int KIND, int AX, class StoreOp, class MulOp, bool ZT = false>
 __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int tj, int tid, PC* buf,
                                           const float4* sfft, const float2* spost, const float2* spre,
@@ -606,6 +608,7 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   static_assert(ZU * NT == LP * NQ && ZU % ZC == 0, "z units");
   float2* rb2 = reinterpret_cast<float2*>(buf);
   const int lineA = 2 * (pair0 + lp);
+  constexpr bool zt_inv = ZT && !fwd_in;  // inverse kinds: pre-processing and first stage done
   if constexpr (!xy && !ZT) {
     if constexpr (fwd_in) pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
     else pair_pre<N>(buf, spre, lp, tj);
@@ -638,7 +641,10 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   }
 
   // ---------------- inverse FFT ----------------
-  if constexpr (inv_out) {
+  if constexpr (zt_inv) {
+    static_assert(Cf::R3 == 1, "two-stage plan");
+    pair_stage<M, 2 * Cf::R2, R1 / 2, TPL, PP>(buf, sfft, lp, tj);
+  } else if constexpr (inv_out) {
     pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
     if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
     if constexpr (xy) {

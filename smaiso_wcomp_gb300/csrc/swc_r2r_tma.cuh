@@ -130,8 +130,9 @@ __device__ __forceinline__ void tma_issue_zrow(const float* zsrc, int t, uint32_
 
 // LMUL: a pointwise multiplier of the loaded values (LdMul); the z pass of the inverse
 // cosine kind applies it as it reads the staged tile, the other forms take NoMul only.
-// ZT: z pass of a forward kind with the row staging (tma_issue_zrow): each thread loads
-// the inputs of its two first-stage butterflies straight from the staged tile, and the
+// ZT: z pass with the row staging (tma_issue_zrow): each thread loads the inputs of its
+// two first-stage butterflies straight from the staged tile -- the Makhoul-ordered
+// elements (forward kinds) or the DCT-III pre-processed pairs (inverse kinds) -- and the
 // line-pair re-layout of the z tile is not needed.
 template <int N, int KIND, int AX, class StoreOp, class MulOp, class LMul, bool ZT = false>
 __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_constant__ CUtensorMap tmap,
@@ -148,7 +149,8 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   constexpr int ZU = (LP * NQ) / NT;
   constexpr bool load_mul = !std::is_same<LMul, NoMul<float>>::value;
   static_assert(!load_mul || (AX == 2 && KIND == K_C3), "load multiplier: z pass of the inverse cosine kind only");
-  static_assert(!ZT || (AX == 2 && fwd_in && !load_mul && Tc::ZROW && R1 % 2 == 0), "z row staging");
+  static_assert(!ZT || (AX == 2 && (fwd_in ? !load_mul : true) && Tc::ZROW && R1 % 2 == 0 && 2 * TPL * (R1 / 2) == M),
+                "z row staging");
   extern __shared__ __align__(128) unsigned char tma_smem[];
   const float* S = reinterpret_cast<const float*>(tma_smem);
   PC* buf = reinterpret_cast<PC*>(tma_smem + Tc::STAGE_BYTES);
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
     }
     const int pair0 = t * LP;
     // ---- staging tile -> PC buffer ----
-    if constexpr (ZT) {
+    if constexpr (ZT && fwd_in) {
       // First Stockham stage of radix R = R1/2 (2 TPL butterflies per line pair, elements
       // m = b + 2 TPL r), two butterflies per thread: b0 = tj and b1 = 2 TPL - 1 - tj. The
       // float4 a of a line holds z_a = (x_4a, x_4a+2) and z_(M-1-a) = (x_4a+3, x_4a+1)
@@ -217,6 +219,68 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
         v1[R - 1 - q] = pmake(make_float2(A0.w, B0.w), make_float2(A0.y, B0.y));
         v1[q] = pmake(make_float2(A1.x, B1.x), make_float2(A1.z, B1.z));
         v0[R - 1 - q] = pmake(make_float2(A1.w, B1.w), make_float2(A1.y, B1.y));
+      }
+      PDft<R>::run(v0);
+      PDft<R>::run(v1);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        buf[(b0 * R + r) * PP + lp] = v0[r];
+        buf[(b1 * R + r) * PP + lp] = v1[r];
+      }
+    } else if constexpr (ZT) {
+      // Inverse kinds. The DCT-III pre-processing (pair_pre_one) maps the reals at k,
+      // N-k, M-k, M+k to Z_k and Z_(M-k), and the first inverse-FFT stage of radix
+      // R = R1/2 runs on (im, re)-swapped Z over butterflies b (elements b + 2 TPL r).
+      // With b0 = tj, b1 = 2 TPL - tj (for tj = 0: b1 = TPL), both members of every
+      // pair k = b + 2 TPL r (r < R/2) belong to this thread's two butterflies: the
+      // partner M-k of a b0 element is element R-1-r of b1 and that of a b1 element is
+      // element R-1-r of b0 -- except for tj = 0, whose b0 = 0 holds the pairs
+      // (2 TPL r, M - 2 TPL r) and the middle mode M/2 (element R/2), and whose b1 = TPL
+      // pairs with itself. The reals come straight from the staged rows (line 2 lp at
+      // row lp, line 2 lp + 1 at row lp + LP); DST-III reads the line reversed; the load
+      // multiplier scales them as they are read.
+      constexpr int R = R1 / 2, TB = 2 * TPL, H = R / 2;
+      const bool t0 = tj == 0;
+      const int b0 = tj, b1 = t0 ? TPL : TB - tj;
+      const int la = 2 * (pair0 + lp);
+      const int li = la >> g.ly, lj = la & (g.ny - 1);
+      auto X = [&](int pos) -> float2 {  // real element pos of lines A and B
+        const int q = (KIND == K_S3) ? (N - 1 - pos) : pos;
+        float a = S[lp * Tc::ZPITCH + q], b = S[(lp + LP) * Tc::ZPITCH + q];
+        if constexpr (load_mul) {
+          a *= lmul(li, lj, q);
+          b *= lmul(li, lj + 1, q);
+        }
+        return make_float2(a, b);
+      };
+      auto pre = [&](int k, PC& z0, PC& z1) {  // k in [0, M/2): pswapped Z_k, Z_(M-k)
+        const float2 xnk = X(k == 0 ? 0 : N - k);
+        pair_pre_one(spre, M, k, X(k), k == 0 ? f2(0.f) : xnk, X(M - k), X(M + k), z0, z1);
+        z0 = pswap(z0);
+        z1 = pswap(z1);
+      };
+      PC v0[R], v1[R], A1[H], B1[H];
+#pragma unroll
+      for (int r = 0; r < H; ++r) {
+        pre(b0 + TB * r, v0[r], A1[r]);
+        pre(b1 + TB * r, v1[r], B1[r]);
+      }
+      PC mid;
+      {
+        const int k = M / 2;
+        const PC U = pmake(X(k), neg2(X(N - k)));
+        mid = pswap(pcomb(spre[2 * k], U, spre[2 * k + 1], U));
+      }
+      auto sel = [&](bool c, const PC& a, const PC& b) -> PC {
+        return pmake(make_float2(c ? a.re.x : b.re.x, c ? a.re.y : b.re.y),
+                     make_float2(c ? a.im.x : b.im.x, c ? a.im.y : b.im.y));
+      };
+#pragma unroll
+      for (int r = 0; r < H; ++r) {
+        // b0's upper elements R-1-r: partners of b1's pairs, or (tj = 0) of b0's own
+        // pairs r+1 and, for r = H-1, the middle mode
+        v0[R - 1 - r] = sel(t0, (r == H - 1) ? mid : A1[r + 1 < H ? r + 1 : 0], B1[r]);
+        v1[R - 1 - r] = sel(t0, B1[r], A1[r]);
       }
       PDft<R>::run(v0);
       PDft<R>::run(v1);
@@ -374,9 +438,10 @@ cudaError_t launch_tma_map(const Grid& g, const R2RTables<float>& tb, cudaStream
   return cudaGetLastError();
 }
 
-// Forward kinds along z take the row staging where the tile allows it (N = 256).
+// z passes take the row staging where the tile allows it (N = 256).
 template <int N, int KIND> constexpr bool zt_kind() {
-  return TmaCfg<N>::ZROW && (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
+  return TmaCfg<N>::ZROW && (KIND == K_C2 || KIND == K_S2 || KIND == K_FILT || KIND == K_DERIV ||
+                             KIND == K_DERIVT || KIND == K_C3 || KIND == K_S3);
 }
 
 template <int N, int KIND, int AX, class ST, class MUL, class LMUL = NoMul<float>>
@@ -384,7 +449,7 @@ cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t s
                        MUL mul, LMUL lmul = LMUL()) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
-  if constexpr (AX == 2 && zt_kind<N, KIND>() && std::is_same<LMUL, NoMul<float>>::value)
+  if constexpr (AX == 2 && zt_kind<N, KIND>())
     return launch_tma_map<N, KIND, AX, ST, MUL, LMUL, true>(g, tb, stream, map, src, st, mul, lmul);
   if constexpr (AX != 2) {
     const cudaError_t e = make_pass_map<N, AX>(g, src, &map);

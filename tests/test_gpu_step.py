@@ -149,19 +149,24 @@ def test_zero_state_fixed_point(lib):
 
 
 @pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
-def test_checkpoint_continuation_is_bitwise(lib, tmp_path, prec):
+@pytest.mark.parametrize("nsave", [3, 4])
+def test_checkpoint_continuation_is_bitwise(lib, tmp_path, prec, nsave):
+    """Save after nsave steps, continue, and continue a loaded copy: every field equal
+    bit for bit. After an odd number of steps the mixed engine's psiq / psiq_old and
+    Nl / Nl_old buffers have exchanged roles, while the loaded engine starts with the
+    first assignment."""
     p = abi.default_params(16, 16, 16, rho_0=0.8, divv_switch=3, precision=prec)
     psi, rho = ic.undulated_interface(p)
     path = os.path.join(tmp_path, "state.swc")
     with Engine(p) as e:
         e.set_state(psi, rho)
-        e.step(4)
+        e.step(nsave)
         e.save(path)
         e.step(5)
-        a = {f: e.field(f) for f in ("psi", "rho", "psiq", "nlq")}
+        a = {f: e.field(f) for f in ("psi", "rho", "psiq", "psiq_old", "nlq")}
     with Engine(p) as e2:
         e2.load(path)
-        assert e2.nloop == 4
+        assert e2.nloop == nsave
         e2.step(5)
         for f, v in a.items():
             assert np.array_equal(e2.field(f), v), f
