@@ -531,11 +531,11 @@ __device__ __forceinline__ void pair_post_store(const Grid& g, int lineA, const 
 // x/y inverse kinds: the last Stockham stage with both lines' outputs stored straight
 // to global memory (slot m holds the swapped z_m: v_2m = .im, v_2m+1 = .re, v_q at
 // position mk_pos(q), negated at odd positions for DST-III).
-template <int N, int KIND, int AX, class ST>
+template <int N, int KIND, int AX, class ST, int R = PairCfg<N>::RL, int NS = PairCfg<N>::NSL>
 __device__ __forceinline__ void pair_last_store(const Grid& g, int lineA, const PC* buf, const float4* tw, int lp,
                                                 int tj, const ST& st) {
   using Cf = PairCfg<N>;
-  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL, R = Cf::RL, NS = Cf::NSL;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL;
   constexpr int NB = M / R, PER = NB / TPL, STRIDE = M / R, TSTEP = M / (NS * R);
   PC v[PER][R];
 #pragma unroll
@@ -570,6 +570,129 @@ __device__ __forceinline__ void pair_last_store(const Grid& g, int lineA, const 
   }
 }
 
+
+// ---- paired radix-8 stages next to the Makhoul steps (x/y passes, N = 256) ---------------
+// In the 16 x 8 plan the stage adjacent to the post-processing (the last forward stage)
+// and, in the 8 x 16 plan, the stage adjacent to the pre-processing (the first inverse
+// stage) have 16 radix-8 butterflies per line pair, two per thread. Thread tj takes
+// b0 = tj and b1 = 16 - tj (tj = 0: 0 and 8). Butterfly b covers the modes b + 16 r, and
+// the Makhoul pair (k, M-k) of k = b0 + 16 r (r < 4) is element r of b0 with element
+// 7 - r of b1, that of k = b1 + 16 r element r of b1 with element 7 - r of b0; for
+// tj = 0, b0 = 0 pairs its own elements r and 8 - r (element 0 alone, element 4 the
+// middle mode M/2) and b1 = 8 its elements r and 7 - r. So the DCT-II post-processing
+// after the last forward stage, and the DCT-III pre-processing before the first inverse
+// stage, run in the registers of one thread.
+template <int N> struct PairR8 {
+  using Cf = PairCfg<N>;
+  static constexpr bool ok = N == 256 && Cf::R3 == 1 && Cf::R2 == 8 && Cf::M == 16 * Cf::TPL && Cf::R1 == 16;
+};
+__device__ __forceinline__ int pr_b1(int tj, int tpl) { return tj == 0 ? tpl : 2 * tpl - tj; }
+__device__ __forceinline__ PC psel(bool c, const PC& a, const PC& b) {
+  return pmake(make_float2(c ? a.re.x : b.re.x, c ? a.re.y : b.re.y),
+               make_float2(c ? a.im.x : b.im.x, c ? a.im.y : b.im.y));
+}
+
+// Last forward stage (radix 8, span M/8) of butterfly b from the buffer: its outputs at
+// modes b + 16 r in o[r].
+template <int M, int PP>
+__device__ __forceinline__ void pr_last_fwd(const PC* buf, const float4* tw, int lp, int b, PC (&o)[8]) {
+  constexpr int R = 8, STRIDE = M / R;  // span M/8 = 16 > b, twiddle step 1
+#pragma unroll
+  for (int r = 0; r < R; ++r) o[r] = buf[(b + r * STRIDE) * PP + lp];
+#pragma unroll
+  for (int r = 1; r < R; ++r) o[r] = pmul(o[r], tw[r * b]);
+  PDft<R>::run(o);
+}
+
+// The FFT outputs z_k and z_(M-k) of the pair k = b + 16 r from the outputs of b0 (o0)
+// and b1 (o1): second == false for k in b0, true for k in b1.
+template <bool second>
+__device__ __forceinline__ void pr_pair_in(bool t0, int r, const PC (&o0)[8], const PC (&o1)[8], PC& zk, PC& zm) {
+  if constexpr (!second) {
+    zk = o0[r];
+    zm = psel(t0, o0[(8 - r) & 7], o1[7 - r]);
+  } else {
+    zk = o1[r];
+    zm = psel(t0, o1[7 - r], o0[7 - r]);
+  }
+}
+
+// The first inverse stage (radix 8) of b0 and b1 from the pre-processed (im, re)-swapped
+// Z of the pairs: Zk0[r], Zm0[r] of k = b0 + 16 r, Zk1[r], Zm1[r] of k = b1 + 16 r, and
+// (tj = 0) the middle mode; written to the buffer as rows b 8 + r after a barrier (the
+// caller's reads of the buffer end there) and a second one after.
+template <int M, int PP>
+__device__ __forceinline__ void pr_first_inv(PC* buf, bool t0, int lp, int b0, int b1, const PC (&Zk0)[4],
+                                             const PC (&Zm0)[4], const PC (&Zk1)[4], const PC (&Zm1)[4],
+                                             const PC& mid) {
+  PC v0[8], v1[8];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    v0[r] = Zk0[r];
+    v1[r] = Zk1[r];
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    v0[7 - r] = psel(t0, (r == 3) ? mid : Zm0[(r + 1) & 3], Zm1[r]);
+    v1[7 - r] = psel(t0, Zm1[r], Zm0[r]);
+  }
+  PDft<8>::run(v0);
+  PDft<8>::run(v1);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    buf[(b0 * 8 + r) * PP + lp] = v0[r];
+    buf[(b1 * 8 + r) * PP + lp] = v1[r];
+  }
+  __syncthreads();
+}
+
+// x/y forward kinds: the last forward stage in registers, the post-processing, and both
+// lines' outputs stored straight to global memory.
+template <int N, int KIND, int AX, class ST>
+__device__ __forceinline__ void pr_post_store(const Grid& g, int lineA, const PC* buf, const float4* tw,
+                                              const float2* post, int lp, int tj, const ST& st) {
+  using Cf = PairCfg<N>;
+  constexpr int M = Cf::M, PP = Cf::PP, TPL = Cf::TPL;
+  const bool t0 = tj == 0;
+  const int b0 = tj, b1 = pr_b1(tj, TPL);
+  PC o0[8], o1[8];
+  pr_last_fwd<M, PP>(buf, tw, lp, b0, o0);
+  pr_last_fwd<M, PP>(buf, tw, lp, b1, o1);
+  auto put = [&](int pos, float2 v) {
+    const int o = (KIND == K_S2) ? (N - 1 - pos) : pos;
+    int i, j, k;
+    long long idx;
+    xy_coords<AX>(g, lineA, o, i, j, k, idx);
+    st_ab<AX>(g, st, i, j, k, idx, v);
+  };
+  auto one = [&](int k, const PC& zk, const PC& zm) {
+    const PC u0 = pcomb(post[2 * k], zk, post[2 * k + 1], zm);
+    const int km = M - k;
+    const PC u1 = pcomb(post[2 * km], zm, post[2 * km + 1], zk);
+    put(k, u0.re);
+    put(M - k, u1.re);
+    if (k > 0) {
+      put(N - k, neg2(u0.im));
+      put(M + k, neg2(u1.im));
+    }
+  };
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    PC zk, zm;
+    pr_pair_in<false>(t0, r, o0, o1, zk, zm);
+    one(b0 + 16 * r, zk, zm);
+    pr_pair_in<true>(t0, r, o0, o1, zk, zm);
+    one(b1 + 16 * r, zk, zm);
+  }
+  if (t0) {
+    const PC z = o0[4];
+    const PC u = pcomb(post[M], z, post[M + 1], z);
+    put(M / 2, u.re);
+    put(M + M / 2, neg2(u.im));
+  }
+}
+
 // Shared-memory twiddle tables: stage twiddles as {c, c, s, s}, Makhoul tables as is.
 template <int N, bool FWD, bool INV>
 __device__ __forceinline__ void pair_tables(const R2RTables<float>& tb, float4* sfft, float2* spost, float2* spre,
@@ -593,7 +716,12 @@ __device__ __forceinline__ void pair_tables(const R2RTables<float>& tb, float4* 
 // of the FFT that follows the load -- the forward FFT of the forward kinds, or the
 // inverse FFT (after the DCT-III pre-processing) of the inverse kinds -- so that FFT
 // ends with one stage of radix 2 R2.
-template <int N, int KIND, int AX, class StoreOp, class MulOp, bool ZT = false>
+// PR (x/y passes of the plain kinds, PairR8<N>::ok): the stages next to the Makhoul
+// steps are paired radix-8 ones -- the forward kinds' last stage and post-processing
+// run in registers (pr_post_store); for the inverse kinds the loader has run the
+// pre-processing and the first inverse stage (pr_first_inv), and the last inverse stage
+// is radix 16.
+template <int N, int KIND, int AX, class StoreOp, class MulOp, bool ZT = false, bool PR = false>
 __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int tj, int tid, PC* buf,
                                           const float4* sfft, const float2* spost, const float2* spre,
                                           const StoreOp& st, const MulOp& mul) {
@@ -609,6 +737,9 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   float2* rb2 = reinterpret_cast<float2*>(buf);
   const int lineA = 2 * (pair0 + lp);
   constexpr bool zt_inv = ZT && !fwd_in;  // inverse kinds: pre-processing and first stage done
+  constexpr bool pr = PR && xy;
+  static_assert(!pr || (PairR8<N>::ok && KIND != K_FILT && KIND != K_DERIV && KIND != K_DERIVT),
+                "paired radix-8 stages");
   if constexpr (!xy && !ZT) {
     if constexpr (fwd_in) pair_stage<M, R1, 1, TPL, PP>(buf, sfft, lp, tj);
     else pair_pre<N>(buf, spre, lp, tj);
@@ -619,12 +750,13 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
     if constexpr (ZT) {
       static_assert(Cf::R3 == 1, "two-stage plan");
       pair_stage<M, 2 * Cf::R2, R1 / 2, TPL, PP>(buf, sfft, lp, tj);
-    } else {
+    } else if constexpr (!pr) {
       pair_stage<M, Cf::R2, R1, TPL, PP>(buf, sfft, lp, tj);
       if constexpr (Cf::R3 > 1) pair_stage<M, Cf::R3, R1 * Cf::R2, TPL, PP>(buf, sfft, lp, tj);
     }
     if constexpr (xy && KIND != K_FILT && KIND != K_DERIV && KIND != K_DERIVT) {
-      pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
+      if constexpr (pr) pr_post_store<N, KIND, AX>(g, lineA, buf, sfft, spost, lp, tj, st);
+      else pair_post_store<N, KIND, AX>(g, lineA, buf, spost, lp, tj, st);
       return;
     }
     if constexpr (KIND == K_DERIV) {
@@ -641,7 +773,10 @@ __device__ __forceinline__ void pair_tail(const Grid& g, int pair0, int lp, int 
   }
 
   // ---------------- inverse FFT ----------------
-  if constexpr (zt_inv) {
+  if constexpr (pr && inv_out) {
+    pair_last_store<N, KIND, AX, StoreOp, 2 * Cf::R2, R1 / 2>(g, lineA, buf, sfft, lp, tj, st);
+    return;
+  } else if constexpr (zt_inv) {
     static_assert(Cf::R3 == 1, "two-stage plan");
     pair_stage<M, 2 * Cf::R2, R1 / 2, TPL, PP>(buf, sfft, lp, tj);
   } else if constexpr (inv_out) {

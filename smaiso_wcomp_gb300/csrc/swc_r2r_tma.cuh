@@ -151,6 +151,11 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   static_assert(!load_mul || (AX == 2 && KIND == K_C3), "load multiplier: z pass of the inverse cosine kind only");
   static_assert(!ZT || (AX == 2 && (fwd_in ? !load_mul : true) && Tc::ZROW && R1 % 2 == 0 && 2 * TPL * (R1 / 2) == M),
                 "z row staging");
+  // paired radix-8 stages next to the Makhoul steps: the plain kinds with plain stores (a
+  // store functor that loads, StLpsiRhoL, runs slower inside the radix-16 last stage, 68 us
+  // against 45; for the kinds with two transforms the paired middle measured no faster)
+  constexpr bool PR = xy && PairR8<N>::ok && std::is_same<StoreOp, StPlain<float, float>>::value &&
+                      !(KIND == K_FILT || KIND == K_DERIV || KIND == K_DERIVT);
   extern __shared__ __align__(128) unsigned char tma_smem[];
   const float* S = reinterpret_cast<const float*>(tma_smem);
   PC* buf = reinterpret_cast<PC*>(tma_smem + Tc::STAGE_BYTES);
@@ -307,6 +312,34 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
       PDft<R1>::run(v);
 #pragma unroll
       for (int r = 0; r < R1; ++r) buf[(tj * R1 + r) * PP + lp] = v[r];
+    } else if constexpr (xy && PR) {
+      // inverse kinds, x/y: the pre-processing of the pairs of this thread's two radix-8
+      // butterflies (pr_* in swc_r2r_pair.cuh) from the staged rows, and the first
+      // inverse stage, in registers
+      const float2* S2 = reinterpret_cast<const float2*>(S);
+      auto X = [&](int r) -> float2 { return S2[((KIND == K_S3) ? (N - 1 - r) : r) * LP + lp]; };
+      const bool t0 = tj == 0;
+      const int b0 = tj, b1 = pr_b1(tj, TPL);
+      auto one = [&](int k, PC& Zk, PC& Zm) {
+        const float2 xnk = X(k == 0 ? 0 : N - k);
+        PC z0, z1;
+        pair_pre_one(spre, M, k, X(k), k == 0 ? f2(0.f) : xnk, X(M - k), X(M + k), z0, z1);
+        Zk = pswap(z0);
+        Zm = pswap(z1);
+      };
+      PC Zk0[4], Zm0[4], Zk1[4], Zm1[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        one(b0 + 16 * r, Zk0[r], Zm0[r]);
+        one(b1 + 16 * r, Zk1[r], Zm1[r]);
+      }
+      PC mid;
+      {
+        const int k = M / 2;
+        const PC U = pmake(X(k), neg2(X(N - k)));
+        mid = pswap(pcomb(spre[2 * k], U, spre[2 * k + 1], U));
+      }
+      pr_first_inv<M, PP>(buf, t0, lp, b0, b1, Zk0, Zm0, Zk1, Zm1, mid);
     } else if constexpr (xy) {
       const float2* S2 = reinterpret_cast<const float2*>(S);
       constexpr int NP = (M / 2) / TPL;
@@ -385,7 +418,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
       if (tid == 0 && t + (int)gridDim.x < ntiles)
         tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx);
     }
-    pair_tail<N, KIND, AX, StoreOp, MulOp, ZT>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
+    pair_tail<N, KIND, AX, StoreOp, MulOp, ZT, PR>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
   }
 }
 
