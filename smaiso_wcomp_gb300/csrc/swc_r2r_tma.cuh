@@ -1,18 +1,20 @@
 // swc_r2r_tma.cuh -- the FP32 two-line r2r pass fed by the Tensor Memory Accelerator.
 //
-// Persistent CTAs walk tiles of 2 LP lines. Each tile arrives in shared memory by one
-// asynchronous copy -- a tiled tensor-map load (cp.async.bulk.tensor.3d) for x/y
-// passes, whose tile is N rows of 2 LP adjacent lines, and a contiguous bulk copy
-// (cp.async.bulk) for z passes, whose 2 LP lines are one block of memory -- issued by
-// one thread as soon as the previous tile has left the staging buffer, so the DRAM
-// read of tile t+1 overlaps the transform and the stores of tile t. Completion is an
+// Persistent CTAs walk tiles of 2 LP lines. Each tile arrives in shared memory by
+// asynchronous copies -- a tiled tensor-map load (cp.async.bulk.tensor.3d) for x/y
+// passes, whose tile is N rows of 2 LP adjacent lines; for z passes, whose 2 LP lines
+// are one block of memory, one contiguous bulk copy (cp.async.bulk), or at N = 256 one
+// bulk copy per line into padded rows (row staging, tma_issue_zrow) -- issued as soon as
+// the previous tile has left the staging buffer, so the DRAM read of tile t+1 overlaps
+// the transform and the stores of tile t. Completion is an
 // mbarrier transaction count; every wait is bounded (tables' max_polls): a wait that
 // runs out sets the tables' status flag and the CTA returns after one more bounded wait
 // for its copy in flight. Test support: wait_extra_tx makes every wait expect more bytes
 // than its copy delivers, so the wait runs out while the copy itself is a valid one; on
 // the way out those extra bytes are credited (mbarrier.complete_tx), so the second wait
 // ends when the valid copy has landed.
-// Used for plain FP32 loads (LdPlain<float, float>), any store/multiplier.
+// Used for plain FP32 loads (LdPlain<float, float>, or times a multiplier applied to the
+// staged tile: LdMul), any store/multiplier.
 #pragma once
 
 #include <cuda.h>
