@@ -53,9 +53,10 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed FP64 steps (default: steps/5, >= 10)")
     ap.add_argument("--cpu-sample-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--accuracy-steps", type=int, default=2000,
+    ap.add_argument("--accuracy-steps", type=int, default=None,
                     help="run both engines this many steps from the initial state and report the mixed "
-                         "engine's psi/rho/mass/energy error against the FP64 engine (0 skips it)")
+                         "engine's psi/rho/mass/energy error against the FP64 engine (0 skips it; default "
+                         "the workload's run length: 2000 steps undulated, 1000 dislocations)")
     ap.add_argument("--grad-steps", type=int, default=40,
                     help="steps of the 128^3 FP64 adjoint timing (gradient/forward ratio); 0 skips it")
     ap.add_argument("--workload", choices=["undulated", "dislocations", "adjoint128", "adjoint256", "adjoint256_fp64"],
@@ -558,7 +559,8 @@ def main():
                                              args.energy_lambda)), flush=True)
         return
     if args.workload == "dislocations":
-        print(json.dumps(dislocation_run(args.steps, args.warmup, args.accuracy_steps or 50, local)), flush=True)
+        acc_n = 1000 if args.accuracy_steps is None else (args.accuracy_steps or 50)
+        print(json.dumps(dislocation_run(args.steps, args.warmup, acc_n, local)), flush=True)
         return
     if args.only == "pass":
         ms, per_axis, alg = pass_roofline(abi.SWC_PREC_MIXED, reps=args.steps)
@@ -602,6 +604,8 @@ def main():
     sps_64 = replicas.job_throughput(k64, ms_64 * 1e-3, 1)
     # accuracy: both engines from the initial state through the relax phase and on
     # (spec bar: psi within 1e-5 of the FP64 engine after 2000 steps)
+    if args.accuracy_steps is None:
+        args.accuracy_steps = 2000
     acc = accuracy_run(args.accuracy_steps, local) if args.accuracy_steps > 0 else None
 
     psi_h = pinned((N, N, N))
