@@ -131,6 +131,7 @@ int swc_r2r_plan_create(int nx, int ny, int nz, int kx, int ky, int kz, int prec
     p->td[a].status = p->status;
     p->tf[a].status = p->status;
     p->kind[a] = kinds[a];
+    p->tf[a].rev = a == 1;  // the y pass walks down the i planes the z pass before it left in L2
     const int rc = precision == SWC_PREC_FP64 ? upload_tables<double>(p, a, dims[a], &p->td[a])
                                               : upload_tables<float>(p, a, dims[a], &p->tf[a]);
     if (rc) { swc_r2r_plan_destroy(p); return rc; }

@@ -34,6 +34,7 @@ template <typename T> struct R2RTables {
   int* status;          // device flag set to 1 when a pass's bounded wait runs out (or null)
   int max_polls = 1 << 22;  // bound of each wait of the TMA-fed pass (mbarrier polls)
   int wait_extra_tx = 0;    // test support: extra bytes each tile wait expects (0 = none)
+  int rev = 0;              // TMA-fed pass: walk the tiles from the last one down
 };
 
 struct PassShape {

@@ -169,13 +169,19 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
   const int tid = threadIdx.x;
   const int lp = tid & (LP - 1), tj = tid >> Cf::LOG2LP;
 
+  // tb.rev: the tiles in reverse order (for z and y passes, the i planes from the last
+  // down), so that a pass can start on the planes the kernel before it touched last
+  const bool rev = tb.rev != 0;
+  auto tile_of = [ntiles, rev](int t) { return rev ? ntiles - 1 - t : t; };
   pair_tables<N, fwd_in, inv_out>(tb, sfft, spost, spre, tid);
   if (tid == 0) mbar_init(bar, 1);
   if constexpr (ZT) {
     __syncthreads();  // the barrier initialised before warp 0 starts the copies
-    if (tid < 32 && (int)blockIdx.x < ntiles) tma_issue_zrow<N>(zsrc, blockIdx.x, sdst, bar, tb.wait_extra_tx, tid);
+    if (tid < 32 && (int)blockIdx.x < ntiles)
+      tma_issue_zrow<N>(zsrc, tile_of(blockIdx.x), sdst, bar, tb.wait_extra_tx, tid);
   } else {
-    if (tid == 0 && (int)blockIdx.x < ntiles) tma_issue<N, AX>(g, &tmap, zsrc, blockIdx.x, sdst, bar, tb.wait_extra_tx);
+    if (tid == 0 && (int)blockIdx.x < ntiles)
+      tma_issue<N, AX>(g, &tmap, zsrc, tile_of(blockIdx.x), sdst, bar, tb.wait_extra_tx);
   }
   __syncthreads();
 
@@ -197,7 +203,7 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
       }
       return;
     }
-    const int pair0 = t * LP;
+    const int pair0 = tile_of(t) * LP;
     // ---- staging tile -> PC buffer ----
     if constexpr (ZT && fwd_in) {
       // First Stockham stage of radix R = R1/2 (2 TPL butterflies per line pair, elements
@@ -415,10 +421,10 @@ __global__ void __launch_bounds__(PairCfg<N>::NT) r2r_tma_kernel(const __grid_co
     __syncthreads();  // the staging tile is free: start the next one
     if constexpr (ZT) {
       if (tid < 32 && t + (int)gridDim.x < ntiles)
-        tma_issue_zrow<N>(zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx, tid);
+        tma_issue_zrow<N>(zsrc, tile_of(t + gridDim.x), sdst, bar, tb.wait_extra_tx, tid);
     } else {
       if (tid == 0 && t + (int)gridDim.x < ntiles)
-        tma_issue<N, AX>(g, &tmap, zsrc, t + gridDim.x, sdst, bar, tb.wait_extra_tx);
+        tma_issue<N, AX>(g, &tmap, zsrc, tile_of(t + gridDim.x), sdst, bar, tb.wait_extra_tx);
     }
     pair_tail<N, KIND, AX, StoreOp, MulOp, ZT, PR>(g, pair0, lp, tj, tid, buf, sfft, spost, spre, st, mul);
   }

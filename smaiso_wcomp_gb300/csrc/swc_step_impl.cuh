@@ -1002,6 +1002,7 @@ template <typename T> class StepEngine : public EngineBase {
   // launch one axis pass on stream_, data type U (T, or double for the FP64 pre-loop)
   template <typename U, int KIND, int AX, class LD, class ST, class MUL = NoMul<U>>
   int passU(LD ld, ST st, MUL mul = MUL());
+  template <typename U, int KIND, int AX, class LD> int plane_order();
   template <int KIND, int AX, class LD, class ST, class MUL = NoMul<T>>
   int pass(LD ld, ST st, MUL mul = MUL()) {
     return passU<T, KIND, AX, LD, ST, MUL>(ld, st, mul);
@@ -1072,6 +1073,10 @@ template <typename T> class StepEngine : public EngineBase {
   std::map<int, int64_t> graph_kernels_;  // kernel nodes per captured variant
   int64_t last_launches_ = 0;
   int64_t launches_ = 0;  // running count while a variant is captured
+  // plane order of the passes (plane_order): launches_ after the last pass, and whether
+  // the last z or y pass walked its planes downward
+  int64_t plane_mark_ = -1;
+  bool plane_desc_ = false;
   bool have_state_ = false;
   bool have_vsol_ = false;
   bool vsol_pending_ = false;  // spectral v_sol of the last step not yet in real space
@@ -1235,9 +1240,32 @@ template <typename T> int StepEngine<T>::init() {
 template <typename T>
 template <typename U, int KIND, int AX, class LD, class ST, class MUL>
 int StepEngine<T>::passU(LD ld, ST st, MUL mul) {
-  SWC_CK((launch_pass<U, KIND, AX, LD, ST, MUL>(g_, tabs<U>(AX), stream_, ld, st, mul)));
+  R2RTables<U> tb = tabs<U>(AX);
+  tb.rev = plane_order<U, KIND, AX, LD>();
+  SWC_CK((launch_pass<U, KIND, AX, LD, ST, MUL>(g_, tb, stream_, ld, st, mul)));
   ++launches_;
   return SWC_OK;
+}
+
+// Tile order of the next pass (R2RTables::rev). z and y passes walk the field by i planes;
+// each runs opposite to the plane-walking kernel before it, so that it starts on the
+// planes that kernel touched last, which are still in L2 (a z pass after a y pass, a y
+// pass after a z pass, a z pass after a pointwise kernel). x passes touch every i plane
+// at each step of their walk (over j) and leave the order as it was; the pointwise
+// kernels and the passes of the other forms walk upward. Only the TMA-fed form takes
+// the order; the results do not depend on it.
+template <typename T>
+template <typename U, int KIND, int AX, class LD>
+int StepEngine<T>::plane_order() {
+  const bool chain = launches_ == plane_mark_;  // no other kernel since the last pass
+  plane_mark_ = launches_ + 1;
+  if (!chain) plane_desc_ = false;
+  if constexpr (AX == 0) {
+    return 0;
+  } else {
+    plane_desc_ = tma_fed_form<U, KIND, AX, LD>() && !plane_desc_;
+    return plane_desc_ ? 1 : 0;
+  }
 }
 
 #define SWC_TRY(x)         \
@@ -1332,6 +1360,7 @@ int StepEngine<T>::graph_of(bool relax, bool first, bool diag, bool vsol, bool t
     cudaGraph_t graph = nullptr;
     SWC_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     launches_ = 0;
+    plane_mark_ = -1;
     cap_vsol_ = vsol;
     cap_tape_ = tape;
     int rc = enqueue_step(relax, first, diag);

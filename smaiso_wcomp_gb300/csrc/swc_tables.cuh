@@ -127,6 +127,13 @@ cudaError_t launch_pair(const Grid& g, const R2RTables<float>& tb, cudaStream_t 
 template <class F> struct IsLdMul : std::false_type {};
 template <class M> struct IsLdMul<LdMul<M>> : std::true_type {};
 
+// Whether launch_pass runs a pass in the TMA-fed form (on the shapes that form supports):
+// the one form that honours R2RTables::rev.
+template <typename U, int KIND, int AX, class LD> constexpr bool tma_fed_form() {
+  return std::is_same<U, float>::value &&
+         (std::is_same<LD, LdPlain<float, float>>::value || (IsLdMul<LD>::value && AX == 2 && KIND == K_C3));
+}
+
 // Launch one axis pass on `stream` (in place or out of place per the functors): for
 // line lengths 64..512 the compile-time kernels (FP32: two lines per thread with packed
 // arithmetic; FP64: one line per thread group), the runtime one otherwise.
