@@ -633,7 +633,8 @@ template <typename T> struct StokesArgs {
 // (REF:1932):
 //   div v-hat = scale/((lambda + 2 nu) |q|^2) sum_valid q_a^2 (fg + D G_a / |q|^2).
 // FP32: three 256-thread blocks per SM (80 registers; uncapped it takes 95 and runs
-// two blocks, measured slower at 256^3: 172 us against 132 us per launch).
+// two blocks, measured slower at 256^3: 172 us against 132 us per launch; capped at 64
+// for four blocks it spills 68 bytes a thread and the 256^3 step is 6 us slower).
 template <typename T, bool DIVV>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) stokes_kernel(Grid g, StokesArgs<T> a) {
   const int idx = 4 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
