@@ -442,6 +442,15 @@ static __global__ void __launch_bounds__(256) nl_update_kernel(long long n, LdNl
   if (idx < n) (void)lu.quad(0, 0, 0, idx);
 }
 
+// |psi, grad psi| (REF:1262-1266) of the mixed engine, four points per thread, ahead of
+// the TMA-fed z pass that starts its transform: the 5-field streaming step runs at the
+// HBM rate on its own, and the z pass, walking down the planes, starts on the ones
+// still in L2.
+static __global__ void __launch_bounds__(256) amp_kernel(long long n, LdAmp<float> la, float* out) {
+  const long long idx = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (idx < n) st4v(out, idx, la.quad(0, 0, 0, idx));
+}
+
 __device__ __forceinline__ void decompose(const Grid& g, long long idx, int& i, int& j, int& k) {
   k = (int)(idx & (g.nz - 1));
   j = (int)((idx >> g.lz) & (g.ny - 1));
@@ -1312,7 +1321,15 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
     }
   }
   // S3 (REF:1254-1289): amplitude, Gaussian filter
-  SWC_TRY((pass<K_C2, 2>(LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
+  if constexpr (std::is_same<T, float>::value) {
+    amp_kernel<<<(unsigned)((g_.ng / 4 + 255) / 256), 256, 0, stream_>>>(
+        g_.ng, LdAmp<float>{psi_, gp_[0], gp_[1], gp_[2], (float)(p_.q0 * p_.q0)}, amp_f_);
+    SWC_CK(cudaGetLastError());
+    ++launches_;
+    SWC_TRY((pass<K_C2, 2>(LP{amp_f_}, SP{amp_f_})));
+  } else {
+    SWC_TRY((pass<K_C2, 2>(LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
+  }
   SWC_TRY((pass<K_C2, 1>(LP{amp_f_}, SP{amp_f_})));
   SWC_TRY((pass<K_FILT, 0>(LP{amp_f_}, SP{amp_f_}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
   SWC_TRY((pass<K_C3, 1>(LP{amp_f_}, SP{amp_f_})));
