@@ -490,13 +490,15 @@ cudaError_t launch_tma(const Grid& g, const R2RTables<float>& tb, cudaStream_t s
                        MUL mul, LMUL lmul = LMUL()) {
   CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
-  if constexpr (AX == 2 && zt_kind<N, KIND>())
+  if constexpr (AX == 2 && zt_kind<N, KIND>()) {
     return launch_tma_map<N, KIND, AX, ST, MUL, LMUL, true>(g, tb, stream, map, src, st, mul, lmul);
-  if constexpr (AX != 2) {
-    const cudaError_t e = make_pass_map<N, AX>(g, src, &map);
-    if (e != cudaSuccess) return e;
+  } else {  // (an else branch, so that the row-staged kinds instantiate no second z kernel)
+    if constexpr (AX != 2) {
+      const cudaError_t e = make_pass_map<N, AX>(g, src, &map);
+      if (e != cudaSuccess) return e;
+    }
+    return launch_tma_map<N, KIND, AX, ST, MUL, LMUL, false>(g, tb, stream, map, src, st, mul, lmul);
   }
-  return launch_tma_map<N, KIND, AX, ST, MUL, LMUL, false>(g, tb, stream, map, src, st, mul, lmul);
 }
 
 }  // namespace swc
