@@ -178,17 +178,10 @@ __global__ void __launch_bounds__(256) adj_cn_kernel(Grid g, const T* qx, const 
       const T aLin = s.ep - s.alpha * (sq * sq);
       const T C1 = T(2.0) - s.dt * s.rho_m * aLin, C2 = T(1.5) - s.dt * s.rho_m * aLin;
       const T b = bq.v[e];
-      if constexpr (sizeof(T) == 8) {  // the FP64 adjoint keeps its divisions
-        T bnl = T(3.0) * h / C2 * b + nlo.v[e];
-        if (first) bnl += -h / C2 * b;  // REF:2170-2172: Nl_old = Nl at nLoop == 1
-        nl.v[e] = bnl;
-        nlo.v[e] = first ? T(0.0) : -h / C2 * b;
-        bq.v[e] = C1 / C2 * b + qo.v[e];
-        qo.v[e] = -T(0.5) / C2 * b;
-        // dC1/dalpha = dC2/dalpha = dt rho_m sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
-        da[0] += b * s.dt * s.rho_m * sq * sq * (q0.v[e] - q1.v[e]) / C2;
-      } else {  // FP32: one reciprocal
-        const T r = T(1.0) / C2, hb = h * r * b;
+      {  // one reciprocal of C2 (FP64: rcp_f64's Newton-Raphson one)
+        // REF:2170-2172: Nl_old = Nl at nLoop == 1; dC1/dalpha = dC2/dalpha = dt rho_m
+        // sq^2  =>  dQ'/dalpha = dt rho_m sq^2 (Q - Q') / C2
+        const T r = div_nr(T(1.0), C2), hb = h * r * b;
         T bnl = T(3.0) * hb + nlo.v[e];
         if (first) bnl -= hb;
         nl.v[e] = bnl;
@@ -284,14 +277,24 @@ __global__ void __launch_bounds__(256) adj_nl_kernel(Grid g, AdjNlArgs<T> a) {
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const T den = A.v[e] + T(0.001);
-        const T cp = s.kp * s.zeta / den;
         const T t2 = rn.v[e] - s.rho0 - s.kp * A.v[e];
+        T cp, t2dd, t2d;  // kp zeta / den, t2 / den^2, t2 / den
+        if constexpr (sizeof(T) == 8) {  // one Newton-Raphson reciprocal (rcp_f64)
+          const T rd = rcp_f64(den);
+          cp = s.kp * s.zeta * rd;
+          t2d = t2 * rd;
+          t2dd = t2d * rd;
+        } else {
+          cp = s.kp * s.zeta / den;
+          t2dd = t2 / (den * den);
+          t2d = t2 / den;
+        }
         const T pb = psi.v[e] * b.v[e];
         brp.v[e] = bR.v[e] + cp * psi.v[e] * b.v[e];  // bar rho'
         o.v[e] = -b.v[e];
-        oA.v[e] = pb * (-s.kp * s.zeta * t2 / (den * den) - cp * s.kp);
+        oA.v[e] = pb * (-s.kp * s.zeta * t2dd - cp * s.kp);
         op.v[e] = cp * t2 * b.v[e];
-        acc[0] += pb * (s.zeta * t2 / den - cp * A.v[e]);
+        acc[0] += pb * (s.zeta * t2d - cp * A.v[e]);
         acc[1] += -b.v[e] * psi.v[e] * cp;
       }
       o.store(a.bmu, x);

@@ -8,7 +8,8 @@
 // pipes do at full rate. Zeros are handled too; subnormal, infinite and NaN operands
 // (never met on the engine's hot paths) take the hardware conversion, so the result
 // is always the one the cast gives: exact for widening, round-to-nearest-even for
-// narrowing. Host builds (the unit test) use the same arithmetic through memcpy.
+// narrowing. Host builds (the unit test) use the same arithmetic through memcpy. The
+// FP64 reciprocal at the end builds on them.
 #pragma once
 
 #include <stdint.h>
@@ -109,6 +110,45 @@ SWC_HD float narrow_f64(double x) {
   }
   if ((hi & 0x7fffffffu) == 0u && lo == 0u) return f32_from_bits(hi);  // +-0
   return narrow_slow(x);
+}
+
+// 1/x in FP64 by Newton-Raphson iteration for the reciprocal, r <- r + r (1 - x r):
+// each step squares the seed's relative error, and the error term 1 - x r and the
+// update are one fused multiply-add each. From a seed within 2^-20 of 1/x, two steps
+// leave FP64's own rounding (within an ulp of 1/x): four FP64 FMAs.
+SWC_HD double rcp_f64_from_seed(double x, double r) {
+#if defined(__CUDA_ARCH__)
+  double t = __fma_rn(-x, r, 1.0);
+  r = __fma_rn(r, t, r);
+  t = __fma_rn(-x, r, 1.0);
+  return __fma_rn(r, t, r);
+#else
+  double t = __builtin_fma(-x, r, 1.0);
+  r = __builtin_fma(r, t, r);
+  t = __builtin_fma(-x, r, 1.0);
+  return __builtin_fma(r, t, r);
+#endif
+}
+
+// 1/x for an FP64 x of either sign whose magnitude lies within FP32's normal range
+// with a margin (2^-124 .. 2^124): the seed is FP32's reciprocal of x narrowed on the
+// integer pipes (on the device the approximate reciprocal, within 2 ulp: about 2^-21
+// with the narrowing), widened back, then two Newton-Raphson steps. Other x (zero,
+// tiny, huge, non-finite) take the IEEE division. On GB300, whose FP64 pipe runs at
+// 1/64 of the FP32 rate, this is fewer FP64 operations than the IEEE division's
+// sequence; the result is within an ulp of it, not always the same bits.
+SWC_HD double rcp_f64(double x) {
+  uint32_t hi, lo;
+  f64_words(x, hi, lo);
+  const uint32_t e = (hi >> 20) & 0x7ffu;
+  if (e < 899u || e > 1147u) return 1.0 / x;
+  const float xf = narrow_f64(x);
+#if defined(__CUDA_ARCH__)
+  const float sf = __fdividef(1.0f, xf);
+#else
+  const float sf = 1.0f / xf;
+#endif
+  return rcp_f64_from_seed(x, widen_f32(sf));
 }
 
 }  // namespace swc

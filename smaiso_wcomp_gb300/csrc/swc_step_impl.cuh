@@ -54,6 +54,14 @@ namespace swc {
 // Multiplier of the derivative pass (shifted spectral derivative onto the sine grid
 // of `axis`, REF:1166-1221): -c Vs[c_axis], c = 1/(2 n_axis); the pass itself applies
 // the shift and the zero on the last mode.
+// a / b of the FP64 terms by rcp_f64's Newton-Raphson reciprocal (1/b within an ulp,
+// the quotient within 1.5 ulp of the division, in fewer FP64 operations on GB300's slow
+// FP64 pipe); FP32 keeps the division.
+template <typename T> __device__ __forceinline__ T div_nr(T a, T b) {
+  if constexpr (sizeof(T) == 8) return a * rcp_f64(b);
+  else return a / b;
+}
+
 template <typename T> struct MulDeriv {
   const T* vs;
   T c;
@@ -200,7 +208,7 @@ template <typename T> struct LdNl {
     rho[idx] = rn;
     frho[idx] = (double)srho;
     const T a = amp[idx];
-    const T c = ((T)kp * (T)zeta / (a + (T)0.001)) * ((T)rn - (T)rho0 - (T)kp * a) * psi[idx];
+    const T c = div_nr((T)kp * (T)zeta, a + (T)0.001) * ((T)rn - (T)rho0 - (T)kp * a) * psi[idx];
     return -mu[idx] + c - ux * gpx[idx] - uy * gpy[idx] - uz * gpz[idx];
   }
   // four consecutive elements with 16-byte loads / stores (FP32 fields, FP64 rho, f_rho);
@@ -340,7 +348,7 @@ template <typename T> struct StNlUpdate {
     auto upd = [&](double cz, double p, double po, double src) {
       const double s = q02 - (ab + cz * cz);
       const double aLin = ep - alpha * (s * s);
-      return ((2.0 - dt * rho_m * aLin) * p - 0.5 * po + src) / (1.5 - dt * rho_m * aLin);
+      return div_nr((2.0 - dt * rho_m * aLin) * p - 0.5 * po + src, 1.5 - dt * rho_m * aLin);
     };
     const double pn0 = upd(qz[k], pq.x, pqo.x, s0);
     const double pn1 = upd(qz[k + 1], pq.y, pqo.y, s1);
@@ -539,9 +547,10 @@ template <typename T> struct V4 {
 template <typename T> __device__ __forceinline__ T ldg1(const T* p) { return __ldg(p); }
 // 1/x for x a positive normal number (|q|^2 of a nonzero mode). FP32: __fdividef's
 // approximate reciprocal (within 2 ulp), without the special-case path of the
-// correctly rounded division; FP64: the division itself.
+// correctly rounded division; FP64: rcp_f64's Newton-Raphson reciprocal (within an ulp
+// of the division, in fewer FP64 operations: csrc/swc_fpconv.h).
 __device__ __forceinline__ float rcp_pos(float x) { return __fdividef(1.0f, x); }
-__device__ __forceinline__ double rcp_pos(double x) { return 1.0 / x; }
+__device__ __forceinline__ double rcp_pos(double x) { return rcp_f64(x); }
 
 // Four consecutive points per thread (n^3 is a multiple of 4: every extent is >= 4).
 // The mixed engine takes its FP32 density from rhof + off and touches the FP64 rho
@@ -597,7 +606,7 @@ template <typename T> __global__ void __launch_bounds__(256) s6_kernel(Grid g, S
     const T p2 = p * p;
     mu.v[c] = lapR.v[c] + rr * (Lc - ep * p - beta * (p2 * p) + gam * (p2 * p2 * p));
     ener.v[c] = rr * E;
-    const T cc = kp * zeta * (rr - rho0 - kp * Ac) / (Ac + (T)0.001);
+    const T cc = div_nr(kp * zeta * (rr - rho0 - kp * Ac), Ac + (T)0.001);
     fx.v[c] = cc * gpx.v[c];
     fy.v[c] = cc * gpy.v[c];
     fz.v[c] = cc * gpz.v[c];

@@ -20,3 +20,17 @@ def test_conversions_match_casts(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "mismatches 0" in r.stdout
+
+
+def test_fp64_reciprocal_within_an_ulp(tmp_path):
+    """rcp_f64, the FP64 engine's Newton-Raphson reciprocal: within one ulp of the IEEE
+    division from seeds 2^-20 off, and the division itself outside its range."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    exe = os.path.join(tmp_path, "rcp_check")
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", CSRC, os.path.join(HERE, "rcp_check.cpp"),
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "rcp mismatches 0" in r.stdout
