@@ -95,6 +95,18 @@ template <typename T> struct MulGauss {
   __device__ __forceinline__ T operator()(int i, int j, int k) const { return scale * gx[i] * gy[j] * gz[k]; }
 };
 
+// One axis's factor of that product, times a constant: the filter pass along axis AX
+// of the mixed engine's separable Gaussian (the three one-axis filter passes multiply
+// out to MulGauss: the DCT-III DCT-II pairs give 2n per axis, 8 N^3 in all, which the
+// scale of the last one cancels).
+template <typename T, int AX> struct MulAxis {
+  const T* g;
+  T scale;
+  __device__ __forceinline__ T operator()(int i, int j, int k) const {
+    return scale * g[AX == 0 ? i : (AX == 1 ? j : k)];
+  }
+};
+
 // -scale * |q|^2 (REF:1333-1334).
 template <typename T> struct MulLap {
   const T *qx, *qy, *qz;
@@ -1335,14 +1347,17 @@ template <typename T> int StepEngine<T>::enqueue_part_a(bool relax, bool first, 
         g_.ng, LdAmp<float>{psi_, gp_[0], gp_[1], gp_[2], (float)(p_.q0 * p_.q0)}, amp_f_);
     SWC_CK(cudaGetLastError());
     ++launches_;
-    SWC_TRY((pass<K_C2, 2>(LP{amp_f_}, SP{amp_f_})));
+    // the Gaussian is a product of per-axis factors: three one-axis filter passes
+    SWC_TRY((pass<K_FILT, 2>(LP{amp_f_}, SP{amp_f_}, MulAxis<T, 2>{gq_[2], (T)1})));
+    SWC_TRY((pass<K_FILT, 1>(LP{amp_f_}, SP{amp_f_}, MulAxis<T, 1>{gq_[1], (T)1})));
+    SWC_TRY((pass<K_FILT, 0>(LP{amp_f_}, SP{amp_f_}, MulAxis<T, 0>{gq_[0], (T)scale_})));
   } else {
     SWC_TRY((pass<K_C2, 2>(LdAmp<T>{psi_, gp_[0], gp_[1], gp_[2], (T)(p_.q0 * p_.q0)}, SP{amp_f_})));
+    SWC_TRY((pass<K_C2, 1>(LP{amp_f_}, SP{amp_f_})));
+    SWC_TRY((pass<K_FILT, 0>(LP{amp_f_}, SP{amp_f_}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
+    SWC_TRY((pass<K_C3, 1>(LP{amp_f_}, SP{amp_f_})));
+    SWC_TRY((pass<K_C3, 2>(LP{amp_f_}, SP{amp_f_})));
   }
-  SWC_TRY((pass<K_C2, 1>(LP{amp_f_}, SP{amp_f_})));
-  SWC_TRY((pass<K_FILT, 0>(LP{amp_f_}, SP{amp_f_}, MulGauss<T>{gq_[0], gq_[1], gq_[2], (T)scale_})));
-  SWC_TRY((pass<K_C3, 1>(LP{amp_f_}, SP{amp_f_})));
-  SWC_TRY((pass<K_C3, 2>(LP{amp_f_}, SP{amp_f_})));
   // S4 (REF:1293-1308): dfDlapPsi
   const T alpha = (T)p_.alpha, q02 = (T)(p_.q0 * p_.q0);
   if constexpr (std::is_same<T, double>::value) {
