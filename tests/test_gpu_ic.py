@@ -98,17 +98,26 @@ def test_set_state_ic_band_matches_reference_run(lib):
 @pytest.mark.parametrize("prec", [abi.SWC_PREC_FP64, abi.SWC_PREC_MIXED])
 def test_set_state_ic_matches_host_state(lib, prec):
     """swc_set_state_ic and swc_set_state from the host generator's arrays start the same
-    run: the fields after 3 steps agree to the initial states' rounding."""
+    run. The device and the host evaluate the initial formula separately, so the two FP64
+    states differ in their last bits; the FP64 engine keeps them that close (1e-12 after
+    3 steps). The mixed engine narrows FP64 values to FP32 every step, and where two values
+    that differ in their last bits round to neighbouring FP32 numbers the runs part at
+    FP32 rounding (2.5e-8 in psi after 3 steps here): it is held to 1e-6. Two runs from the
+    same start are bit for bit equal in both engines."""
     p = abi.default_params(64, 32, 64, rho_0=0.8, divv_switch=2, precision=prec)
     hpsi, hrho = ic.undulated_interface(p)
-    with Engine(p) as a, Engine(p) as b:
+    tol = 1e-12 if prec == abi.SWC_PREC_FP64 else 1e-6
+    with Engine(p) as a, Engine(p) as b, Engine(p) as c:
         a.set_state(hpsi, hrho)
         b.set_state_ic(abi.SWC_IC_UNDULATED)
+        c.set_state_ic(abi.SWC_IC_UNDULATED)
         a.step(3)
         b.step(3)
+        c.step(3)
         for f in ("psi", "rho", "psiq", "amp"):
             x, y = a.field(f), b.field(f)
-            assert np.linalg.norm(x - y) <= 1e-12 * np.linalg.norm(x), f
+            assert np.linalg.norm(x - y) <= tol * np.linalg.norm(x), f
+            assert np.array_equal(y, c.field(f)), f
 
 
 def test_bad_initial_condition_is_rejected(lib):
