@@ -41,3 +41,27 @@ def test_forward_inverse_pairs(oracle_mod, n):
     for f, b in ((0, 1), (2, 3)):
         y = oracle_mod.r2r1d(oracle_mod.r2r1d(x, f), b)
         np.testing.assert_allclose(y, 2 * n * x, rtol=0, atol=1e-13 * n)
+
+
+def test_separable_gaussian_filter(oracle_mod):
+    """The mixed engine's Gaussian amplitude filter as three one-axis filter passes (along
+    z, y, x: DCT-II along the axis, that axis's factor, DCT-III; the scale 1/(8 N^3) in
+    the last) equals the reference's 3D form DCT-III^3(scale g_x g_y g_z DCT-II^3 A)
+    (REF:1271-1289): each DCT-III DCT-II pair along an axis gives 2n."""
+    shape = (8, 4, 16)
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal(shape)
+    g = [np.exp(-1.57 ** 2 * 2 * (np.pi * np.arange(n) / (0.7 * n)) ** 2) for n in shape]
+    scale = 0.125 / np.prod(shape)
+    G = scale * g[0][:, None, None] * g[1][None, :, None] * g[2][None, None, :]
+    ref = oracle_mod.r2r3d(G * oracle_mod.r2r3d(a, (0, 0, 0)), (1, 1, 1))
+
+    def filt(x, axis, factor):
+        y = np.apply_along_axis(lambda v: oracle_mod.r2r1d(v, 0), axis, x)
+        sh = [1, 1, 1]
+        sh[axis] = -1
+        y = y * factor.reshape(sh)
+        return np.apply_along_axis(lambda v: oracle_mod.r2r1d(v, 1), axis, y)
+
+    out = filt(filt(filt(a, 2, g[2]), 1, g[1]), 0, scale * g[0])
+    np.testing.assert_allclose(out, ref, rtol=0, atol=1e-13 * np.max(np.abs(ref)))
